@@ -1,0 +1,193 @@
+/* mpsft-gb300: C ABI of a GB300 (sm_103a) implementation of the Matrix
+ * Pencil Sparse Fourier Transform recovery loop of jiaweichiu/mpsft.
+ *
+ * Every entry point returns an int status (MPSFT_OK = 0). Nothing aborts: the
+ * reference's glog CHECKs become status codes, and mpsft_last_error() gives the
+ * message of the last failure on a context. All sizes are plain integers and
+ * all buffers plain pointers; complex arrays are interleaved (re, im).
+ *
+ * Threading: one context per host thread. A context owns one CUDA stream
+ * (or borrows the caller's, mpsft_ctx_set_stream) and its work buffers.
+ *
+ * Reference interfaces replaced (file:line in jiaweichiu/mpsft):
+ *   mpsft_bin_in_time   BinInTime::Run         src/binner.h:30-41, src/binner.cc:394-521
+ *   mpsft_bin_in_freq   BinInFreq::Run         src/binner.h:123-133, src/binner.cc:565-591
+ *   mpsft_mat_pencil    MatPencil              src/freqid.h:28, src/freqid.cc:27-48
+ *   mpsft_iterate       Iterate                src/iterate.h:65, src/iterate.cc:80-176
+ *   mpsft_solve         Demo1::Run             src/demo1.h:39, src/demo1.cc:36-59
+ *   mpsft_solve_batched (no counterpart: many Demo1::Run solves in one launch sequence)
+ *   mpsft_window_*      Window                 src/window.h:25-55, src/window.cc:28-81
+ *   mpsft_rng_*         RandomSeed/RandomInt32 src/base.h:61-62, src/base.cc:52-53
+ *   mpsft_num_bits      NumBits                src/iterate.cc:30-42
+ */
+#ifndef MPSFT_GB300_H_
+#define MPSFT_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  MPSFT_OK = 0,
+  MPSFT_ERR_INVALID = 1,       /* bad argument (even bins, trials even, ...)  */
+  MPSFT_ERR_UNSUPPORTED_N = 2, /* n must be prime or a power of two           */
+  MPSFT_ERR_CUDA = 3,          /* a CUDA runtime call failed                  */
+  MPSFT_ERR_CAPACITY = 4,      /* found-mode table or output buffer too small */
+  MPSFT_ERR_ITER_CAP = 5,      /* iteration cap reached before the stop rule  */
+  MPSFT_ERR_NONFINITE = 6,     /* NaN or Inf met in the bins                  */
+  MPSFT_ERR_NOMEM = 7          /* device allocation failed                    */
+};
+
+/* ---- element types and precisions -------------------------------------- */
+enum { MPSFT_C64 = 1, MPSFT_C128 = 2 };
+/* FP32: binning, fold (compensated) and size-B FFT in FP32; mode subtraction,
+ *       pencil, thresholds and coefficients in FP64.
+ * FP64: everything in FP64 (the plain per-signal path). */
+enum { MPSFT_PREC_FP32 = 0, MPSFT_PREC_FP64 = 1 };
+
+typedef struct mpsft_ctx mpsft_ctx;
+typedef struct mpsft_signal mpsft_signal;
+typedef struct mpsft_rng mpsft_rng;
+
+/* ---- context ------------------------------------------------------------ */
+int mpsft_ctx_create(int device, mpsft_ctx **out);
+int mpsft_ctx_destroy(mpsft_ctx *ctx);
+/* Launch on the caller's CUDA stream (cudaStream_t) instead of the context's
+ * own; NULL restores the context's stream. */
+int mpsft_ctx_set_stream(mpsft_ctx *ctx, void *stream);
+/* Time every binning-kernel launch with CUDA events (0 = off, default). The
+ * totals are reported in mpsft_stats. */
+int mpsft_ctx_set_profiling(mpsft_ctx *ctx, int enable);
+const char *mpsft_last_error(const mpsft_ctx *ctx);
+const char *mpsft_status_string(int status);
+
+/* ---- random draws (the reference's global RNG, made explicit) ----------- */
+/* std::mt19937 with std::uniform_int_distribution<int32_t> over
+ * [0, 2^31 - 1]; mpsft_rng_create(123534) is the state MainInit leaves. */
+int mpsft_rng_create(int32_t seed, mpsft_rng **out);
+int mpsft_rng_destroy(mpsft_rng *rng);
+int mpsft_rng_seed(mpsft_rng *rng, int32_t seed);
+int32_t mpsft_rng_int32(mpsft_rng *rng);
+
+/* ---- small host helpers -------------------------------------------------- */
+/* NumBits: 1 + floor(log2(n / bins)) counted by halving (1 if n < bins). */
+int32_t mpsft_num_bits(int32_t n, int32_t bins);
+/* Window support p for (bins, delta); 0 on bad arguments. */
+int32_t mpsft_window_support(int32_t n, int32_t bins, double delta);
+/* Window tables computed on the device: wt[i] for i in [0, p) in the
+ * reference's index order t = 0, 1..p2, -p2..-1 (host output). */
+int mpsft_window_table(mpsft_ctx *ctx, int32_t n, int32_t bins, double delta,
+                       double *wt_host, int32_t cap);
+
+/* ---- signals (x resident on the device across calls) -------------------- */
+/* Copies n complex samples of type dtype from host memory. */
+int mpsft_signal_upload(mpsft_ctx *ctx, const void *x_host, int64_t n,
+                        int dtype, mpsft_signal **out);
+/* Wraps n samples already in device memory (not copied, not freed). */
+int mpsft_signal_wrap_device(mpsft_ctx *ctx, const void *x_device, int64_t n,
+                             int dtype, mpsft_signal **out);
+int mpsft_signal_free(mpsft_signal *sig);
+
+/* ---- BinInTime::Run ------------------------------------------------------- */
+/* Overwrites out with the (1 + 2*bits) x bins bin matrix of signal sig for the
+ * transform (a, b, c) and offset q: row 0 is tau = q, row 2s+1 is
+ * q + bins*2^s, row 2s+2 is q - bins*2^s. out is host memory of complex128
+ * (out_on_device = 0) or device memory (out_on_device = 1), row-major. */
+int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
+                      int32_t bits, double delta, int32_t a, int32_t b,
+                      int32_t c, int32_t q, int precision, double *out,
+                      int out_on_device);
+
+/* ---- BinInFreq::Run ------------------------------------------------------- */
+/* Subtracts from the host bin matrix inout ((1 + 2*bits) x bins complex128)
+ * the window responses of the m modes (k0[i], coef[2i] + i coef[2i+1]). */
+int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
+                      double delta, int32_t a, int32_t b, int32_t c, int32_t q,
+                      const int32_t *k0, const double *coef, int64_t m,
+                      double *inout);
+
+/* ---- MatPencil (batched) -------------------------------------------------- */
+/* For each i < count: the 2x2 pencil [[u0, u2], [u1, u0]] with
+ * u = (u0, u1, u2) = u3[6i .. 6i+6) (interleaved complex); writes
+ * sigma[2i], sigma[2i+1] and vote[i] (1 = upper half). Host buffers. */
+int mpsft_mat_pencil(mpsft_ctx *ctx, const double *u3, int64_t count,
+                     double *sigma, int32_t *vote);
+
+/* ---- Iterate -------------------------------------------------------------- */
+typedef struct {
+  int32_t bins;            /* odd number of bins B                          */
+  double window_delta;     /* reference default 1e-6                        */
+  int32_t trials;          /* odd; reference default 1                      */
+  double bin_threshold;    /* 0 = off                                       */
+  double window_threshold; /* must be > 0, as in the reference              */
+  double sv_threshold;     /* 0 = off                                       */
+  int32_t precision;       /* MPSFT_PREC_FP32 or MPSFT_PREC_FP64            */
+} mpsft_iterate_options;
+
+/* One Iterate call: draws (a, b, c) and one q per trial from rng, bins the
+ * signal, subtracts the modes already in the map, identifies and estimates.
+ * The mode map is passed in and out as (mm_k[i], mm_c[2i..2i+1]),
+ * i < *mm_size <= mm_cap (host memory); on return it is sorted by k.
+ * *found = 1 if something was added. */
+int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
+                  const mpsft_iterate_options *opt, mpsft_rng *rng,
+                  int32_t *mm_k, double *mm_c, int32_t *mm_size,
+                  int32_t mm_cap, int32_t *found);
+
+/* ---- Demo1::Run ------------------------------------------------------------ */
+typedef struct {
+  int32_t k;               /* sparsity S used to size the bins              */
+  double sigma;            /* noise level: bin_threshold = 3 sigma/sqrt(B), */
+                           /* sv_threshold = sigma/sqrt(B)                  */
+  int32_t trials;          /* odd                                           */
+  int32_t min_bins;        /* reference default 101 (benchmarks: 51)        */
+  double window_delta;     /* reference default 1e-6 (benchmarks: 1e-5)     */
+  double window_threshold; /* reference default 0.1                         */
+  int32_t max_stale_iter;  /* reference default 3 (benchmarks: 5)           */
+  int32_t max_iter;        /* cap on Iterate calls; 0 = 64 + 8*k            */
+  int32_t precision;       /* MPSFT_PREC_FP32 or MPSFT_PREC_FP64            */
+  int32_t mode_capacity;   /* found-mode table size; 0 = automatic          */
+} mpsft_solve_options;
+
+/* Fills opt with the reference's Demo1Options defaults (src/demo1.h:25-33)
+ * and FP32 precision; k and sigma must still be set. */
+void mpsft_solve_options_default(mpsft_solve_options *opt);
+
+typedef struct {
+  int32_t iterations;     /* Iterate calls made                              */
+  int32_t found;          /* distinct modes in the result                    */
+  int64_t gathers;        /* samples gathered by the binning kernel          */
+  int64_t bin_bytes;      /* algorithmic bytes of the binning launches       */
+  int32_t bin_launches;   /* binning launches timed (profiling on)           */
+  double bin_ms;          /* summed binning-kernel time (profiling on)       */
+  int32_t escalated_bins; /* FP32 near-tie bins recomputed in FP64           */
+  int32_t status;         /* per-signal status (batched calls)               */
+} mpsft_stats;
+
+/* One full recovery (the Demo1::Run loop) of sig. Draws 3 + trials values
+ * from rng per Iterate call, in the reference's order. Writes up to cap
+ * found modes sorted by k (host memory) and their count. */
+int mpsft_solve(mpsft_ctx *ctx, const mpsft_signal *sig,
+                const mpsft_solve_options *opt, mpsft_rng *rng,
+                int32_t *out_k, double *out_c, int32_t cap, int32_t *count,
+                mpsft_stats *stats);
+
+/* Many independent recoveries advanced together, one iteration of every
+ * active signal per launch sequence. Signal i uses opts[i] and rngs[i]
+ * (all precisions must agree) and writes out_k[i], out_c[i] (cap[i] entries)
+ * and count[i]. stats may be NULL; otherwise it has nsig entries. */
+int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                        const mpsft_solve_options *opts, int32_t nsig,
+                        mpsft_rng *const *rngs, int32_t *const *out_k,
+                        double *const *out_c, const int32_t *cap,
+                        int32_t *count, mpsft_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPSFT_GB300_H_ */

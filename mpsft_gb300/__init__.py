@@ -1,0 +1,351 @@
+"""mpsft_gb300: GB300 (sm_103a) MPSFT recovery loop behind a C ABI.
+
+This module is a thin ctypes binding of ``include/mpsft.h`` (the library is
+``mpsft_gb300/_lib/libmpsft_gb300.so``, built by ``mpsft_gb300.build``). It
+mirrors the reference's entry points (jiaweichiu/mpsft):
+
+=====================  =========================================  ==============================
+this module            reference                                  file:line
+=====================  =========================================  ==============================
+``bin_in_time``        ``BinInTime::Run``                         src/binner.h:30-41
+``bin_in_freq``        ``BinInFreq::Run``                         src/binner.h:123-133
+``mat_pencil``         ``MatPencil``                              src/freqid.h:28
+``iterate``            ``Iterate``                                src/iterate.h:65
+``solve``              ``Demo1::Run``                             src/demo1.cc:36-59
+``Rng``                ``RandomSeed`` / ``RandomInt32``           src/base.cc:52-53
+=====================  =========================================  ==============================
+
+There is no CPU fallback: if the library is missing or no GPU is present, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmpsft_gb300.so")
+
+OK, ERR_INVALID, ERR_UNSUPPORTED_N, ERR_CUDA, ERR_CAPACITY, ERR_ITER_CAP, \
+    ERR_NONFINITE, ERR_NOMEM = range(8)
+C64, C128 = 1, 2
+FP32, FP64 = 0, 1
+
+
+class MpsftError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mpsft status {status}: {msg}")
+        self.status = status
+
+
+class IterateOptions(ctypes.Structure):
+    _fields_ = [("bins", ctypes.c_int32), ("window_delta", ctypes.c_double),
+                ("trials", ctypes.c_int32), ("bin_threshold", ctypes.c_double),
+                ("window_threshold", ctypes.c_double),
+                ("sv_threshold", ctypes.c_double), ("precision", ctypes.c_int32)]
+
+
+class SolveOptions(ctypes.Structure):
+    _fields_ = [("k", ctypes.c_int32), ("sigma", ctypes.c_double),
+                ("trials", ctypes.c_int32), ("min_bins", ctypes.c_int32),
+                ("window_delta", ctypes.c_double),
+                ("window_threshold", ctypes.c_double),
+                ("max_stale_iter", ctypes.c_int32), ("max_iter", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("mode_capacity", ctypes.c_int32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("found", ctypes.c_int32),
+                ("gathers", ctypes.c_int64), ("bin_bytes", ctypes.c_int64),
+                ("bin_launches", ctypes.c_int32), ("bin_ms", ctypes.c_double),
+                ("escalated_bins", ctypes.c_int32), ("status", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: build it with `python -m mpsft_gb300.build`")
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    I32, I64, D, I = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_int
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    sigs = {
+        "mpsft_ctx_create": (I, [I, PP]),
+        "mpsft_ctx_destroy": (I, [P]),
+        "mpsft_ctx_set_stream": (I, [P, P]),
+        "mpsft_ctx_set_profiling": (I, [P, I]),
+        "mpsft_last_error": (ctypes.c_char_p, [P]),
+        "mpsft_status_string": (ctypes.c_char_p, [I]),
+        "mpsft_rng_create": (I, [I32, PP]),
+        "mpsft_rng_destroy": (I, [P]),
+        "mpsft_rng_seed": (I, [P, I32]),
+        "mpsft_rng_int32": (I32, [P]),
+        "mpsft_num_bits": (I32, [I32, I32]),
+        "mpsft_window_support": (I32, [I32, I32, D]),
+        "mpsft_window_table": (I, [P, I32, I32, D, P, I32]),
+        "mpsft_signal_upload": (I, [P, P, I64, I, PP]),
+        "mpsft_signal_wrap_device": (I, [P, P, I64, I, PP]),
+        "mpsft_signal_free": (I, [P]),
+        "mpsft_bin_in_time": (I, [P, P, I32, I32, D, I32, I32, I32, I32, I, P, I]),
+        "mpsft_bin_in_freq": (I, [P, I32, I32, I32, D, I32, I32, I32, I32, P, P,
+                                  I64, P]),
+        "mpsft_mat_pencil": (I, [P, P, I64, P, P]),
+        "mpsft_iterate": (I, [P, P, ctypes.POINTER(IterateOptions), P, P, P, P,
+                              I32, P]),
+        "mpsft_solve_options_default": (None, [ctypes.POINTER(SolveOptions)]),
+        "mpsft_solve": (I, [P, P, ctypes.POINTER(SolveOptions), P, P, P, I32, P,
+                            ctypes.POINTER(Stats)]),
+        "mpsft_solve_batched": (I, [P, P, ctypes.POINTER(SolveOptions), I32, P, P,
+                                    P, P, P, ctypes.POINTER(Stats)]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    """Names declared in include/mpsft.h (used by the load test)."""
+    import re
+    hdr = os.path.join(os.path.dirname(_HERE), "include", "mpsft.h")
+    txt = open(hdr).read()
+    return sorted(set(re.findall(r"\b(mpsft_[a-z0-9_]+)\s*\(", txt)))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Rng:
+    """The reference's global RNG made explicit (std::mt19937 +
+    uniform_int_distribution<int32_t>); Rng(123534) is MainInit's state."""
+
+    def __init__(self, seed: int = 123534):
+        lib = load_library()
+        h = ctypes.c_void_p()
+        _check(None, lib.mpsft_rng_create(int(seed), ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def seed(self, s: int) -> None:
+        self._lib.mpsft_rng_seed(self._h, int(s))
+
+    def int32(self) -> int:
+        return int(self._lib.mpsft_rng_int32(self._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.mpsft_rng_destroy(self._h)
+            self._h = None
+
+
+def _check(ctx, rc: int) -> None:
+    if rc != OK:
+        lib = load_library()
+        msg = lib.mpsft_last_error(ctx._h).decode() if ctx is not None else \
+            lib.mpsft_status_string(rc).decode()
+        raise MpsftError(rc, msg)
+
+
+class Context:
+    """One CUDA device, one stream, reusable work buffers."""
+
+    def __init__(self, device: int = 0):
+        lib = load_library()
+        h = ctypes.c_void_p()
+        rc = lib.mpsft_ctx_create(int(device), ctypes.byref(h))
+        if rc != OK:
+            raise MpsftError(rc, "mpsft_ctx_create failed (is a GPU present?)")
+        self._h = h
+        self._lib = lib
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.mpsft_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        _check(self, self._lib.mpsft_ctx_set_stream(
+            self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def set_profiling(self, on: bool) -> None:
+        _check(self, self._lib.mpsft_ctx_set_profiling(self._h, int(bool(on))))
+
+    # ---- signals --------------------------------------------------------
+    def upload(self, x: np.ndarray) -> "Signal":
+        x = np.ascontiguousarray(x)
+        if x.dtype == np.complex64:
+            dt = C64
+        elif x.dtype == np.complex128:
+            dt = C128
+        else:
+            raise TypeError("x must be complex64 or complex128")
+        h = ctypes.c_void_p()
+        _check(self, self._lib.mpsft_signal_upload(self._h, _ptr(x), x.size, dt,
+                                                   ctypes.byref(h)))
+        return Signal(self, h, x.size, dt)
+
+    def wrap_device(self, ptr: int, n: int, dtype: int) -> "Signal":
+        h = ctypes.c_void_p()
+        _check(self, self._lib.mpsft_signal_wrap_device(
+            self._h, ctypes.c_void_p(ptr), int(n), int(dtype), ctypes.byref(h)))
+        return Signal(self, h, n, dtype)
+
+    # ---- operators -------------------------------------------------------
+    def window_table(self, n: int, bins: int, delta: float) -> np.ndarray:
+        p = int(self._lib.mpsft_window_support(n, bins, delta))
+        if p <= 0:
+            raise MpsftError(ERR_INVALID, "bad window arguments")
+        wt = np.zeros(p, np.float64)
+        _check(self, self._lib.mpsft_window_table(self._h, n, bins, delta, _ptr(wt), p))
+        return wt
+
+    def bin_in_time(self, sig: "Signal", bins: int, bits: int, delta: float,
+                    a: int, b: int, c: int, q: int,
+                    precision: int = FP32) -> np.ndarray:
+        out = np.zeros((1 + 2 * bits, bins), np.complex128)
+        _check(self, self._lib.mpsft_bin_in_time(
+            self._h, sig._h, bins, bits, delta, a, b, c, q, precision, _ptr(out), 0))
+        return out
+
+    def bin_in_freq(self, out: np.ndarray, n: int, bins: int, bits: int,
+                    delta: float, a: int, b: int, c: int, q: int,
+                    k0: np.ndarray, coef: np.ndarray) -> np.ndarray:
+        out = np.ascontiguousarray(out, np.complex128).copy()
+        k0 = np.ascontiguousarray(k0, np.int32)
+        coef = np.ascontiguousarray(coef, np.complex128)
+        _check(self, self._lib.mpsft_bin_in_freq(
+            self._h, n, bins, bits, delta, a, b, c, q, _ptr(k0), _ptr(coef),
+            k0.size, _ptr(out)))
+        return out
+
+    def mat_pencil(self, u: np.ndarray):
+        """u: (count, 3) complex128 rows (u0, u1, u2). Returns (sigma, vote)."""
+        u = np.ascontiguousarray(u, np.complex128).reshape(-1, 3)
+        sig = np.zeros((u.shape[0], 2), np.float64)
+        vote = np.zeros(u.shape[0], np.int32)
+        _check(self, self._lib.mpsft_mat_pencil(self._h, _ptr(u), u.shape[0],
+                                                _ptr(sig), _ptr(vote)))
+        return sig, vote.astype(bool)
+
+    def iterate(self, sig: "Signal", rng: Rng, bins: int,
+                window_delta: float = 1e-6, trials: int = 1,
+                bin_threshold: float = 0.0, window_threshold: float = 0.1,
+                sv_threshold: float = 0.0, mm: dict | None = None,
+                precision: int = FP32):
+        mm = dict(mm or {})
+        cap = len(mm) + bins + 16
+        k = np.zeros(cap, np.int32)
+        c = np.zeros(cap, np.complex128)
+        for i, (kk, cc) in enumerate(mm.items()):
+            k[i] = kk
+            c[i] = cc
+        size = np.array([len(mm)], np.int32)
+        found = np.zeros(1, np.int32)
+        opt = IterateOptions(bins, window_delta, trials, bin_threshold,
+                             window_threshold, sv_threshold, precision)
+        _check(self, self._lib.mpsft_iterate(self._h, sig._h, ctypes.byref(opt),
+                                             rng._h, _ptr(k), _ptr(c), _ptr(size),
+                                             cap, _ptr(found)))
+        m = int(size[0])
+        return bool(found[0]), {int(k[i]): complex(c[i]) for i in range(m)}
+
+    @staticmethod
+    def solve_options(k: int, sigma: float, **kw) -> SolveOptions:
+        o = SolveOptions()
+        load_library().mpsft_solve_options_default(ctypes.byref(o))
+        o.k = k
+        o.sigma = sigma
+        for name, v in kw.items():
+            setattr(o, name, v)
+        return o
+
+    def solve(self, sig: "Signal", rng: Rng, opt: SolveOptions,
+              cap: int | None = None):
+        """Demo1::Run. Returns (modes dict, Stats)."""
+        cap = cap or (4 * opt.k + 4096)
+        k = np.zeros(cap, np.int32)
+        c = np.zeros(cap, np.complex128)
+        count = np.zeros(1, np.int32)
+        st = Stats()
+        _check(self, self._lib.mpsft_solve(self._h, sig._h, ctypes.byref(opt),
+                                           rng._h, _ptr(k), _ptr(c), cap,
+                                           _ptr(count), ctypes.byref(st)))
+        m = int(count[0])
+        return {int(k[i]): complex(c[i]) for i in range(m)}, st
+
+    def solve_arrays(self, sig: "Signal", rng: Rng, opt: SolveOptions,
+                     cap: int | None = None):
+        """Like solve but returns (k int32 array, coef complex128 array, Stats)."""
+        cap = cap or (4 * opt.k + 4096)
+        k = np.zeros(cap, np.int32)
+        c = np.zeros(cap, np.complex128)
+        count = np.zeros(1, np.int32)
+        st = Stats()
+        _check(self, self._lib.mpsft_solve(self._h, sig._h, ctypes.byref(opt),
+                                           rng._h, _ptr(k), _ptr(c), cap,
+                                           _ptr(count), ctypes.byref(st)))
+        m = int(count[0])
+        return k[:m], c[:m], st
+
+    def solve_batched(self, sigs: list, rngs: list, opts: list,
+                      cap: int | None = None, raise_on_error: bool = True):
+        """Many Demo1::Run solves advanced together. Returns
+        (list of (k, coef) arrays, list of Stats dicts)."""
+        nsig = len(sigs)
+        caps = np.array([cap or (4 * o.k + 4096) for o in opts], np.int32)
+        ks = [np.zeros(int(cp), np.int32) for cp in caps]
+        cs = [np.zeros(int(cp), np.complex128) for cp in caps]
+        count = np.zeros(nsig, np.int32)
+        stats = (Stats * nsig)()
+        opt_arr = (SolveOptions * nsig)(*opts)
+        sig_arr = (ctypes.c_void_p * nsig)(*[s._h.value for s in sigs])
+        rng_arr = (ctypes.c_void_p * nsig)(*[r._h.value for r in rngs])
+        k_arr = (ctypes.c_void_p * nsig)(*[a.ctypes.data for a in ks])
+        c_arr = (ctypes.c_void_p * nsig)(*[a.ctypes.data for a in cs])
+        rc = self._lib.mpsft_solve_batched(
+            self._h, sig_arr, opt_arr, nsig, rng_arr, k_arr, c_arr, _ptr(caps),
+            _ptr(count), stats)
+        if raise_on_error:
+            _check(self, rc)
+        out = [(ks[i][:count[i]], cs[i][:count[i]]) for i in range(nsig)]
+        return out, [stats[i].as_dict() for i in range(nsig)]
+
+
+@dataclass
+class Signal:
+    ctx: Context
+    _h: ctypes.c_void_p
+    n: int
+    dtype: int
+    _freed: bool = field(default=False)
+
+    def free(self) -> None:
+        if not self._freed and self._h:
+            self.ctx._lib.mpsft_signal_free(self._h)
+            self._freed = True
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

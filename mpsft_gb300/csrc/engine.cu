@@ -1,0 +1,1138 @@
+// Host engine of the C ABI declared in include/mpsft.h.
+//
+// Per iteration of every active signal the host computes the scalars the
+// reference computes on the host side of Iterate (bins, NumBits, the window
+// scalars, the thresholds of Demo1::Run) and draws the transform and the q's
+// from the signal's RNG in the reference's order (src/iterate.cc:92-104);
+// everything proportional to n, p, bins or the mode count runs on the GPU:
+//   window tables -> Bluestein tables -> mode buckets -> gather/fold ->
+//   size-B FFT -> decide (subtract, energy, pencils, coefficient) -> merge.
+// One small device-to-host copy per iteration returns the found flag, the
+// status bits and the mode count that drive the reference's stop rule.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/mpsft.h"
+#include "launch.h"
+
+using namespace mpsft;
+
+struct mpsft_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool profiling = false;
+  float2 *tw32 = nullptr;
+  double2 *tw64 = nullptr;
+  // grow-only device arena reused across calls
+  unsigned char *arena = nullptr;
+  size_t arena_size = 0;
+  // pinned host staging for per-iteration control words
+  int32_t *h_ctl = nullptr;
+  size_t h_ctl_n = 0;
+  std::vector<cudaEvent_t> events;
+};
+
+struct mpsft_signal {
+  mpsft_ctx *ctx = nullptr;
+  void *d_x = nullptr;
+  int64_t n = 0;
+  int dtype = MPSFT_C64;
+  bool owned = false;
+};
+
+struct mpsft_rng {
+  std::mt19937 eng;
+  std::uniform_int_distribution<int32_t> uid;
+  int32_t Draw() { return uid(eng); }
+};
+
+namespace {
+
+constexpr int kCtlWords = 4;  // found flag, status bits, mode count, spare
+
+int Fail(mpsft_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+#define MPSFT_CUDA(ctx, call)                                                  \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      return Fail(ctx, MPSFT_ERR_CUDA,                                         \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));         \
+    }                                                                          \
+  } while (0)
+
+bool IsPow2(int64_t n) { return n > 0 && (n & (n - 1)) == 0; }
+
+uint64_t MulModU64(uint64_t a, uint64_t b, uint64_t m) {
+  return uint64_t((unsigned __int128)a * b % m);
+}
+uint64_t PowModU64(uint64_t b, uint64_t e, uint64_t m) {
+  uint64_t r = 1 % m;
+  b %= m;
+  while (e) {
+    if (e & 1) r = MulModU64(r, b, m);
+    b = MulModU64(b, b, m);
+    e >>= 1;
+  }
+  return r;
+}
+// Deterministic Miller-Rabin, exact for n < 3.2e9 with bases 2, 3, 5, 7.
+bool IsPrime(int64_t n) {
+  if (n < 2) return false;
+  for (int64_t p : {2, 3, 5, 7, 11, 13}) {
+    if (n % p == 0) return n == p;
+  }
+  uint64_t d = uint64_t(n) - 1;
+  int r = 0;
+  while ((d & 1) == 0) {
+    d >>= 1;
+    ++r;
+  }
+  for (uint64_t a : {2ull, 3ull, 5ull, 7ull}) {
+    uint64_t x = PowModU64(a, d, uint64_t(n));
+    if (x == 1 || x == uint64_t(n) - 1) continue;
+    bool comp = true;
+    for (int i = 1; i < r; ++i) {
+      x = MulModU64(x, x, uint64_t(n));
+      if (x == uint64_t(n) - 1) {
+        comp = false;
+        break;
+      }
+    }
+    if (comp) return false;
+  }
+  return true;
+}
+
+// a^{-1} mod m by the extended Euclidean algorithm; 0 if not invertible.
+int32_t InverseMod(int64_t a, int64_t m) {
+  int64_t r0 = m, r1 = ((a % m) + m) % m, s0 = 0, s1 = 1;
+  while (r1 != 0) {
+    const int64_t qt = r0 / r1;
+    int64_t t = r0 - qt * r1;
+    r0 = r1;
+    r1 = t;
+    t = s0 - qt * s1;
+    s0 = s1;
+    s1 = t;
+  }
+  if (r0 != 1) return 0;
+  return int32_t(((s0 % m) + m) % m);
+}
+
+int32_t NumBits(int32_t n, int32_t bins) {
+  if (n < bins) return 1;
+  int32_t out = 0;
+  while (n >= bins) {
+    n >>= 1;
+    ++out;
+  }
+  return out;
+}
+
+// Window scalars, in the reference's operation order (src/window.cc:28-51).
+struct WinParams {
+  int32_t p = 0, p2 = 0, folds = 0;
+  double width = 0, sigma_f = 0, sigma_t = 0, erf_d = 0;
+};
+WinParams MakeWindow(int32_t bins, double delta) {
+  WinParams w;
+  w.width = 1.0 / (2.0 * bins);
+  const double sq = std::sqrt(-std::log(delta));
+  w.sigma_f = 0.5 / (bins * 2.0 * M_SQRT2 * sq);
+  w.sigma_t = 1.0 / ((2.0 * M_PI) * w.sigma_f);
+  const double tmp = 2.0 * M_SQRT2 * w.sigma_t * sq + 1;
+  int32_t f = int32_t(std::ceil(tmp / double(bins)));
+  if (f % 2 == 0) ++f;
+  w.folds = f;
+  w.p = f * bins;
+  w.p2 = (w.p - 1) / 2;
+  w.erf_d = M_SQRT2 * M_PI * w.sigma_t;
+  return w;
+}
+
+int FFTLog2(int32_t bins) {
+  int l = 0;
+  while ((1 << l) < 2 * bins - 1) ++l;
+  return l;
+}
+
+struct Transform {
+  int32_t a, b, c, a_inv;
+};
+
+// Transform(n) (src/integer.cc:44-49): a, b, c drawn in that order; a is made
+// odd for power-of-two n so that it is invertible.
+Transform DrawTransform(mpsft_rng *rng, int32_t n) {
+  Transform t;
+  t.a = (rng->Draw() % (n - 1)) + 1;
+  t.b = rng->Draw() % n;
+  t.c = rng->Draw() % n;
+  if (IsPow2(n)) t.a |= 1;
+  t.a_inv = InverseMod(t.a, n);
+  return t;
+}
+
+int CheckN(mpsft_ctx *ctx, int64_t n) {
+  if (n < 3 || n > INT32_MAX) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "n must be in [3, 2^31 - 1]");
+  }
+  if (!IsPow2(n) && !IsPrime(n)) {
+    return Fail(ctx, MPSFT_ERR_UNSUPPORTED_N,
+                "n must be prime or a power of two (the permutation needs an "
+                "invertible a)");
+  }
+  return MPSFT_OK;
+}
+
+// ---------------------------------------------------------------- buffers
+struct Carve {
+  unsigned char *base;
+  size_t off = 0;
+  template <typename T> T *take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T *p = reinterpret_cast<T *>(base ? base + off : nullptr);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+// Buffer shape of one signal for a whole call.
+struct Shape {
+  int32_t n = 0, bins_cap = 0, rows_cap = 0, trials = 1, p2_cap = 0;
+  int32_t m_cap = 0, tab_cap = 0;
+  bool fp64 = false;
+};
+
+void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
+  it->wt32 = cv.take<float>(size_t(s.p2_cap) + 1);
+  it->wt64 = cv.take<double>(size_t(s.p2_cap) + 1);
+  const size_t cells = size_t(s.trials) * s.rows_cap * s.bins_cap;
+  it->fold = cv.take<unsigned char>(cells * (s.fp64 ? 16 : 8));
+  it->ubuf = cv.take<double2>(cells);
+  it->chirp = cv.take<unsigned char>(size_t(s.bins_cap) * (s.fp64 ? 16 : 8));
+  it->chat = cv.take<unsigned char>(size_t(s.m_cap) * (s.fp64 ? 16 : 8));
+  it->tab_key = cv.take<int32_t>(s.tab_cap);
+  it->tab_coef = cv.take<double2>(s.tab_cap);
+  it->tab_cap = s.tab_cap;
+  it->bkt_count = cv.take<int32_t>(s.bins_cap);
+  it->bkt_start = cv.take<int32_t>(s.bins_cap);
+  it->bkt_list = cv.take<int32_t>(s.tab_cap);
+  it->cand_valid = cv.take<int32_t>(s.bins_cap);
+  it->cand_k0 = cv.take<int32_t>(s.bins_cap);
+  it->cand_coef = cv.take<double2>(s.bins_cap);
+  *ctl = cv.take<int32_t>(kCtlWords);
+  it->flags = *ctl;
+  it->tab_count = *ctl + 2;
+  it->bins_cap = s.bins_cap;
+}
+
+int EnsureArena(mpsft_ctx *ctx, size_t bytes) {
+  if (ctx->arena_size >= bytes) return MPSFT_OK;
+  if (ctx->arena) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->arena);
+    ctx->arena = nullptr;
+    ctx->arena_size = 0;
+  }
+  const size_t want = bytes + (bytes >> 3);
+  if (cudaMalloc(&ctx->arena, want) != cudaSuccess) {
+    cudaGetLastError();
+    return Fail(ctx, MPSFT_ERR_NOMEM, "device allocation of the work arena failed");
+  }
+  ctx->arena_size = want;
+  return MPSFT_OK;
+}
+
+int EnsureHostCtl(mpsft_ctx *ctx, size_t words) {
+  if (ctx->h_ctl_n >= words) return MPSFT_OK;
+  if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+  ctx->h_ctl = nullptr;
+  MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_ctl, words * sizeof(int32_t)));
+  ctx->h_ctl_n = words;
+  return MPSFT_OK;
+}
+
+int32_t NextPow2(int64_t v) {
+  int32_t p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+// Fills the per-iteration scalars of it for (bins, bits, transform, q's).
+void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
+              double delta, const Transform &tf, const int32_t *q,
+              int32_t trials) {
+  const WinParams w = MakeWindow(bins, delta);
+  it->x = sig->d_x;
+  it->n = int32_t(sig->n);
+  it->bins = bins;
+  it->bits = bits;
+  it->rows = 1 + 2 * bits;
+  it->p = w.p;
+  it->p2 = w.p2;
+  it->folds = w.folds;
+  it->a = tf.a;
+  it->b = tf.b;
+  it->c = tf.c;
+  it->a_inv = tf.a_inv;
+  it->trials = trials;
+  it->active = 1;
+  for (int t = 0; t < trials; ++t) {
+    it->q[t] = q[t];
+    // bq = e^{2 pi i (b q mod n)/n}, as Sinusoid(MulMod(b, q, n) / n).
+    const int64_t m = (int64_t(tf.b) * q[t]) % sig->n;
+    const double f = double(m) / double(sig->n) * (2.0 * M_PI);
+    it->bq_re[t] = std::cos(f);
+    it->bq_im[t] = std::sin(f);
+  }
+  it->width = w.width;
+  it->sigma_f = w.sigma_f;
+  it->erf_d = w.erf_d;
+  it->fft_log2m = FFTLog2(bins);
+  it->fft_m = 1 << it->fft_log2m;
+}
+
+int CheckWindow(mpsft_ctx *ctx, int32_t bins, double delta, bool fp64) {
+  if (bins <= 0 || bins % 2 == 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bins must be odd and positive");
+  }
+  if (!(delta > 0 && delta < 1)) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "window_delta must be in (0, 1)");
+  }
+  const WinParams w = MakeWindow(bins, delta);
+  if (w.folds > kFoldLanes * kMaxFoldsPerLane) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "window_delta too small (p/bins > 80)");
+  }
+  const int m = 1 << FFTLog2(bins);
+  if (m > (fp64 ? kMaxFFT64 : kMaxFFT)) {
+    return Fail(ctx, MPSFT_ERR_INVALID,
+                fp64 ? "bins too large for the FP64 path (max 4096)"
+                     : "bins too large (max 8192)");
+  }
+  return MPSFT_OK;
+}
+
+// Records the binning launch between an event pair when profiling.
+struct BinTimer {
+  mpsft_ctx *ctx;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> used;
+  size_t next = 0;
+  int Begin() {
+    if (!ctx->profiling) return MPSFT_OK;
+    while (ctx->events.size() < 2 * (next + 1)) {
+      cudaEvent_t e;
+      MPSFT_CUDA(ctx, cudaEventCreate(&e));
+      ctx->events.push_back(e);
+    }
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->events[2 * next], ctx->stream));
+    return MPSFT_OK;
+  }
+  int End() {
+    if (!ctx->profiling) return MPSFT_OK;
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->events[2 * next + 1], ctx->stream));
+    used.emplace_back(ctx->events[2 * next], ctx->events[2 * next + 1]);
+    ++next;
+    return MPSFT_OK;
+  }
+  double TotalMs() {
+    double tot = 0;
+    for (auto &p : used) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, p.first, p.second);
+      tot += ms;
+    }
+    return tot;
+  }
+};
+
+int64_t BinBytes(const SigIter &it, bool fp64) {
+  const int64_t g = int64_t(it.trials) * it.p * it.rows;
+  return 32 * g + int64_t(fp64 ? 8 : 4) * (it.p2 + 1) +
+         int64_t(it.trials) * (fp64 ? 16 : 8) * it.rows * it.bins;
+}
+
+// Launch sequence of one iteration for nsig signals whose SigIter array is
+// already on the device.
+int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
+                    const std::vector<SigIter> &h_its, bool x_c128, bool fp64,
+                    BinTimer *timer) {
+  int max_bins = 0, max_bits = 0, max_trials = 0, max_p2 = 0, max_m = 0,
+      max_rows = 0;
+  for (const SigIter &it : h_its) {
+    if (!it.active) continue;
+    max_bins = std::max(max_bins, it.bins);
+    max_bits = std::max(max_bits, it.bits);
+    max_trials = std::max(max_trials, it.trials);
+    max_p2 = std::max(max_p2, it.p2);
+    max_m = std::max(max_m, it.fft_m);
+    max_rows = std::max(max_rows, it.rows);
+  }
+  if (max_bins == 0) return MPSFT_OK;
+  cudaStream_t s = ctx->stream;
+  LaunchWindow(d_its, nsig, max_p2, s);
+  LaunchBluesteinSetup(d_its, nsig, max_m, fp64, ctx->tw32, ctx->tw64, s);
+  LaunchBucket(d_its, nsig, max_bins, 0, s);
+  if (timer) {
+    int rc = timer->Begin();
+    if (rc) return rc;
+  }
+  LaunchBinFold(d_its, nsig, max_bins, max_bits, max_trials, x_c128, fp64, s);
+  if (timer) {
+    int rc = timer->End();
+    if (rc) return rc;
+  }
+  LaunchRowFFT(d_its, nsig, max_rows, max_trials, max_m, fp64, ctx->tw32,
+               ctx->tw64, s);
+  LaunchDecide(d_its, nsig, max_bins, max_trials, false, s);
+  LaunchMerge(d_its, nsig, max_bins, s);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  return MPSFT_OK;
+}
+
+struct ModeOut {
+  std::vector<std::pair<int32_t, double2>> modes;
+};
+
+int DownloadTable(mpsft_ctx *ctx, const SigIter &it,
+                  std::vector<std::pair<int32_t, double2>> *out) {
+  std::vector<int32_t> keys(it.tab_cap);
+  std::vector<double2> coefs(it.tab_cap);
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(keys.data(), it.tab_key,
+                                  sizeof(int32_t) * it.tab_cap,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(coefs.data(), it.tab_coef,
+                                  sizeof(double2) * it.tab_cap,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  out->clear();
+  for (int i = 0; i < it.tab_cap; ++i) {
+    if (keys[i] != kEmptyKey) out->emplace_back(keys[i], coefs[i]);
+  }
+  std::sort(out->begin(), out->end(),
+            [](const std::pair<int32_t, double2> &l,
+               const std::pair<int32_t, double2> &r) { return l.first < r.first; });
+  return MPSFT_OK;
+}
+
+int ClearTable(mpsft_ctx *ctx, const SigIter &it, int32_t *ctl) {
+  MPSFT_CUDA(ctx, cudaMemsetAsync(it.tab_key, 0xFF,
+                                  sizeof(int32_t) * it.tab_cap, ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemsetAsync(it.tab_coef, 0, sizeof(double2) * it.tab_cap,
+                                  ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(int32_t) * kCtlWords,
+                                  ctx->stream));
+  return MPSFT_OK;
+}
+
+int CheckSignal(mpsft_ctx *ctx, const mpsft_signal *sig) {
+  if (!sig || !sig->d_x) return Fail(ctx, MPSFT_ERR_INVALID, "null signal");
+  if (sig->ctx != ctx) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "signal belongs to another context");
+  }
+  return CheckN(ctx, sig->n);
+}
+
+// One batched solve; the core of mpsft_solve and mpsft_solve_batched.
+int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+              const mpsft_solve_options *opts, int32_t nsig,
+              mpsft_rng *const *rngs, int32_t *const *out_k,
+              double *const *out_c, const int32_t *cap, int32_t *count,
+              mpsft_stats *stats) {
+  if (nsig <= 0) return Fail(ctx, MPSFT_ERR_INVALID, "no signals");
+  const bool fp64 = opts[0].precision == MPSFT_PREC_FP64;
+  const bool x_c128 = sigs[0]->dtype == MPSFT_C128;
+  std::vector<Shape> shapes(nsig);
+  size_t bytes = 0;
+  for (int i = 0; i < nsig; ++i) {
+    const mpsft_solve_options &o = opts[i];
+    int rc = CheckSignal(ctx, sigs[i]);
+    if (rc) return rc;
+    if (!rngs[i]) return Fail(ctx, MPSFT_ERR_INVALID, "null rng");
+    if ((o.precision == MPSFT_PREC_FP64) != fp64) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "all signals must share a precision");
+    }
+    if ((sigs[i]->dtype == MPSFT_C128) != x_c128) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "all signals must share a dtype");
+    }
+    if (o.trials < 1 || o.trials % 2 == 0 || o.trials > kMaxTrials) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "trials must be odd and <= 15");
+    }
+    if (o.k < 0 || o.min_bins < 1 || o.max_stale_iter < 1) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "bad k, min_bins or max_stale_iter");
+    }
+    if (!(o.window_threshold > 0)) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "window_threshold must be > 0");
+    }
+    const int32_t n = int32_t(sigs[i]->n);
+    const int64_t bmax64 = std::max<int64_t>(2 * int64_t(o.k) + 1, o.min_bins);
+    if (bmax64 > INT32_MAX) return Fail(ctx, MPSFT_ERR_INVALID, "k too large");
+    Shape &s = shapes[i];
+    s.n = n;
+    s.bins_cap = int32_t(bmax64);
+    // Window CHECKs an odd number of bins (src/window.cc:33); B is
+    // 2(k - found) + 1 or min_bins, so min_bins must be odd.
+    if (o.min_bins % 2 == 0) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "min_bins must be odd");
+    }
+    for (int32_t bb : {s.bins_cap, std::min(s.bins_cap, o.min_bins)}) {
+      rc = CheckWindow(ctx, bb, o.window_delta, fp64);
+      if (rc) return rc;
+    }
+    s.rows_cap = 1 + 2 * NumBits(n, std::min(s.bins_cap, o.min_bins));
+    s.trials = o.trials;
+    s.p2_cap = std::max(MakeWindow(s.bins_cap, o.window_delta).p2,
+                        MakeWindow(std::min(s.bins_cap, o.min_bins),
+                                   o.window_delta).p2);
+    s.m_cap = 1 << FFTLog2(s.bins_cap);
+    s.tab_cap = o.mode_capacity > 0
+                    ? NextPow2(o.mode_capacity)
+                    : NextPow2(std::max<int64_t>(64, 4 * (int64_t(o.k) + s.bins_cap)));
+    s.fp64 = fp64;
+    Carve probe{nullptr};
+    SigIter dummy{};
+    int32_t *ctl = nullptr;
+    CarveSignal(probe, s, &dummy, &ctl);
+    bytes += probe.off + 256;
+  }
+  bytes += sizeof(SigIter) * nsig + 256;
+  int rc = EnsureArena(ctx, bytes);
+  if (rc) return rc;
+  rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
+  if (rc) return rc;
+
+  Carve cv{ctx->arena};
+  SigIter *d_its = cv.take<SigIter>(nsig);
+  std::vector<SigIter> its(nsig);
+  std::vector<int32_t *> ctls(nsig);
+  for (int i = 0; i < nsig; ++i) {
+    std::memset(&its[i], 0, sizeof(SigIter));
+    CarveSignal(cv, shapes[i], &its[i], &ctls[i]);
+    rc = ClearTable(ctx, its[i], ctls[i]);
+    if (rc) return rc;
+  }
+  // All control words are contiguous only per signal; copy them one by one.
+  struct Run {
+    int32_t iter = 0, stale = 0, found = 0, status = MPSFT_OK;
+    bool done = false;
+    int64_t gathers = 0, bin_bytes = 0;
+  };
+  std::vector<Run> run(nsig);
+  BinTimer timer{ctx};
+  int active = nsig;
+  while (active > 0) {
+    for (int i = 0; i < nsig; ++i) {
+      SigIter &it = its[i];
+      if (run[i].done) {
+        it.active = 0;
+        continue;
+      }
+      const mpsft_solve_options &o = opts[i];
+      const int32_t n = int32_t(sigs[i]->n);
+      const int32_t bins =
+          std::max<int32_t>((o.k - run[i].found) * 2 + 1, o.min_bins);
+      const int32_t bits = NumBits(n, bins);
+      const Transform tf = DrawTransform(rngs[i], n);
+      int32_t q[kMaxTrials];
+      for (int t = 0; t < o.trials; ++t) q[t] = rngs[i]->Draw() % n;
+      FillIter(&it, sigs[i], bins, bits, o.window_delta, tf, q, o.trials);
+      it.bin_thr = 3.0 * o.sigma / std::sqrt(double(bins));
+      it.sv_thr = 1.0 * o.sigma / std::sqrt(double(bins));
+      it.win_thr = o.window_threshold;
+      run[i].gathers += int64_t(it.trials) * it.p * it.rows;
+      run[i].bin_bytes += BinBytes(it, fp64);
+    }
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    for (int i = 0; i < nsig; ++i) {
+      if (!run[i].done) {
+        MPSFT_CUDA(ctx, cudaMemsetAsync(ctls[i], 0, sizeof(int32_t) * 2,
+                                        ctx->stream));
+      }
+    }
+    rc = LaunchIteration(ctx, d_its, nsig, its, x_c128, fp64, &timer);
+    if (rc) return rc;
+    for (int i = 0; i < nsig; ++i) {
+      MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_ctl + kCtlWords * i, ctls[i],
+                                      sizeof(int32_t) * kCtlWords,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < nsig; ++i) {
+      if (run[i].done) continue;
+      const mpsft_solve_options &o = opts[i];
+      const int32_t *c = ctx->h_ctl + kCtlWords * i;
+      Run &r = run[i];
+      r.iter += 1;
+      r.found = c[2];
+      if (c[1] & kStatusCapacity) {
+        r.status = MPSFT_ERR_CAPACITY;
+      } else if (c[1] & kStatusNonFinite) {
+        r.status = MPSFT_ERR_NONFINITE;
+      } else if (int64_t(r.found) * 2 > its[i].tab_cap) {
+        r.status = MPSFT_ERR_CAPACITY;
+      }
+      if (!c[0]) r.stale += 1;
+      const int32_t max_iter = o.max_iter > 0 ? o.max_iter : 64 + 8 * o.k;
+      if (r.status == MPSFT_OK && r.stale < o.max_stale_iter &&
+          r.iter >= max_iter) {
+        r.status = MPSFT_ERR_ITER_CAP;
+      }
+      if (r.status != MPSFT_OK || r.stale >= o.max_stale_iter) {
+        r.done = true;
+        --active;
+      }
+    }
+  }
+  int first_err = MPSFT_OK;
+  const double bin_ms = timer.TotalMs();
+  for (int i = 0; i < nsig; ++i) {
+    std::vector<std::pair<int32_t, double2>> modes;
+    rc = DownloadTable(ctx, its[i], &modes);
+    if (rc) return rc;
+    int st = run[i].status;
+    const int32_t m = int32_t(modes.size());
+    if (m > cap[i]) st = st ? st : MPSFT_ERR_CAPACITY;
+    const int32_t w = std::min(m, cap[i]);
+    for (int32_t j = 0; j < w; ++j) {
+      out_k[i][j] = modes[j].first;
+      out_c[i][2 * j] = modes[j].second.x;
+      out_c[i][2 * j + 1] = modes[j].second.y;
+    }
+    count[i] = m;
+    if (stats) {
+      mpsft_stats &s = stats[i];
+      std::memset(&s, 0, sizeof(s));
+      s.iterations = run[i].iter;
+      s.found = m;
+      s.gathers = run[i].gathers;
+      s.bin_bytes = run[i].bin_bytes;
+      s.bin_launches = int32_t(timer.used.size());
+      s.bin_ms = bin_ms;
+      s.status = st;
+    }
+    if (st && !first_err) {
+      first_err = st;
+      char buf[160];
+      std::snprintf(buf, sizeof(buf), "signal %d: %s after %d iterations", i,
+                    mpsft_status_string(st), run[i].iter);
+      ctx->err = buf;
+    }
+  }
+  return first_err;
+}
+
+}  // namespace
+
+// ===================================================================== ABI
+extern "C" {
+
+const char *mpsft_status_string(int status) {
+  switch (status) {
+    case MPSFT_OK: return "ok";
+    case MPSFT_ERR_INVALID: return "invalid argument";
+    case MPSFT_ERR_UNSUPPORTED_N: return "unsupported n";
+    case MPSFT_ERR_CUDA: return "CUDA error";
+    case MPSFT_ERR_CAPACITY: return "capacity exceeded";
+    case MPSFT_ERR_ITER_CAP: return "iteration cap reached";
+    case MPSFT_ERR_NONFINITE: return "non-finite values in the bins";
+    case MPSFT_ERR_NOMEM: return "out of device memory";
+    default: return "unknown status";
+  }
+}
+
+int mpsft_ctx_create(int device, mpsft_ctx **out) {
+  if (!out) return MPSFT_ERR_INVALID;
+  *out = nullptr;
+  mpsft_ctx *ctx = new mpsft_ctx;
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return MPSFT_ERR_CUDA;
+  }
+  ctx->stream = ctx->own;
+  LaunchTwiddles(ctx->tw32, ctx->tw64, ctx->stream);
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    mpsft_ctx_destroy(ctx);
+    return MPSFT_ERR_CUDA;
+  }
+  *out = ctx;
+  return MPSFT_OK;
+}
+
+int mpsft_ctx_destroy(mpsft_ctx *ctx) {
+  if (!ctx) return MPSFT_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
+  if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+  if (ctx->tw32) cudaFree(ctx->tw32);
+  if (ctx->tw64) cudaFree(ctx->tw64);
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return MPSFT_OK;
+}
+
+int mpsft_ctx_set_stream(mpsft_ctx *ctx, void *stream) {
+  if (!ctx) return MPSFT_ERR_INVALID;
+  ctx->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->own;
+  return MPSFT_OK;
+}
+
+int mpsft_ctx_set_profiling(mpsft_ctx *ctx, int enable) {
+  if (!ctx) return MPSFT_ERR_INVALID;
+  ctx->profiling = enable != 0;
+  return MPSFT_OK;
+}
+
+const char *mpsft_last_error(const mpsft_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+int mpsft_rng_create(int32_t seed, mpsft_rng **out) {
+  if (!out) return MPSFT_ERR_INVALID;
+  *out = new mpsft_rng;
+  (*out)->eng.seed(seed);
+  return MPSFT_OK;
+}
+int mpsft_rng_destroy(mpsft_rng *rng) {
+  delete rng;
+  return MPSFT_OK;
+}
+int mpsft_rng_seed(mpsft_rng *rng, int32_t seed) {
+  if (!rng) return MPSFT_ERR_INVALID;
+  rng->eng.seed(seed);
+  rng->uid.reset();
+  return MPSFT_OK;
+}
+int32_t mpsft_rng_int32(mpsft_rng *rng) { return rng ? rng->Draw() : -1; }
+
+int32_t mpsft_num_bits(int32_t n, int32_t bins) {
+  return bins > 0 ? NumBits(n, bins) : 0;
+}
+
+int32_t mpsft_window_support(int32_t n, int32_t bins, double delta) {
+  (void)n;
+  if (bins <= 0 || bins % 2 == 0 || !(delta > 0 && delta < 1)) return 0;
+  return MakeWindow(bins, delta).p;
+}
+
+void mpsft_solve_options_default(mpsft_solve_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->trials = 1;
+  o->min_bins = 101;
+  o->window_delta = 1e-6;
+  o->window_threshold = 0.1;
+  o->max_stale_iter = 3;
+  o->precision = MPSFT_PREC_FP32;
+}
+
+int mpsft_signal_upload(mpsft_ctx *ctx, const void *x_host, int64_t n,
+                        int dtype, mpsft_signal **out) {
+  if (!ctx || !x_host || !out) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  if (dtype != MPSFT_C64 && dtype != MPSFT_C128) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "dtype must be MPSFT_C64 or MPSFT_C128");
+  }
+  int rc = CheckN(ctx, n);
+  if (rc) return rc;
+  const size_t bytes = size_t(n) * (dtype == MPSFT_C64 ? 8 : 16);
+  mpsft_signal *s = new mpsft_signal;
+  s->ctx = ctx;
+  s->n = n;
+  s->dtype = dtype;
+  s->owned = true;
+  if (cudaMalloc(&s->d_x, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    return Fail(ctx, MPSFT_ERR_NOMEM, "device allocation of the signal failed");
+  }
+  cudaError_t e = cudaMemcpyAsync(s->d_x, x_host, bytes, cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(s->d_x);
+    delete s;
+    return Fail(ctx, MPSFT_ERR_CUDA, cudaGetErrorString(e));
+  }
+  *out = s;
+  return MPSFT_OK;
+}
+
+int mpsft_signal_wrap_device(mpsft_ctx *ctx, const void *x_device, int64_t n,
+                             int dtype, mpsft_signal **out) {
+  if (!ctx || !x_device || !out) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  if (dtype != MPSFT_C64 && dtype != MPSFT_C128) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "dtype must be MPSFT_C64 or MPSFT_C128");
+  }
+  int rc = CheckN(ctx, n);
+  if (rc) return rc;
+  mpsft_signal *s = new mpsft_signal;
+  s->ctx = ctx;
+  s->n = n;
+  s->dtype = dtype;
+  s->owned = false;
+  s->d_x = const_cast<void *>(x_device);
+  *out = s;
+  return MPSFT_OK;
+}
+
+int mpsft_signal_free(mpsft_signal *sig) {
+  if (!sig) return MPSFT_OK;
+  if (sig->owned && sig->d_x) {
+    if (sig->ctx) cudaStreamSynchronize(sig->ctx->stream);
+    cudaFree(sig->d_x);
+  }
+  delete sig;
+  return MPSFT_OK;
+}
+
+int mpsft_window_table(mpsft_ctx *ctx, int32_t n, int32_t bins, double delta,
+                       double *wt_host, int32_t cap) {
+  if (!ctx || !wt_host) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  int rc = CheckWindow(ctx, bins, delta, false);
+  if (rc) return rc;
+  const WinParams w = MakeWindow(bins, delta);
+  if (cap < w.p) return Fail(ctx, MPSFT_ERR_CAPACITY, "wt buffer smaller than p");
+  Shape s;
+  s.n = n;
+  s.bins_cap = bins;
+  s.rows_cap = 1;
+  s.p2_cap = w.p2;
+  s.m_cap = 1 << FFTLog2(bins);
+  s.tab_cap = 64;
+  Carve probe{nullptr};
+  SigIter it{};
+  int32_t *ctl;
+  CarveSignal(probe, s, &it, &ctl);
+  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 512);
+  if (rc) return rc;
+  Carve cv{ctx->arena};
+  SigIter *d_it = cv.take<SigIter>(1);
+  std::memset(&it, 0, sizeof(it));
+  CarveSignal(cv, s, &it, &ctl);
+  it.active = 1;
+  it.n = n;
+  it.bins = bins;
+  it.p = w.p;
+  it.p2 = w.p2;
+  it.width = w.width;
+  it.sigma_f = w.sigma_f;
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  LaunchWindow(d_it, 1, w.p2, ctx->stream);
+  std::vector<double> half(w.p2 + 1);
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(half.data(), it.wt64,
+                                  sizeof(double) * (w.p2 + 1),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int32_t i = 0; i < w.p; ++i) {
+    const int32_t t = i <= w.p2 ? i : i - w.p;
+    wt_host[i] = half[t < 0 ? -t : t];
+  }
+  return MPSFT_OK;
+}
+
+int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
+                      int32_t bits, double delta, int32_t a, int32_t b,
+                      int32_t c, int32_t q, int precision, double *out,
+                      int out_on_device) {
+  if (!ctx || !out) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  int rc = CheckSignal(ctx, sig);
+  if (rc) return rc;
+  const bool fp64 = precision == MPSFT_PREC_FP64;
+  rc = CheckWindow(ctx, bins, delta, fp64);
+  if (rc) return rc;
+  if (bits < 0 || bits > kMaxBits) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bits must be in [0, 31]");
+  }
+  if (int64_t(bins) << (bits > 0 ? bits - 1 : 0) > INT32_MAX) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bins * 2^(bits-1) overflows int32");
+  }
+  const int32_t n = int32_t(sig->n);
+  Shape s;
+  s.n = n;
+  s.bins_cap = bins;
+  s.rows_cap = 1 + 2 * bits;
+  s.trials = 1;
+  s.p2_cap = MakeWindow(bins, delta).p2;
+  s.m_cap = 1 << FFTLog2(bins);
+  s.tab_cap = 64;
+  s.fp64 = fp64;
+  Carve probe{nullptr};
+  SigIter it{};
+  int32_t *ctl;
+  CarveSignal(probe, s, &it, &ctl);
+  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 512);
+  if (rc) return rc;
+  Carve cv{ctx->arena};
+  SigIter *d_it = cv.take<SigIter>(1);
+  std::memset(&it, 0, sizeof(it));
+  CarveSignal(cv, s, &it, &ctl);
+  const Transform tf{a, b, c, InverseMod(a, n)};
+  FillIter(&it, sig, bins, bits, delta, tf, &q, 1);
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  cudaStream_t st = ctx->stream;
+  LaunchWindow(d_it, 1, it.p2, st);
+  LaunchBluesteinSetup(d_it, 1, it.fft_m, fp64, ctx->tw32, ctx->tw64, st);
+  BinTimer timer{ctx};
+  rc = timer.Begin();
+  if (rc) return rc;
+  LaunchBinFold(d_it, 1, bins, bits, 1, sig->dtype == MPSFT_C128, fp64, st);
+  rc = timer.End();
+  if (rc) return rc;
+  LaunchRowFFT(d_it, 1, it.rows, 1, it.fft_m, fp64, ctx->tw32, ctx->tw64, st);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  const size_t row_bytes = sizeof(double2) * size_t(bins);
+  MPSFT_CUDA(ctx, cudaMemcpy2DAsync(
+                      out, row_bytes, it.ubuf, sizeof(double2) * it.bins_cap,
+                      row_bytes, it.rows,
+                      out_on_device ? cudaMemcpyDeviceToDevice
+                                    : cudaMemcpyDeviceToHost,
+                      st));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  return MPSFT_OK;
+}
+
+int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
+                      double delta, int32_t a, int32_t b, int32_t c, int32_t q,
+                      const int32_t *k0, const double *coef, int64_t m,
+                      double *inout) {
+  if (!ctx || !inout || (m > 0 && (!k0 || !coef))) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  int rc = CheckN(ctx, n);
+  if (rc) return rc;
+  rc = CheckWindow(ctx, bins, delta, false);
+  if (rc) return rc;
+  if (bits < 0 || bits > kMaxBits || m < 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bad bits or mode count");
+  }
+  Shape s;
+  s.n = n;
+  s.bins_cap = bins;
+  s.rows_cap = 1 + 2 * bits;
+  s.trials = 1;
+  s.p2_cap = 1;
+  s.m_cap = 1;
+  s.tab_cap = NextPow2(std::max<int64_t>(64, 4 * m));
+  Carve probe{nullptr};
+  SigIter it{};
+  int32_t *ctl;
+  CarveSignal(probe, s, &it, &ctl);
+  const size_t extra = size_t(m) * (sizeof(int32_t) + sizeof(double2)) + 1024;
+  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + extra);
+  if (rc) return rc;
+  Carve cv{ctx->arena};
+  SigIter *d_it = cv.take<SigIter>(1);
+  std::memset(&it, 0, sizeof(it));
+  CarveSignal(cv, s, &it, &ctl);
+  int32_t *d_k0 = cv.take<int32_t>(size_t(m));
+  double2 *d_coef = cv.take<double2>(size_t(m));
+  const Transform tf{a, b, c, 0};
+  mpsft_signal fake;
+  fake.n = n;
+  FillIter(&it, &fake, bins, bits, delta, tf, &q, 1);
+  it.x = nullptr;
+  cudaStream_t st = ctx->stream;
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
+                                  st));
+  rc = ClearTable(ctx, it, ctl);
+  if (rc) return rc;
+  if (m > 0) {
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_k0, k0, sizeof(int32_t) * m,
+                                    cudaMemcpyHostToDevice, st));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_coef, coef, sizeof(double2) * m,
+                                    cudaMemcpyHostToDevice, st));
+    LaunchTableInsert(d_it, d_k0, d_coef, m, st);
+  }
+  const size_t row_bytes = sizeof(double2) * size_t(bins);
+  MPSFT_CUDA(ctx, cudaMemcpy2DAsync(it.ubuf, sizeof(double2) * it.bins_cap,
+                                    inout, row_bytes, row_bytes, it.rows,
+                                    cudaMemcpyHostToDevice, st));
+  LaunchBucket(d_it, 1, bins, s.tab_cap, st);
+  LaunchDecide(d_it, 1, bins, 1, true, st);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  MPSFT_CUDA(ctx, cudaMemcpy2DAsync(inout, row_bytes, it.ubuf,
+                                    sizeof(double2) * it.bins_cap, row_bytes,
+                                    it.rows, cudaMemcpyDeviceToHost, st));
+  int32_t h_ctl[kCtlWords];
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl),
+                                  cudaMemcpyDeviceToHost, st));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  if (h_ctl[1] & kStatusCapacity) {
+    return Fail(ctx, MPSFT_ERR_CAPACITY, "mode table full");
+  }
+  return MPSFT_OK;
+}
+
+int mpsft_mat_pencil(mpsft_ctx *ctx, const double *u3, int64_t count,
+                     double *sigma, int32_t *vote) {
+  if (!ctx || count < 0 || (count > 0 && (!u3 || !sigma || !vote))) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bad argument");
+  }
+  if (count == 0) return MPSFT_OK;
+  const size_t need = size_t(count) * (3 * sizeof(double2) + 2 * sizeof(double) +
+                                       sizeof(int32_t)) + 1024;
+  int rc = EnsureArena(ctx, need);
+  if (rc) return rc;
+  Carve cv{ctx->arena};
+  double2 *d_u = cv.take<double2>(size_t(count) * 3);
+  double *d_s = cv.take<double>(size_t(count) * 2);
+  int32_t *d_v = cv.take<int32_t>(size_t(count));
+  cudaStream_t st = ctx->stream;
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_u, u3, sizeof(double2) * 3 * count,
+                                  cudaMemcpyHostToDevice, st));
+  LaunchPencil(d_u, count, d_s, d_v, st);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(sigma, d_s, sizeof(double) * 2 * count,
+                                  cudaMemcpyDeviceToHost, st));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(vote, d_v, sizeof(int32_t) * count,
+                                  cudaMemcpyDeviceToHost, st));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  return MPSFT_OK;
+}
+
+int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
+                  const mpsft_iterate_options *opt, mpsft_rng *rng,
+                  int32_t *mm_k, double *mm_c, int32_t *mm_size,
+                  int32_t mm_cap, int32_t *found) {
+  if (!ctx || !opt || !rng || !mm_size || !found || (mm_cap > 0 && (!mm_k || !mm_c))) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  int rc = CheckSignal(ctx, sig);
+  if (rc) return rc;
+  const bool fp64 = opt->precision == MPSFT_PREC_FP64;
+  if (!(opt->window_threshold > 0)) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "window_threshold must be > 0");
+  }
+  if (opt->trials < 1 || opt->trials % 2 == 0 || opt->trials > kMaxTrials) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "trials must be odd and <= 15");
+  }
+  rc = CheckWindow(ctx, opt->bins, opt->window_delta, fp64);
+  if (rc) return rc;
+  if (*mm_size < 0 || *mm_size > mm_cap) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "mm_size out of range");
+  }
+  const int32_t n = int32_t(sig->n);
+  const int32_t bins = opt->bins;
+  const int32_t bits = NumBits(n, bins);
+  Shape s;
+  s.n = n;
+  s.bins_cap = bins;
+  s.rows_cap = 1 + 2 * bits;
+  s.trials = opt->trials;
+  s.p2_cap = MakeWindow(bins, opt->window_delta).p2;
+  s.m_cap = 1 << FFTLog2(bins);
+  s.tab_cap = NextPow2(std::max<int64_t>(64, 4 * (int64_t(*mm_size) + bins)));
+  s.fp64 = fp64;
+  Carve probe{nullptr};
+  SigIter it{};
+  int32_t *ctl;
+  CarveSignal(probe, s, &it, &ctl);
+  const int64_t m0 = *mm_size;
+  const size_t extra = size_t(m0) * (sizeof(int32_t) + sizeof(double2)) + 1024;
+  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + extra);
+  if (rc) return rc;
+  Carve cv{ctx->arena};
+  SigIter *d_it = cv.take<SigIter>(1);
+  std::memset(&it, 0, sizeof(it));
+  CarveSignal(cv, s, &it, &ctl);
+  int32_t *d_k0 = cv.take<int32_t>(size_t(m0));
+  double2 *d_coef = cv.take<double2>(size_t(m0));
+  const Transform tf = DrawTransform(rng, n);
+  int32_t q[kMaxTrials];
+  for (int t = 0; t < opt->trials; ++t) q[t] = rng->Draw() % n;
+  FillIter(&it, sig, bins, bits, opt->window_delta, tf, q, opt->trials);
+  it.bin_thr = opt->bin_threshold;
+  it.sv_thr = opt->sv_threshold;
+  it.win_thr = opt->window_threshold;
+  cudaStream_t st = ctx->stream;
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
+                                  st));
+  rc = ClearTable(ctx, it, ctl);
+  if (rc) return rc;
+  if (m0 > 0) {
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_k0, mm_k, sizeof(int32_t) * m0,
+                                    cudaMemcpyHostToDevice, st));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_coef, mm_c, sizeof(double2) * m0,
+                                    cudaMemcpyHostToDevice, st));
+    LaunchTableInsert(d_it, d_k0, d_coef, m0, st);
+  }
+  std::vector<SigIter> h_its(1, it);
+  BinTimer timer{ctx};
+  rc = LaunchIteration(ctx, d_it, 1, h_its, sig->dtype == MPSFT_C128, fp64,
+                       &timer);
+  if (rc) return rc;
+  int32_t h_ctl[kCtlWords];
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl),
+                                  cudaMemcpyDeviceToHost, st));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  if (h_ctl[1] & kStatusCapacity) {
+    return Fail(ctx, MPSFT_ERR_CAPACITY, "mode table full");
+  }
+  if (h_ctl[1] & kStatusNonFinite) {
+    return Fail(ctx, MPSFT_ERR_NONFINITE, "non-finite values in the bins");
+  }
+  std::vector<std::pair<int32_t, double2>> modes;
+  rc = DownloadTable(ctx, it, &modes);
+  if (rc) return rc;
+  if (int64_t(modes.size()) > mm_cap) {
+    return Fail(ctx, MPSFT_ERR_CAPACITY, "mode map capacity too small");
+  }
+  for (size_t j = 0; j < modes.size(); ++j) {
+    mm_k[j] = modes[j].first;
+    mm_c[2 * j] = modes[j].second.x;
+    mm_c[2 * j + 1] = modes[j].second.y;
+  }
+  *mm_size = int32_t(modes.size());
+  *found = h_ctl[0] ? 1 : 0;
+  return MPSFT_OK;
+}
+
+int mpsft_solve(mpsft_ctx *ctx, const mpsft_signal *sig,
+                const mpsft_solve_options *opt, mpsft_rng *rng,
+                int32_t *out_k, double *out_c, int32_t cap, int32_t *count,
+                mpsft_stats *stats) {
+  if (!ctx || !opt || !rng || !count || (cap > 0 && (!out_k || !out_c))) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  const mpsft_signal *sigs[1] = {sig};
+  mpsft_rng *rngs[1] = {rng};
+  int32_t *ok[1] = {out_k};
+  double *oc[1] = {out_c};
+  return SolveMany(ctx, sigs, opt, 1, rngs, ok, oc, &cap, count, stats);
+}
+
+int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                        const mpsft_solve_options *opts, int32_t nsig,
+                        mpsft_rng *const *rngs, int32_t *const *out_k,
+                        double *const *out_c, const int32_t *cap,
+                        int32_t *count, mpsft_stats *stats) {
+  if (!ctx || !sigs || !opts || !rngs || !out_k || !out_c || !cap || !count) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  return SolveMany(ctx, sigs, opts, nsig, rngs, out_k, out_c, cap, count,
+                   stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Window tables, FFT twiddles and Bluestein chirp tables.
+//
+// Window (src/window.cc:28-75): wt(t) = w * sinc(pi t w) * exp(-2 (pi t sigma_f)^2)
+// with w = 1/(2 bins); wt(0) = w. The window is even, so only |t| in
+// [0, p2] is stored. Computed in FP64 and also rounded to FP32.
+//
+// Bluestein (chirp-z) form of the size-B DFT X[k] = sum_j y[j] e^{-2 pi i jk/B}:
+//   X[k] = chirp[k] * sum_j (y[j] chirp[j]) * conj(chirp[k - j]),
+//   chirp[j] = e^{-pi i j^2 / B} with j^2 reduced mod 2B exactly,
+// a circular convolution of length M = 2^ceil(log2(2B - 1)) done with the
+// radix-2 shared-memory FFT; chat = FFT_M of the conjugate chirp sequence.
+#include "fft.cuh"
+#include "launch.h"
+
+namespace mpsft {
+
+namespace {
+
+__global__ void k_twiddles(float2 *tw32, double2 *tw64) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kMaxFFT / 2) return;
+  double s, c;
+  sincospi(-2.0 * double(e) / double(kMaxFFT), &s, &c);
+  tw64[e] = make_double2(c, s);
+  tw32[e] = make_float2(float(c), float(s));
+}
+
+// sin(x)/x with the reference's Taylor guard (src/sincos.cc:69-88).
+__device__ double SincPi(double x) {
+  const double t0 = 2.220446049250313080847e-16;  // DBL_EPSILON
+  const double t2 = 1.4901161193847656e-08;       // sqrt(t0)
+  const double tn = 1.220703125e-04;              // sqrt(t2)
+  if (x < 0) x = -x;
+  if (x >= tn) return sin(x) / x;
+  double r = 1.0;
+  if (x >= t0) {
+    const double x2 = x * x;
+    r -= x2 / 6.0;
+    if (x >= t2) r += (x2 * x2) / 120.0;
+  }
+  return r;
+}
+
+__global__ void k_window(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > it.p2) return;
+  double v;
+  if (i == 0) {
+    v = it.width;
+  } else {
+    const double t = double(i);
+    const double u = __dmul_rn(__dmul_rn(t, M_PI), it.sigma_f);
+    v = __dmul_rn(__dmul_rn(it.width, SincPi(__dmul_rn(__dmul_rn(t, M_PI),
+                                                       it.width))),
+                  exp(__dmul_rn(__dmul_rn(-2.0, u), u)));
+  }
+  it.wt64[i] = v;
+  it.wt32[i] = float(v);
+}
+
+template <typename V>
+__global__ void k_bluestein_setup(const SigIter *__restrict__ its,
+                                  const V *__restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *a = reinterpret_cast<V *>(smem_raw);
+  const SigIter &it = its[blockIdx.x];
+  if (!it.active) return;
+  const int B = it.bins, M = it.fft_m;
+  V *chirp = reinterpret_cast<V *>(it.chirp);
+  V *chat = reinterpret_cast<V *>(it.chat);
+  const int64_t twoB = 2 * int64_t(B);
+  for (int j = threadIdx.x; j < M; j += blockDim.x) {
+    a[j] = vmake2(0.0, 0.0, (V *)nullptr);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < B; j += blockDim.x) {
+    const int64_t j2 = (int64_t(j) * j) % twoB;
+    double s, c;
+    sincospi(-double(j2) / double(B), &s, &c);
+    chirp[j] = vmake2(c, s, (V *)nullptr);
+    const V cc = vmake2(c, -s, (V *)nullptr);  // conj(chirp[j])
+    a[j] = cc;
+    if (j > 0) a[M - j] = cc;
+  }
+  __syncthreads();
+  BlockFFT(a, M, it.fft_log2m, tw, false);
+  for (int j = threadIdx.x; j < M; j += blockDim.x) chat[j] = a[j];
+}
+
+}  // namespace
+
+void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s) {
+  const int n = kMaxFFT / 2;
+  k_twiddles<<<(n + 255) / 256, 256, 0, s>>>(tw32, tw64);
+}
+
+void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
+  dim3 grid((max_p2 + 1 + 255) / 256, nsig);
+  k_window<<<grid, 256, 0, s>>>(d_its);
+}
+
+void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
+                          const float2 *tw32, const double2 *tw64,
+                          cudaStream_t s) {
+  if (fp64) {
+    const size_t sm = size_t(max_m) * sizeof(double2);
+    cudaFuncSetAttribute(k_bluestein_setup<double2>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    k_bluestein_setup<double2><<<nsig, 1024, sm, s>>>(d_its, tw64);
+  } else {
+    const size_t sm = size_t(max_m) * sizeof(float2);
+    cudaFuncSetAttribute(k_bluestein_setup<float2>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    k_bluestein_setup<float2><<<nsig, 1024, sm, s>>>(d_its, tw32);
+  }
+}
+
+}  // namespace mpsft

@@ -1,0 +1,54 @@
+// Host-side launchers of the sm_103a kernels (one translation unit each).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace mpsft {
+
+// e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2, for the FFT twiddles.
+void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s);
+
+// Window tables wt32 / wt64 at |t| in [0, p2] of every active signal.
+void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s);
+
+// Bluestein chirp and FFT(conjugate chirp) of every active signal.
+// fp64 selects double tables.
+void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
+                          const float2 *tw32, const double2 *tw64,
+                          cudaStream_t s);
+
+// Fold of the windowed, modulated, permuted samples (the time-domain part of
+// BinInTime::Run). x_c128 selects double2 input, fp64 the FP64 arithmetic.
+void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
+                   int max_trials, bool x_c128, bool fp64, cudaStream_t s);
+
+// Size-B FFT of every folded row, times e^{2 pi i b q / n}, into ubuf.
+void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
+                  int max_trials, int max_m, bool fp64, const float2 *tw32,
+                  const double2 *tw64, cudaStream_t s);
+
+// Lists of table slots per bin (counting sort by bin).
+void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
+                  cudaStream_t s);
+
+// Per-bin mode subtraction, energy test, pencil votes and coefficient
+// estimation (the bin loop of Iterate); writes the candidates. With
+// subtract_only, only the mode subtraction of BinInFreq::Run is applied to
+// ubuf in place.
+void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
+                  bool subtract_only, cudaStream_t s);
+
+// Candidates -> mode table (mm[k0] += coef).
+void LaunchMerge(const SigIter *d_its, int nsig, int max_bins, cudaStream_t s);
+
+// Inserts / accumulates explicit (k0, coef) pairs into one signal's table.
+void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,
+                       const double2 *coef, int64_t m, cudaStream_t s);
+
+// Batched 2x2 pencils.
+void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
+                  int32_t *vote, cudaStream_t s);
+
+}  // namespace mpsft

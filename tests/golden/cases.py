@@ -1,0 +1,71 @@
+"""Inputs of the golden cases, regenerated deterministically on any host.
+
+The outputs for these inputs were produced by the reference itself
+(jiaweichiu/mpsft sources compiled against the oracle's stand-in headers, see
+oracle/Makefile) and stored in ref_golden.npz by make_golden.py. Signals are
+not stored: they are rebuilt here from closed-form modes or numpy PCG64 seeds.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from mpsft_gb300.signals import make_signal
+
+
+def as_i32(v: int) -> int:
+    """C++ int32_t conversion of an integer literal (wraps like the reference's
+    Transform(n, 0x3FFFFFFF, 0xEEEEEEEE, 0xDDDDDD), src/binner_test.cc:124)."""
+    return int(np.array(v & 0xFFFFFFFF, np.uint32).astype(np.int32))
+
+
+def evaluate_modes(n: int, modes: dict) -> np.ndarray:
+    """EvaluateModes (src/gen.cc:41-53): x_t = sum c e^{2 pi i (k t mod n)/n}."""
+    t = np.arange(n, dtype=np.int64)
+    x = np.zeros(n, np.complex128)
+    for k, c in modes.items():
+        ang = 2.0 * np.pi * (((k * t) % n).astype(np.float64) / n)
+        x += c * (np.cos(ang) + 1j * np.sin(ang))
+    return x
+
+
+# Known-answer binning case of src/binner_test.cc:54-103.
+KNOWN = dict(n=1109, bins=5, bits=2, q=106, a=3, b=847, c=45, delta=1e-6,
+             modes={550: 2.0 + 0.0j})
+# Large-n overflow case of src/binner_test.cc:112-143 (q = 0xFFFFFF).
+BIGGER = dict(n=1048573, bins=5, bits=2, q=0xFFFFFF, a=0x3FFFFFFF,
+              b=as_i32(0xEEEEEEEE), c=0xDDDDDD, delta=1e-6,
+              modes={565336: 2.0 + 1.0j})
+
+# Random-signal binning cases: (name, n, bins, delta, a, b, c, q, seed).
+RANDOM_BINS = [
+    ("pow2_b101", 1 << 16, 101, 1e-5, 12345, 678, 910, 4444, 11),
+    ("prime_b101", 65537, 101, 1e-5, 12345, 678, 910, 4444, 12),
+    ("pow2_b2001", 1 << 20, 2001, 1e-5, 987653, 31337, 271828, 99991, 13),
+    ("prime_b51", 1048573, 51, 1e-6, 76543, 5, 123456, 1000003, 14),
+]
+
+# Solve cases: (name, n, S, sigma, trials, min_bins, delta, seed_signal,
+# seed_rng, magnitude).
+SOLVES = [
+    ("pow2_s50", 1 << 16, 50, 1e-6, 1, 51, 1e-5, 21, 123537, "unit"),
+    ("prime_s50", 65537, 50, 1e-6, 1, 51, 1e-5, 22, 123537, "unit"),
+    ("pow2_s200_t3", 1 << 18, 200, 1e-3, 3, 51, 1e-5, 23, 123537, "unit"),
+    ("config1", 1 << 20, 50, 1e-6, 1, 51, 1e-5, 1, 123537, "unit"),
+    ("pow2_s300_logu", 1 << 20, 300, None, 1, 51, 1e-5, 24, 123537, "loguniform"),
+]
+
+
+def random_signal(n: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((2, n))
+    return v[0] + 1j * v[1]
+
+
+def solve_signal(case) -> tuple[np.ndarray, float]:
+    name, n, s, sigma, trials, min_bins, delta, sseed, rseed, mag = case
+    if mag == "unit":
+        sig = make_signal(n, s, sseed, sigma=sigma, dtype=np.complex128)
+    else:
+        sig = make_signal(n, s, sseed, magnitude="loguniform", snr_db=60.0,
+                          dtype=np.complex64)
+    return sig.x, sig.sigma

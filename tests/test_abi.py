@@ -1,0 +1,67 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol that
+include/mpsft.h declares, and its host-side logic (RNG draw order, NumBits,
+window support, error statuses) matches the reference / oracle."""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+
+import numpy as np
+import pytest
+
+import mpsft_gb300 as m
+
+
+def test_library_exports_header_symbols(lib):
+    declared = m.exported_symbols()
+    assert len(declared) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", m.LIB_PATH],
+                         capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    for s in declared:
+        assert getattr(lib, s) is not None
+
+
+def test_rng_matches_reference(lib, golden):
+    r = m.Rng(123534)
+    assert [r.int32() for _ in range(16)] == golden["rng_123534"].tolist()
+    r.seed(123534)
+    assert r.int32() == int(golden["rng_123534"][0])
+
+
+def test_num_bits_and_window_support(lib, port):
+    for n in (1109, 4099, 1 << 16, 65537, 1 << 20, 1 << 22, 1048573):
+        for bins in (1, 5, 11, 51, 101, 501, 2001, 8001):
+            assert lib.mpsft_num_bits(n, bins) == port.num_bits(n, bins)
+    for bins in (5, 11, 51, 2001, 8001):
+        for delta in (1e-5, 1e-6):
+            p = lib.mpsft_window_support(1 << 20, bins, delta)
+            assert p == port.window(1 << 20, bins, delta).size
+    assert lib.mpsft_window_support(1 << 20, 100, 1e-5) == 0  # even bins
+
+
+def test_status_strings(lib):
+    for code in range(8):
+        assert lib.mpsft_status_string(code)
+
+
+def test_no_gpu_is_an_error_not_a_crash(lib):
+    """On a host without a GPU, creating a context returns a status."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    h = ctypes.c_void_p()
+    rc = lib.mpsft_ctx_create(0, ctypes.byref(h))
+    assert rc == m.ERR_CUDA and not h.value
+
+
+def test_null_arguments_are_rejected(lib):
+    assert lib.mpsft_ctx_create(0, None) == m.ERR_INVALID
+    assert lib.mpsft_solve(None, None, None, None, None, None, 0, None, None) \
+        == m.ERR_INVALID
+    assert lib.mpsft_rng_seed(None, 1) == m.ERR_INVALID

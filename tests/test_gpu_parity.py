@@ -1,0 +1,246 @@
+"""Parity of the CUDA path (called through the C ABI) with the reference.
+
+Bins and operators are compared with the reference's own outputs
+(tests/golden/ref_golden.npz) and with the oracle; whole solves must return
+the reference's exact frequency set.
+
+Tolerances (stated per result):
+  * FP64 path: bins within 1e-11 of max|U|; coefficients within 1e-9
+    (relative, norm over the common set).
+  * FP32 path: bins within 1e-5 of max|U| (FP32 gather/fold/FFT, FP64 after);
+    coefficients within 1e-5 relative (the precision-error target).
+  * frequency sets: identical (bit-exact k0 values) for both paths.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cases
+import mpsft_gb300 as m
+
+pytestmark = pytest.mark.gpu
+
+TOL_BINS = {m.FP64: 1e-11, m.FP32: 1e-5}
+TOL_COEF = {m.FP64: 1e-9, m.FP32: 1e-5}
+PRECS = [m.FP64, m.FP32]
+PREC_IDS = ["fp64", "fp32"]
+
+
+def rel_err(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def coef_err(got: dict, want_k, want_c):
+    d = np.array([got[int(k)] for k in want_k]) - np.asarray(want_c)
+    return float(np.linalg.norm(d) / np.linalg.norm(want_c))
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+def test_known_answer_bins(ctx, golden, prec):
+    kc = cases.KNOWN
+    x = cases.evaluate_modes(kc["n"], kc["modes"])
+    sig = ctx.upload(x)
+    u = ctx.bin_in_time(sig, kc["bins"], kc["bits"], kc["delta"], kc["a"], kc["b"],
+                        kc["c"], kc["q"], precision=prec)
+    # src/binner_test.cc:74-75
+    assert abs(u[0, 1] - (1.12652 - 0.108838j)) < 1e-5 * 2
+    assert rel_err(u, golden["known_v4"]) < TOL_BINS[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+def test_bigger_bins(ctx, golden, prec):
+    bc = cases.BIGGER
+    x = cases.evaluate_modes(bc["n"], bc["modes"])
+    sig = ctx.upload(x)
+    u = ctx.bin_in_time(sig, bc["bins"], bc["bits"], bc["delta"], bc["a"], bc["b"],
+                        bc["c"], bc["q"], precision=prec)
+    assert rel_err(u, golden["bigger_v4"]) < 10 * TOL_BINS[prec]
+    # time + freq = 0 (src/binner_test.cc:140-142)
+    ks = np.array(list(bc["modes"]), np.int32)
+    cs = np.array(list(bc["modes"].values()))
+    f = ctx.bin_in_freq(np.zeros_like(u), bc["n"], bc["bins"], bc["bits"],
+                        bc["delta"], bc["a"], bc["b"], bc["c"], bc["q"], ks, cs)
+    assert rel_err(f, golden["bigger_freq"]) < 1e-12
+    assert np.abs(u[0] + f[0]).max() < 1e-5
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+@pytest.mark.parametrize("case", cases.RANDOM_BINS, ids=[c[0] for c in cases.RANDOM_BINS])
+def test_random_bins(ctx, golden, case, prec):
+    name, n, bins, delta, a, b, c, q, seed = case
+    x = cases.random_signal(n, seed)
+    sig = ctx.upload(x)
+    bits = m.load_library().mpsft_num_bits(n, bins)
+    u = ctx.bin_in_time(sig, bins, bits, delta, a, b, c, q, precision=prec)
+    assert rel_err(u, golden[f"rb_{name}"]) < TOL_BINS[prec]
+
+
+@pytest.mark.parametrize("case", cases.RANDOM_BINS, ids=[c[0] for c in cases.RANDOM_BINS])
+def test_bin_in_freq(ctx, golden, case):
+    name, n, bins, delta, a, b, c, q, seed = case
+    bits = m.load_library().mpsft_num_bits(n, bins)
+    f = ctx.bin_in_freq(golden[f"rb_{name}"], n, bins, bits, delta, a, b, c, q,
+                        golden[f"rf_{name}_k"], golden[f"rf_{name}_c"])
+    assert rel_err(f, golden[f"rf_{name}"]) < 1e-12
+
+
+def test_pencil_known_answers(ctx):
+    u = np.array([[-2.3 + 5.2j, -5.5 - 3.1j, 4.0 + 3.0j],
+                  [2.3 + 5.2j, 5.5 - 3.1j, 4.0 + 3.0j],
+                  [-15.3 - 5.2j, 8.0 + 3.0j, -1.5 + 3.5j]])
+    sig, vote = ctx.mat_pencil(u)
+    want = np.array([[11.34419934, 0.91057194], [9.80673965, 5.77476038],
+                     [21.27794592, 12.53032391]])
+    assert np.allclose(sig, want, rtol=1.2e-5, atol=0)
+    assert vote.tolist() == [False, True, False]
+
+
+def test_pencil_matches_oracle(ctx, port):
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((500, 3)) + 1j * rng.standard_normal((500, 3))
+    sig, vote = ctx.mat_pencil(u)
+    for i in range(500):
+        s0, s1, v = port.mat_pencil(*u[i])
+        assert abs(sig[i, 0] - s0) <= 1e-13 * s0 and abs(sig[i, 1] - s1) <= 1e-12 * s0
+        assert vote[i] == v
+
+
+def test_window_table(ctx, golden):
+    wt = ctx.window_table(1109, 5, 1e-6)
+    assert rel_err(wt, golden["window_1109_5_1e-6"]) < 1e-14
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+def test_iterate_matches_reference(ctx, golden, prec):
+    case = cases.SOLVES[2]
+    x, sigma = cases.solve_signal(case)
+    sig = ctx.upload(np.asarray(x, np.complex128))
+    rng = m.Rng(4242)
+    mm: dict = {}
+    for i, bins in enumerate((401, 201)):
+        found, mm = ctx.iterate(sig, rng, bins, window_delta=1e-5, trials=3,
+                                bin_threshold=3 * sigma / np.sqrt(bins),
+                                window_threshold=0.1,
+                                sv_threshold=sigma / np.sqrt(bins), mm=mm,
+                                precision=prec)
+        assert sorted(mm) == golden[f"iter{i}_k"].tolist()
+        assert coef_err(mm, golden[f"iter{i}_k"], golden[f"iter{i}_c"]) < TOL_COEF[prec]
+        assert int(found) == int(golden[f"iter{i}_found"][0])
+
+
+def _solve(ctx, x, s, sigma, rseed, trials, min_bins, delta, prec, **kw):
+    sig = ctx.upload(x)
+    opt = ctx.solve_options(s, sigma, trials=trials, min_bins=min_bins,
+                            window_delta=delta, window_threshold=0.1,
+                            max_stale_iter=5, precision=prec, **kw)
+    return ctx.solve(sig, m.Rng(rseed), opt)
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+@pytest.mark.parametrize("case", cases.SOLVES, ids=[c[0] for c in cases.SOLVES])
+def test_solve_matches_reference(ctx, golden, case, prec):
+    name, n, s, _, trials, min_bins, delta, _, rseed, _ = case
+    x, sigma = cases.solve_signal(case)
+    modes, st = _solve(ctx, x, s, sigma, rseed, trials, min_bins, delta, prec)
+    want_k = golden[f"solve_{name}_k"]
+    assert sorted(modes) == want_k.tolist()
+    assert coef_err(modes, want_k, golden[f"solve_{name}_c"]) < TOL_COEF[prec]
+    assert st.iterations > 0 and st.found == len(modes)
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+def test_config2_full_size_matches_oracle(ctx, port, prec):
+    """N = 2^22, S = 1000, |c| log-uniform [1e-2, 1], 60 dB: same frequency set
+    as the oracle (FP64, same draws); coefficient precision error within the
+    stated tolerance; algorithm error vs an FP64 dense FFT reported."""
+    from mpsft_gb300.signals import config2
+
+    sgl = config2(seed=7)
+    want, _ = port.demo1_run(sgl.x.astype(np.complex128), 1000, sgl.sigma, 123537,
+                             min_bins=51, window_delta=1e-5, max_stale_iter=5)
+    got, st = _solve(ctx, sgl.x, 1000, sgl.sigma, 123537, 1, 51, 1e-5, prec)
+    assert sorted(got) == sorted(want)
+    wk = np.array(sorted(want))
+    err = coef_err(got, wk, [want[k] for k in wk])
+    assert err < TOL_COEF[prec], err
+    xf = np.fft.fft(sgl.x.astype(np.complex128)) / sgl.n
+    hits = np.array(sorted(set(got) & set(sgl.k.tolist())))
+    alg = np.linalg.norm([got[k] - xf[k] for k in hits]) / np.linalg.norm(xf[hits])
+    print(f"prec={prec} iterations={st.iterations} found={len(got)} "
+          f"precision_err={err:.2e} algorithm_err={alg:.2e}")
+    assert alg < 1e-2
+
+
+def test_batched_equals_single(ctx):
+    from mpsft_gb300.signals import make_signal
+
+    sigs, opts, rngs, singles = [], [], [], []
+    for i, (n, s) in enumerate([(1 << 16, 40), (1 << 18, 120), (65537, 60)]):
+        sg = make_signal(n, s, 100 + i, sigma=1e-5)
+        sigs.append(ctx.upload(sg.x))
+        opts.append(ctx.solve_options(s, sg.sigma, min_bins=51, window_delta=1e-5,
+                                      max_stale_iter=5))
+        rngs.append(m.Rng(777 + i))
+        singles.append(ctx.solve(sigs[-1], m.Rng(777 + i), opts[-1])[0])
+    out, stats = ctx.solve_batched(sigs, rngs, opts)
+    for (k, c), single, st in zip(out, singles, stats):
+        assert k.tolist() == sorted(single)
+        assert np.array_equal(c, np.array([single[kk] for kk in sorted(single)]))
+        assert st["status"] == 0
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+def test_deterministic(ctx, prec):
+    from mpsft_gb300.signals import make_signal
+
+    sg = make_signal(1 << 18, 200, 5, magnitude="loguniform", snr_db=50.0)
+    sig = ctx.upload(sg.x)
+    opt = ctx.solve_options(200, sg.sigma, min_bins=51, window_delta=1e-5,
+                            max_stale_iter=5, precision=prec)
+    k1, c1, _ = ctx.solve_arrays(sig, m.Rng(9), opt)
+    k2, c2, _ = ctx.solve_arrays(sig, m.Rng(9), opt)
+    assert np.array_equal(k1, k2) and np.array_equal(c1.view(np.uint64),
+                                                     c2.view(np.uint64))
+
+
+# ------------------------------------------------------------ error paths
+def test_errors_are_statuses(ctx):
+    from mpsft_gb300.signals import make_signal
+
+    with pytest.raises(m.MpsftError) as e:
+        ctx.upload(np.zeros(1000, np.complex64))  # composite, not a power of 2
+    assert e.value.status == m.ERR_UNSUPPORTED_N
+    sg = make_signal(1 << 14, 30, 1, sigma=1e-6)
+    sig = ctx.upload(sg.x)
+    with pytest.raises(m.MpsftError) as e:
+        ctx.bin_in_time(sig, 100, 3, 1e-5, 3, 1, 1, 1)  # even bins
+    assert e.value.status == m.ERR_INVALID
+    with pytest.raises(m.MpsftError) as e:
+        ctx.solve(sig, m.Rng(1), ctx.solve_options(30, 1e-6, trials=2))
+    assert e.value.status == m.ERR_INVALID
+    # iteration cap: stop with a status, never spin
+    with pytest.raises(m.MpsftError) as e:
+        ctx.solve(sig, m.Rng(1), ctx.solve_options(30, 1e-6, min_bins=51,
+                                                  max_stale_iter=5, max_iter=1))
+    assert e.value.status == m.ERR_ITER_CAP
+    # mode table too small for what is found
+    with pytest.raises(m.MpsftError) as e:
+        ctx.solve(sig, m.Rng(1), ctx.solve_options(30, 1e-6, min_bins=51,
+                                                  max_stale_iter=5,
+                                                  mode_capacity=16))
+    assert e.value.status == m.ERR_CAPACITY
+    # a NaN in the signal is reported, not looped on
+    bad = sg.x.copy()
+    bad[::16] = np.nan
+    sig2 = ctx.upload(bad)
+    with pytest.raises(m.MpsftError) as e:
+        ctx.solve(sig2, m.Rng(1), ctx.solve_options(30, 1e-6, min_bins=51,
+                                                   max_stale_iter=5))
+    assert e.value.status == m.ERR_NONFINITE
+    # the context stays usable afterwards
+    modes, _ = ctx.solve(sig, m.Rng(1), ctx.solve_options(30, 1e-6, min_bins=51,
+                                                         max_stale_iter=5))
+    assert len(modes) >= 30
