@@ -40,6 +40,7 @@ __device__ inline double2 to_d2(double2 a) { return a; }
 template <typename V>
 __device__ void BlockFFT(V *a, int m, int log2m, const V *__restrict__ tw,
                          bool inverse) {
+  if (log2m == 0) return;  // a 1-point transform is the identity
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const int j = int(__brev(uint32_t(i)) >> (32 - log2m));
     if (j > i) {
