@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Benchmark of the MPSFT recovery loop on GB300.
+
+Workload (one "step"): a batched recovery (the Demo1::Run loop of
+jiaweichiu/mpsft, src/demo1.cc:36-59) of G independent synthetic signals of
+the headline configuration: N = 2^22 complex64 samples, S = 1000 modes at
+distinct uniform-random frequencies, |c| log-uniform in [1e-2, 1], uniform
+phase, complex Gaussian noise at 60 dB SNR; reference parameters trials = 1,
+window_delta = 1e-5, window_threshold = 0.1, max_stale_iter = 5,
+min_bins = 51 (src/demo1_bench.cc:34-39), thresholds 3 sigma/sqrt(B) and
+sigma/sqrt(B). FP32 gather/fold/FFT, FP64 pencil and coefficients.
+
+Printed: one JSON line. ``value`` is recoveries per second with the signals
+resident in HBM (G x 32 MiB > L2, so no L2 flush is needed); ``e2e`` is the
+same through the public API from pinned host buffers (host-to-device copy of
+every signal and device-to-host read of every result inside the timed region).
+
+``--impl reference`` times the reference's algorithm on the host cores: the
+oracle's FP64 restatement (oracle/liboracle.so), one process per core, each
+recovering its own signal of the same configuration.
+
+Multi-GPU: one process per GPU under torchrun; every rank recovers its own G
+signals (independent replicas, no collective on the data path); the time is the
+maximum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("solves/s, N=2^22 S=1000: batched FP32 vs plain GPU @ coef err≤1e-5; "
+          "bin GB/s")
+N = 1 << 22
+S = 1000
+SEED_RNG = 123537
+WORKLOAD = ("MPSFT recovery (Demo1::Run loop), N=2^22 complex64, S=1000, "
+            "|c| log-uniform [1e-2,1], 60 dB SNR, trials=1, delta=1e-5, "
+            "min_bins=51, max_stale_iter=5")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--batch", type=int, default=8, help="signals per step per GPU")
+    p.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    p.add_argument("--cpu-seconds", type=float, default=10.0,
+                   help="bounded CPU-baseline sample length")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def solve_opts(ctx, sigma, precision):
+    import mpsft_gb300 as m
+    return ctx.solve_options(S, sigma, trials=1, min_bins=51, window_delta=1e-5,
+                             window_threshold=0.1, max_stale_iter=5,
+                             precision=precision)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in out.splitlines():
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def _cpu_worker_init(seed):
+    global _W_SIG
+    from mpsft_gb300.signals import config2
+    _W_SIG = config2(seed)
+
+
+def _cpu_worker_solve(rseed):
+    from oracle import oracle
+    port = oracle.Oracle("port")
+    t0 = time.perf_counter()
+    modes, _ = port.demo1_run(_W_SIG.x.astype(np.complex128), S, _W_SIG.sigma, rseed,
+                              min_bins=51, window_delta=1e-5, max_stale_iter=5)
+    return time.perf_counter() - t0, len(modes)
+
+
+def cpu_baseline_single(seconds: float) -> dict:
+    """The oracle port on one host core, a bounded sample of whole solves."""
+    from mpsft_gb300.signals import config2
+    from oracle import oracle
+    if not oracle.available("port"):
+        oracle.build_port()
+    port = oracle.Oracle("port")
+    sg = config2(1001)
+    x = sg.x.astype(np.complex128)
+    done, t_total = 0, 0.0
+    while t_total < seconds or done == 0:
+        t0 = time.perf_counter()
+        port.demo1_run(x, S, sg.sigma, SEED_RNG + done, min_bins=51,
+                       window_delta=1e-5, max_stale_iter=5)
+        t_total += time.perf_counter() - t0
+        done += 1
+    return {"value": done / t_total, "unit": "solves/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{done} full config-2 recoveries on 1 core "
+                      f"({t_total:.1f} s, oracle/mpsft_oracle.cc, -O2 FP64)"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import oracle
+    if not oracle.available("port"):
+        oracle.build_port()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") \
+        else (os.cpu_count() or 1)
+    ctxm = mp.get_context("spawn")
+    step_times = []
+    with ctxm.Pool(cores, initializer=_cpu_worker_init, initargs=(2024,)) as pool:
+        # warm-up: every worker builds its signal and runs once
+        for w in range(args.warmup):
+            pool.map(_cpu_worker_solve, [SEED_RNG + 1000 * w + i for i in range(cores)])
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            pool.map(_cpu_worker_solve, [SEED_RNG + 77 * s + i for i in range(cores)])
+            step_times.append(time.perf_counter() - t0)
+    total = sum(step_times)
+    value = cores * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "batch": cores,
+                   "implementation": "oracle port of the reference algorithm, "
+                                     "one process per host core"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{args.steps} steps x {cores} recoveries, one "
+                                   f"per core"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU arm
+def load_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic() -> float | None:
+    """DRAM bytes per gathered sample of the binning kernel, from the ncu
+    summary committed under profiles/ (None when absent)."""
+    p = os.path.join(ROOT, "profiles", "bin_fold_config2.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_gather:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gpu(args) -> None:
+    import torch
+    import mpsft_gb300 as m
+    from mpsft_gb300.signals import config2
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    if not os.path.exists(m.LIB_PATH):
+        raise SystemExit("library not built: run __graft_entry__.build() first")
+
+    G = args.batch
+    sigs_host = [config2(10_000 + rank * G + i) for i in range(G)]
+    ctx = m.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    # pinned host copies for the end-to-end leg
+    pinned = []
+    for sg in sigs_host:
+        t = torch.empty(N, dtype=torch.complex64, pin_memory=True)
+        t.numpy()[:] = sg.x
+        pinned.append(t)
+    sigs = [ctx.upload(sg.x) for sg in sigs_host]
+    opts = [solve_opts(ctx, sg.sigma, m.FP32) for sg in sigs_host]
+
+    def step(profile=False):
+        rngs = [m.Rng(SEED_RNG + i) for i in range(G)]
+        return ctx.solve_batched(sigs, rngs, opts)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    # ---- device-resident timed region (also times every binning launch)
+    ctx.set_profiling(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    bin_ms = 0.0
+    bin_bytes = 0
+    bin_launches = 0
+    iters = []
+    launches = 0
+    for _ in range(args.steps):
+        out, stats = step()
+        bin_ms += stats[0]["bin_ms"]
+        bin_launches += stats[0]["bin_launches"]
+        bin_bytes += sum(s["bin_bytes"] for s in stats)
+        iters += [s["iterations"] for s in stats]
+        launches += stats[0]["kernel_launches"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ctx.set_profiling(False)
+    ms = ev0.elapsed_time(ev1)
+    t_rank = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t_rank, op=dist.ReduceOp.MAX)
+    ms_max = float(t_rank.item())
+    value = world * G * args.steps / (ms_max / 1e3)
+
+    # ---- end to end through the public API from pinned host buffers
+    h2d = G * N * 8
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    d2h = 0
+    for _ in range(args.steps):
+        for sg, pin in zip(sigs, pinned):
+            sg.write(pin.numpy())
+        out, stats = step()
+        d2h += sum(k.nbytes + c.nbytes for k, c in out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e_ms = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(e_ms, op=dist.ReduceOp.MAX)
+    e2e_value = world * G * args.steps / (float(e_ms.item()) / 1e3)
+
+    # ---- plain per-signal FP64 path and precision error (rank 0, one signal)
+    extra = {}
+    if rank == 0:
+        sg0 = sigs_host[0]
+        o64 = solve_opts(ctx, sg0.sigma, m.FP64)
+        k64, c64, _ = ctx.solve_arrays(sigs[0], m.Rng(SEED_RNG), o64)  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            k64, c64, st64 = ctx.solve_arrays(sigs[0], m.Rng(SEED_RNG), o64)
+        torch.cuda.synchronize()
+        t64 = (time.perf_counter() - t0) / reps
+        k32, c32, _ = ctx.solve_arrays(sigs[0], m.Rng(SEED_RNG), opts[0])
+        same = bool(np.array_equal(k32, k64))
+        perr = float(np.linalg.norm(c32 - c64) / np.linalg.norm(c64)) if same else None
+        extra = {"plain_fp64_gpu": {"value": 1.0 / t64, "unit": "solves/s",
+                                    "ms_per_solve": 1e3 * t64,
+                                    "iterations": st64.iterations},
+                 "fp32_vs_fp64": {"same_frequency_set": same,
+                                  "coef_precision_err": perr}}
+
+    if rank == 0:
+        peaks = load_peaks()
+        achieved = (bin_bytes / (bin_ms / 1e3)) / 1e9 if bin_ms > 0 else None
+        gathers_per_launch = None
+        traffic_per_gather = profile_traffic()
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch_per_gpu": G,
+                       "precision": "f32 gather/fold/FFT, f64 pencil+coefficients",
+                       "l2": f"inputs larger than L2: {G} x 32 MiB signals resident",
+                       "parallelism": f"replicas x{world}",
+                       "iterations_mean": float(np.mean(iters))},
+            "e2e": {"value": e2e_value, "unit": "solves/s",
+                    "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": int(d2h // max(args.steps, 1))},
+            "roofline": {"bound": "hbm", "achieved": achieved,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+                         "traffic": traffic_per_gather,
+                         "kernel": "k_bin_fold32 (gather/window/modulate/fold)",
+                         "bytes_model": "32 B sector per gathered sample + window "
+                                        "table + fold output",
+                         "launches": bin_launches,
+                         "kernel_ms": bin_ms,
+                         "peak_source": peaks["source"]},
+            "clocks": clk,
+            "gpu_launches": int(launches),
+        }
+        line.update(extra)
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_single(args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

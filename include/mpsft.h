@@ -91,6 +91,10 @@ int mpsft_signal_upload(mpsft_ctx *ctx, const void *x_host, int64_t n,
 int mpsft_signal_wrap_device(mpsft_ctx *ctx, const void *x_device, int64_t n,
                              int dtype, mpsft_signal **out);
 int mpsft_signal_free(mpsft_signal *sig);
+/* Copies n new samples (the signal's own n and dtype) from host memory into
+ * an existing signal; pinned host memory makes the copy asynchronous with
+ * respect to the host until the next solve call. */
+int mpsft_signal_write(mpsft_ctx *ctx, mpsft_signal *sig, const void *x_host);
 
 /* ---- BinInTime::Run ------------------------------------------------------- */
 /* Overwrites out with the (1 + 2*bits) x bins bin matrix of signal sig for the
@@ -164,8 +168,9 @@ typedef struct {
   int64_t bin_bytes;      /* algorithmic bytes of the binning launches       */
   int32_t bin_launches;   /* binning launches timed (profiling on)           */
   double bin_ms;          /* summed binning-kernel time (profiling on)       */
-  int32_t escalated_bins; /* FP32 near-tie bins recomputed in FP64           */
+  int32_t escalated;      /* FP32 near-tie escalations to FP64 (bins)        */
   int32_t status;         /* per-signal status (batched calls)               */
+  int64_t kernel_launches;/* CUDA kernels launched by the call               */
 } mpsft_stats;
 
 /* One full recovery (the Demo1::Run loop) of sig. Draws 3 + trials values

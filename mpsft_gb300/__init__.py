@@ -61,7 +61,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("found", ctypes.c_int32),
                 ("gathers", ctypes.c_int64), ("bin_bytes", ctypes.c_int64),
                 ("bin_launches", ctypes.c_int32), ("bin_ms", ctypes.c_double),
-                ("escalated_bins", ctypes.c_int32), ("status", ctypes.c_int32)]
+                ("escalated", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -100,6 +101,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_signal_upload": (I, [P, P, I64, I, PP]),
         "mpsft_signal_wrap_device": (I, [P, P, I64, I, PP]),
         "mpsft_signal_free": (I, [P]),
+        "mpsft_signal_write": (I, [P, P, P]),
         "mpsft_bin_in_time": (I, [P, P, I32, I32, D, I32, I32, I32, I32, I, P, I]),
         "mpsft_bin_in_freq": (I, [P, I32, I32, I32, D, I32, I32, I32, I32, P, P,
                                   I64, P]),
@@ -338,6 +340,14 @@ class Signal:
     n: int
     dtype: int
     _freed: bool = field(default=False)
+
+    def write(self, x: np.ndarray) -> None:
+        """Refills the device copy from host memory (same n and dtype)."""
+        want = np.complex64 if self.dtype == C64 else np.complex128
+        if x.dtype != want or x.size != self.n or not x.flags.c_contiguous:
+            raise ValueError("x must match the signal's n and dtype")
+        _check(self.ctx, self.ctx._lib.mpsft_signal_write(self.ctx._h, self._h,
+                                                          _ptr(x)))
 
     def free(self) -> None:
         if not self._freed and self._h:

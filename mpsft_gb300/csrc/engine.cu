@@ -365,6 +365,8 @@ int64_t BinBytes(const SigIter &it, bool fp64) {
 
 // Launch sequence of one iteration for nsig signals whose SigIter array is
 // already on the device.
+constexpr int kKernelsPerIteration = 7;
+
 int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
                     const std::vector<SigIter> &h_its, bool x_c128, bool fp64,
                     BinTimer *timer) {
@@ -531,6 +533,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   std::vector<Run> run(nsig);
   BinTimer timer{ctx};
   int active = nsig;
+  int64_t launches = 0;
   while (active > 0) {
     for (int i = 0; i < nsig; ++i) {
       SigIter &it = its[i];
@@ -563,6 +566,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
     rc = LaunchIteration(ctx, d_its, nsig, its, x_c128, fp64, &timer);
     if (rc) return rc;
+    launches += kKernelsPerIteration;
     for (int i = 0; i < nsig; ++i) {
       MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_ctl + kCtlWords * i, ctls[i],
                                       sizeof(int32_t) * kCtlWords,
@@ -621,6 +625,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       s.bin_launches = int32_t(timer.used.size());
       s.bin_ms = bin_ms;
       s.status = st;
+      s.kernel_launches = launches;
     }
     if (st && !first_err) {
       first_err = st;
@@ -802,6 +807,17 @@ int mpsft_signal_free(mpsft_signal *sig) {
     cudaFree(sig->d_x);
   }
   delete sig;
+  return MPSFT_OK;
+}
+
+int mpsft_signal_write(mpsft_ctx *ctx, mpsft_signal *sig, const void *x_host) {
+  if (!ctx || !sig || !x_host) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  if (sig->ctx != ctx) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "signal belongs to another context");
+  }
+  const size_t bytes = size_t(sig->n) * (sig->dtype == MPSFT_C64 ? 8 : 16);
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(sig->d_x, x_host, bytes, cudaMemcpyHostToDevice,
+                                  ctx->stream));
   return MPSFT_OK;
 }
 
