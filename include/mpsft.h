@@ -106,6 +106,24 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
                       int32_t c, int32_t q, int precision, double *out,
                       int out_on_device);
 
+/* ---- BinInTime::Run without device allocation --------------------------- */
+/* No counterpart in the reference. The same bins as mpsft_bin_in_time, for
+ * callers that cannot call cudaMalloc (a caller-managed memory pool, a plugin
+ * host that forbids allocation after start-up): x_device (n samples of dtype)
+ * and out_device ((1 + 2*bits) x bins complex128, row-major) are the caller's
+ * device memory, and the work runs asynchronously on stream (a cudaStream_t;
+ * NULL = the legacy default stream). Scratch is one fixed array of about
+ * 2.5 MiB compiled into the library and held on every GPU that loads it.
+ * Limits: bins <= 2047, bits <= 20, window folds p/bins <= 80; larger sizes
+ * return MPSFT_ERR_CAPACITY. The first call on a device resolves the array's
+ * address and fills its twiddle table, synchronising stream; make that first
+ * call before any stream capture. Calls share the array, so calls that overlap
+ * on the GPU race; calls on one stream are ordered and safe. */
+int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n, int dtype,
+                              int32_t bins, int32_t bits, double delta,
+                              int32_t a, int32_t b, int32_t c, int32_t q,
+                              int precision, double *out_device, void *stream);
+
 /* ---- BinInFreq::Run ------------------------------------------------------- */
 /* Subtracts from the host bin matrix inout ((1 + 2*bits) x bins complex128)
  * the window responses of the m modes (k0[i], coef[2i] + i coef[2i+1]). */
