@@ -278,8 +278,10 @@ def run_gpu(args) -> None:
     bin_launches = 0
     iters = []
     launches = 0
+    near = 0
     for _ in range(args.steps):
         out, stats = step()
+        near += sum(s["escalated"] for s in stats)
         bin_ms += stats[0]["bin_ms"]
         bin_launches += stats[0]["bin_launches"]
         bin_bytes += sum(s["bin_bytes"] for s in stats)
@@ -351,7 +353,8 @@ def run_gpu(args) -> None:
                        "precision": "f32 gather/fold/FFT, f64 pencil+coefficients",
                        "l2": f"inputs larger than L2: {G} x 32 MiB signals resident",
                        "parallelism": f"replicas x{world}",
-                       "iterations_mean": float(np.mean(iters))},
+                       "iterations_mean": float(np.mean(iters)),
+                       "near_tie_bins_per_solve": near / (G * args.steps)},
             "e2e": {"value": e2e_value, "unit": "solves/s",
                     "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(d2h // max(args.steps, 1))},

@@ -47,7 +47,10 @@ enum { MPSFT_C64 = 1, MPSFT_C128 = 2 };
 /* FP32: binning, fold (compensated) and size-B FFT in FP32; mode subtraction,
  *       pencil, thresholds and coefficients in FP64.
  * FP64: everything in FP64 (the plain per-signal path). */
-enum { MPSFT_PREC_FP32 = 0, MPSFT_PREC_FP64 = 1 };
+/* FP64_DIRECT (mpsft_bin_in_time only): every bin as a direct FP64 sum over
+ * the window support, without the fold and the size-B FFT (the evaluation the
+ * FP32 path uses for its near-tie bins); slow, for checking. */
+enum { MPSFT_PREC_FP32 = 0, MPSFT_PREC_FP64 = 1, MPSFT_PREC_FP64_DIRECT = 2 };
 
 typedef struct mpsft_ctx mpsft_ctx;
 typedef struct mpsft_signal mpsft_signal;
@@ -148,6 +151,9 @@ typedef struct {
   double window_threshold; /* must be > 0, as in the reference              */
   double sv_threshold;     /* 0 = off                                       */
   int32_t precision;       /* MPSFT_PREC_FP32 or MPSFT_PREC_FP64            */
+  double near_tie_margin;  /* FP32: decisions closer to their threshold     */
+                           /* than margin * 2^-24 * (bin rms) are near ties */
+                           /* (0 = default 256)                             */
 } mpsft_iterate_options;
 
 /* One Iterate call: draws (a, b, c) and one q per trial from rng, bins the
@@ -173,6 +179,7 @@ typedef struct {
   int32_t max_iter;        /* cap on Iterate calls; 0 = 64 + 8*k            */
   int32_t precision;       /* MPSFT_PREC_FP32 or MPSFT_PREC_FP64            */
   int32_t mode_capacity;   /* found-mode table size; 0 = automatic          */
+  double near_tie_margin;  /* as in mpsft_iterate_options (0 = default)     */
 } mpsft_solve_options;
 
 /* Fills opt with the reference's Demo1Options defaults (src/demo1.h:25-33)
@@ -189,6 +196,10 @@ typedef struct {
   int32_t escalated;      /* FP32 near-tie escalations to FP64 (bins)        */
   int32_t status;         /* per-signal status (batched calls)               */
   int64_t kernel_launches;/* CUDA kernels launched by the call               */
+  int32_t unresolved;     /* iterations whose FP32 near ties could not be    */
+                          /* redone in FP64 (bins > 4096); 0 otherwise       */
+  int32_t fp64_iterations;/* FP32 path: iterations run on the FP64 kernels   */
+                          /* because rounding was not small against noise    */
 } mpsft_stats;
 
 /* One full recovery (the Demo1::Run loop) of sig. Draws 3 + trials values

@@ -32,7 +32,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmpsft_gb300.so")
 OK, ERR_INVALID, ERR_UNSUPPORTED_N, ERR_CUDA, ERR_CAPACITY, ERR_ITER_CAP, \
     ERR_NONFINITE, ERR_NOMEM = range(8)
 C64, C128 = 1, 2
-FP32, FP64 = 0, 1
+FP32, FP64, FP64_DIRECT = 0, 1, 2
 
 
 class MpsftError(RuntimeError):
@@ -45,7 +45,8 @@ class IterateOptions(ctypes.Structure):
     _fields_ = [("bins", ctypes.c_int32), ("window_delta", ctypes.c_double),
                 ("trials", ctypes.c_int32), ("bin_threshold", ctypes.c_double),
                 ("window_threshold", ctypes.c_double),
-                ("sv_threshold", ctypes.c_double), ("precision", ctypes.c_int32)]
+                ("sv_threshold", ctypes.c_double), ("precision", ctypes.c_int32),
+                ("near_tie_margin", ctypes.c_double)]
 
 
 class SolveOptions(ctypes.Structure):
@@ -54,7 +55,8 @@ class SolveOptions(ctypes.Structure):
                 ("window_delta", ctypes.c_double),
                 ("window_threshold", ctypes.c_double),
                 ("max_stale_iter", ctypes.c_int32), ("max_iter", ctypes.c_int32),
-                ("precision", ctypes.c_int32), ("mode_capacity", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("mode_capacity", ctypes.c_int32),
+                ("near_tie_margin", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -62,7 +64,8 @@ class Stats(ctypes.Structure):
                 ("gathers", ctypes.c_int64), ("bin_bytes", ctypes.c_int64),
                 ("bin_launches", ctypes.c_int32), ("bin_ms", ctypes.c_double),
                 ("escalated", ctypes.c_int32), ("status", ctypes.c_int32),
-                ("kernel_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("unresolved", ctypes.c_int32),
+                ("fp64_iterations", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -127,7 +130,8 @@ def exported_symbols() -> list[str]:
     import re
     hdr = os.path.join(os.path.dirname(_HERE), "include", "mpsft.h")
     txt = open(hdr).read()
-    return sorted(set(re.findall(r"\b(mpsft_[a-z0-9_]+)\s*\(", txt)))
+    decl = r"(?m)^(?:int|int32_t|void|const char\s*\*)\s*\*?\s*(mpsft_[a-z0-9_]+)\s*\("
+    return sorted(set(re.findall(decl, txt)))
 
 
 def _ptr(a: np.ndarray):
@@ -264,7 +268,7 @@ class Context:
         size = np.array([len(mm)], np.int32)
         found = np.zeros(1, np.int32)
         opt = IterateOptions(bins, window_delta, trials, bin_threshold,
-                             window_threshold, sv_threshold, precision)
+                             window_threshold, sv_threshold, precision, 0.0)
         _check(self, self._lib.mpsft_iterate(self._h, sig._h, ctypes.byref(opt),
                                              rng._h, _ptr(k), _ptr(c), _ptr(size),
                                              cap, _ptr(found)))

@@ -25,12 +25,23 @@ constexpr int kMaxFoldsPerLane = 10;  // folds f = p / bins <= 80
 constexpr int kMaxFFT = 16384;     // largest Bluestein transform (FP32)
 constexpr int kMaxFFT64 = 8192;    // largest Bluestein transform (FP64)
 constexpr int32_t kEmptyKey = -1;
+constexpr int kRebinChunks = 16;   // FP64 re-binning: chunks of the support
+constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
 
 // Per-signal status bits written by the device.
 enum : int32_t {
   kStatusCapacity = 1,   // mode table full
   kStatusNonFinite = 2,  // NaN / Inf in a bin that reached the decisions
+  kStatusUnresolved = 4, // near ties left to FP32 (bins too large for FP64 redo)
 };
+
+// FP32 near-tie bound, in units of eps_rel = margin * 2^-24: the bins of a
+// row carry at most kEpsRms * rms + kEpsRowMax * (largest |U| of the row) +
+// kEpsValue * |U| of rounding error (measured on GB300: about 3, 1 and 3.6 at
+// the maximum over 10^6 bins; the margin multiplies these).
+constexpr float kEpsRms = 8.0f;
+constexpr float kEpsRowMax = 1.0f;
+constexpr float kEpsValue = 4.0f;
 
 // Everything a kernel needs about one signal in the current iteration.
 // Filled by the host engine and copied to the device once per iteration.
@@ -39,6 +50,7 @@ struct SigIter {
   int32_t n, bins, bits, rows;
   int32_t p, p2, folds;
   int32_t a, b, c, a_inv;
+  int32_t phase_shift;  // 32 - log2(n) when n is a power of two, else -1
   int32_t trials;
   int32_t active;
   int32_t q[kMaxTrials];
@@ -57,13 +69,22 @@ struct SigIter {
   void *fold;           // FP32: float2, FP64: double2
   double2 *ubuf;
   int32_t bins_cap;     // row stride of fold / ubuf
-  void *chirp;          // bins entries, e^{-pi i k^2 / bins} (float2 / double2)
-  void *chat;           // fft_m entries, FFT of the conjugate chirp sequence
+  // Bluestein tables: chirp = e^{-pi i k^2 / bins} (bins entries) and
+  // chat = FFT of the conjugate chirp sequence (fft_m entries), FP32 and FP64
+  float2 *chirp32, *chat32;
+  double2 *chirp64, *chat64;
   // mode table
   int32_t *tab_key;
   double2 *tab_coef;
+  double *tab_err;      // bound on each coefficient's FP32 rounding error
   int32_t tab_cap;      // power of two
-  int32_t *tab_count;   // distinct keys stored
+  int32_t *tab_count;   // distinct keys stored = length of occ_list
+  int32_t *occ_list;    // occupied slots, in insertion order
+  // per-slot quantities of the current permutation (k_mode_prep)
+  int32_t *mode_bin;    // bin of the slot's mode, -1 for an empty slot
+  int32_t *mode_k1;     // (a k0 + b) mod n
+  double *mode_wf;      // window response of the mode in its bin
+  double2 *mode_base;   // [slot * trials + t]: wf * coef * e^{2 pi i (q_t k1 + c k0)/n}
   // bucketing of table modes by bin
   int32_t *bkt_count;   // bins_cap
   int32_t *bkt_start;   // bins_cap
@@ -72,7 +93,33 @@ struct SigIter {
   int32_t *cand_valid;  // bins_cap
   int32_t *cand_k0;
   double2 *cand_coef;
-  int32_t *flags;       // [0] found this iteration, [1] status bits
+  double *cand_err;
+  // FP32 near-tie detection: bins whose decisions lie within eps_u (the
+  // a-priori bound on an FP32 bin's rounding error) plus the error carried by
+  // the subtracted modes are listed for FP64 treatment.
+  //   eps = eps_scale * sqrt(*x_energy) with x_energy = mean |x|^2, so that
+  //   eps tracks the bins' rms sqrt(mean|x|^2 / (2 bins)).
+  double eps_scale;     // 0 on the FP64 path
+  const double *x_energy;
+  float *eps_dev;       // eps_scale * sqrt(*x_energy), set by k_bucket
+  float *row_max;       // [t * rows + r]: max |U| of the row (k_row_fft)
+  // FP64 re-binning of listed bins: [((e * trials + t) * rows + r) * chunks
+  // + c] partial sums over chunk c of the window support
+  double2 *esc_part;
+  // per-value part of the FP32 error bound: eps_rel * (kEpsRowMax * max |U|
+  // of the rows involved + kEpsValue * |value|)
+  float eps_rel;
+  // FP32 path only: 1 when this signal's FP32 rounding is not small against
+  // its noise thresholds, so this iteration runs on the FP64 kernels
+  int32_t force_fp64;
+  // 1 when the window and FP32 Bluestein tables of the previous iteration
+  // (same number of bins) are still valid
+  int32_t tables_valid;
+  int32_t *esc_list;    // esc_cap bins
+  uint32_t *esc_mask;   // per listed bin: bit s set = rows 2s+1, 2s+2 near
+  int32_t esc_cap;
+  int32_t *flags;       // [0] found, [1] status bits, [2] near-tie bins
+                        // flagged this iteration, [3] mode count
 };
 
 // ---------------------------------------------------------------- helpers
@@ -106,46 +153,77 @@ __device__ inline double2 UnitPhase64(int64_t m, int64_t n) {
   return make_double2(c, s);
 }
 
+// Same in FP32. The residue r = m mod n becomes 32-bit fixed-point turns
+// floor(r 2^32 / n) (a shift when n = 2^k, shift = 32 - k), whose signed value
+// is the angle reduced to [-1/2, 1/2) turns exactly.
+__device__ inline float2 UnitPhase32(int64_t m, int64_t n, int shift) {
+  uint32_t ph;
+  if (shift >= 0) {
+    ph = uint32_t(uint64_t(m) & uint64_t(n - 1)) << shift;
+  } else {
+    const uint64_t r = uint64_t(PosMod(m, n));
+    ph = uint32_t((r << 32) / uint64_t(n));
+  }
+  float s, c;
+  sincospif(2.0f * (float(int32_t(ph)) * 2.3283064365386963e-10f), &s, &c);
+  return make_float2(c, s);
+}
+
 // SampleInFreq (src/window.cc:77-81): window response at offset xi.
 __device__ inline double WindowInFreq(const SigIter &it, double xi) {
   const double c = 0.5 * it.width;
   return 0.5 * (erf((xi + c) * it.erf_d) - erf((xi - c) * it.erf_d));
 }
 
-// 2x2 matrix pencil [[u0, u2], [u1, u0]] (src/freqid.cc:27-48), FP64.
-// sigma0 = sqrt(largest eigenvalue of A^H A), sigma1 = |det A| / sigma0.
-// The vote Im(conj(v00) v10) < 0 of the dominant right singular vector v
-// reduces to Im(m01) > 0 with m01 = conj(u0) u2 + conj(u1) u0 (the
-// off-diagonal of A^H A); the eigenvector is built the same way as in the
-// oracle so that degenerate cases (m01 = 0) agree.
+// 2x2 matrix pencil [[u0, u2], [u1, u0]] (src/freqid.cc:27-48).
+// sigma0 = sqrt(largest eigenvalue of A^H A), sigma1 = |det A| / sigma0 (no
+// cancellation). With m01 = conj(u0) u2 + conj(u1) u0, the off-diagonal of
+// A^H A, the dominant right singular vector is (lmax - m11, conj(m01)) or
+// (m01, lmax - m00), so the reference's vote Im(conj(v00) v10) < 0 is exactly
+// Im(m01) > 0 (and false when m01 = 0, where v is a unit axis). Returns the
+// vote; *im_m01 receives Im(m01) for the near-tie margin.
+template <typename T> struct CplxOf;
+template <> struct CplxOf<float> { using V = float2; };
+template <> struct CplxOf<double> { using V = double2; };
+
+template <typename T, typename V>
+__device__ inline bool PencilT(V u0, V u1, V u2, T *s0_out, T *s1_out,
+                               T *im_m01) {
+  const T m00 = u0.x * u0.x + u0.y * u0.y + u1.x * u1.x + u1.y * u1.y;
+  const T m11 = u2.x * u2.x + u2.y * u2.y + u0.x * u0.x + u0.y * u0.y;
+  // m01 = conj(u0) u2 + conj(u1) u0
+  const T mr = (u0.x * u2.x + u0.y * u2.y) + (u1.x * u0.x + u1.y * u0.y);
+  const T mi = (u0.x * u2.y - u0.y * u2.x) + (u1.x * u0.y - u1.y * u0.x);
+  const T hd = T(0.5) * (m00 - m11);
+  const T r = sqrt(hd * hd + (mr * mr + mi * mi));
+  const T lmax = T(0.5) * (m00 + m11) + r;
+  const T s0 = sqrt(lmax > T(0) ? lmax : T(0));
+  // det = u0 u0 - u2 u1
+  const T dr = (u0.x * u0.x - u0.y * u0.y) - (u2.x * u1.x - u2.y * u1.y);
+  const T di = (T(2) * u0.x * u0.y) - (u2.x * u1.y + u2.y * u1.x);
+  *s0_out = s0;
+  *s1_out = s0 > T(0) ? sqrt(dr * dr + di * di) / s0 : T(0);
+  *im_m01 = mi;
+  return mi > T(0);
+}
+
 __device__ inline bool Pencil(double2 u0, double2 u1, double2 u2,
                               double *s0_out, double *s1_out) {
-  const double m00 = u0.x * u0.x + u0.y * u0.y + u1.x * u1.x + u1.y * u1.y;
-  const double m11 = u2.x * u2.x + u2.y * u2.y + u0.x * u0.x + u0.y * u0.y;
-  const double2 m01 = cadd(cmul(cconj(u0), u2), cmul(cconj(u1), u0));
-  const double hd = 0.5 * (m00 - m11);
-  const double nm01 = m01.x * m01.x + m01.y * m01.y;
-  const double r = sqrt(hd * hd + nm01);
-  const double lmax = 0.5 * (m00 + m11) + r;
-  const double s0 = sqrt(lmax > 0 ? lmax : 0.0);
-  const double2 det = csub(cmul(u0, u0), cmul(u2, u1));
-  const double adet = hypot(det.x, det.y);
-  *s0_out = s0;
-  *s1_out = s0 > 0 ? adet / s0 : 0.0;
-  double2 v0, v1;
-  if (nm01 == 0.0) {
-    v0 = make_double2(m00 >= m11 ? 1.0 : 0.0, 0.0);
-    v1 = make_double2(m00 >= m11 ? 0.0 : 1.0, 0.0);
-  } else if (m00 >= m11) {
-    v0 = make_double2(lmax - m11, 0.0);
-    v1 = cconj(m01);
-  } else {
-    v0 = m01;
-    v1 = make_double2(lmax - m00, 0.0);
-  }
-  // Im(conj(v0) v1); normalisation does not change its sign.
-  return (v0.x * v1.y - v0.y * v1.x) < 0;
+  double im;
+  return PencilT<double, double2>(u0, u1, u2, s0_out, s1_out, &im);
 }
+
+// True when signal `it` takes the FP64 kernels of the FP32 path this
+// iteration: by the precision policy, or because its near-tie list overflowed.
+__device__ inline bool RedoFP64(const SigIter &it) {
+  return it.force_fp64 || *(volatile int32_t *)&it.flags[2] > it.esc_cap;
+}
+
+// Shared-memory keys of k_bucket: half the table (a power of two). The host
+// keeps tables at or below kMaxTableCap so that this fits in shared memory
+// and slots fit the 20 bits of the sort key.
+constexpr int32_t kMaxTableCap = 1 << 15;
+__host__ __device__ inline int BucketKeys(int tab_cap) { return tab_cap / 2; }
 
 // Hash slot of a mode key (Fibonacci hashing into a power-of-two table).
 __device__ inline uint32_t KeySlot(int32_t k, int32_t cap) {

@@ -27,6 +27,10 @@ struct mpsft_ctx {
   int device = 0;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
+  // second stream for the kernels of an iteration that do not depend on the
+  // gather/fold (tables, mode preparation and bucketing)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   bool profiling = false;
   float2 *tw32 = nullptr;
@@ -56,7 +60,13 @@ struct mpsft_rng {
 
 namespace {
 
-constexpr int kCtlWords = 4;  // found flag, status bits, mode count, spare
+constexpr int kCtlWords = 4;  // found flag, status bits, near ties, mode count
+// FP32 near-tie margin: the safety factor on the FP32 error model of the bins
+// (kEpsRms, kEpsRowMax, kEpsValue in units of 2^-24; the rms of the bins is
+// estimated as sqrt(mean|x|^2 / (2 bins))).
+constexpr double kDefaultNearTieMargin = 2.0;
+
+
 
 int Fail(mpsft_ctx *ctx, int code, const std::string &msg) {
   if (ctx) ctx->err = msg;
@@ -196,6 +206,48 @@ int CheckN(mpsft_ctx *ctx, int64_t n) {
   return MPSFT_OK;
 }
 
+// Precision policy of the FP32 path: a signal stays on the FP32 kernels
+// while the FP32 rounding of its bins (eps, about 16 * 2^-24 * rms) is below
+// 1% of its noise thresholds; otherwise (very high SNR) rounding would decide
+// near the thresholds, and the iteration runs on the FP64 kernels. The ratio
+// eps / threshold does not depend on the number of bins: it is an SNR test
+// (about 90 dB with the reference's thresholds 3 sigma/sqrt(B), sigma/sqrt(B)).
+constexpr double kPrecisionRatio = 0.01;
+
+// FP32 error-model scalars of an iteration with `bins` bins; `energy` is the
+// signal's mean |x|^2.
+void SetNearTie(SigIter *it, bool fp64, double margin, int32_t bins,
+                double energy) {
+  it->force_fp64 = 0;
+  if (fp64) {
+    it->eps_scale = 0;
+    it->eps_rel = 0;
+    return;
+  }
+  const double m = margin > 0 ? margin : kDefaultNearTieMargin;
+  it->eps_rel = float(m * std::ldexp(1.0, -24));
+  it->eps_scale = m * kEpsRms * std::ldexp(1.0, -24) / std::sqrt(2.0 * bins);
+  double scale = 0;
+  if (it->bin_thr > 0) scale = it->bin_thr;
+  if (it->sv_thr > 0) scale = scale > 0 ? std::min(scale, it->sv_thr) : it->sv_thr;
+  const double eps = it->eps_scale * std::sqrt(energy);
+  if (scale > 0 && eps > kPrecisionRatio * scale && (1 << FFTLog2(bins)) <= kMaxFFT64) {
+    it->force_fp64 = 1;
+  }
+}
+
+// mean |x|^2 of the signals (device values, one synchronisation)
+int ReadEnergy(mpsft_ctx *ctx, const double *d_energy, int nsig,
+               std::vector<double> *out) {
+  out->assign(nsig, 0.0);
+  MPSFT_CUDA(ctx, cudaMemcpy2DAsync(out->data(), sizeof(double), d_energy,
+                                    sizeof(double) * kEnergyStride,
+                                    sizeof(double), nsig,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return MPSFT_OK;
+}
+
 // ---------------------------------------------------------------- buffers
 struct Carve {
   unsigned char *base;
@@ -219,22 +271,39 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->wt32 = cv.take<float>(size_t(s.p2_cap) + 1);
   it->wt64 = cv.take<double>(size_t(s.p2_cap) + 1);
   const size_t cells = size_t(s.trials) * s.rows_cap * s.bins_cap;
-  it->fold = cv.take<unsigned char>(cells * (s.fp64 ? 16 : 8));
+  // 16-byte cells: the FP32 path may redo an iteration in FP64
+  it->fold = cv.take<double2>(cells);
   it->ubuf = cv.take<double2>(cells);
-  it->chirp = cv.take<unsigned char>(size_t(s.bins_cap) * (s.fp64 ? 16 : 8));
-  it->chat = cv.take<unsigned char>(size_t(s.m_cap) * (s.fp64 ? 16 : 8));
+  it->row_max = cv.take<float>(size_t(s.trials) * s.rows_cap);
+  it->chirp32 = cv.take<float2>(s.bins_cap);
+  it->chat32 = cv.take<float2>(s.m_cap);
+  it->chirp64 = cv.take<double2>(s.bins_cap);
+  it->chat64 = cv.take<double2>(s.m_cap);
+  it->esc_part =
+      cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap * kRebinChunks);
   it->tab_key = cv.take<int32_t>(s.tab_cap);
   it->tab_coef = cv.take<double2>(s.tab_cap);
+  it->tab_err = cv.take<double>(s.tab_cap);
   it->tab_cap = s.tab_cap;
+  it->occ_list = cv.take<int32_t>(s.tab_cap);
+  it->eps_dev = cv.take<float>(1);
+  it->mode_bin = cv.take<int32_t>(s.tab_cap);
+  it->mode_k1 = cv.take<int32_t>(s.tab_cap);
+  it->mode_wf = cv.take<double>(s.tab_cap);
+  it->mode_base = cv.take<double2>(size_t(s.tab_cap) * s.trials);
   it->bkt_count = cv.take<int32_t>(s.bins_cap);
   it->bkt_start = cv.take<int32_t>(s.bins_cap);
   it->bkt_list = cv.take<int32_t>(s.tab_cap);
   it->cand_valid = cv.take<int32_t>(s.bins_cap);
   it->cand_k0 = cv.take<int32_t>(s.bins_cap);
   it->cand_coef = cv.take<double2>(s.bins_cap);
+  it->cand_err = cv.take<double>(s.bins_cap);
+  it->esc_list = cv.take<int32_t>(kMaxListed);
+  it->esc_mask = cv.take<uint32_t>(kMaxListed);
+  it->esc_cap = kMaxListed;
   *ctl = cv.take<int32_t>(kCtlWords);
   it->flags = *ctl;
-  it->tab_count = *ctl + 2;
+  it->tab_count = *ctl + 3;
   it->bins_cap = s.bins_cap;
 }
 
@@ -287,6 +356,12 @@ void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
   it->b = tf.b;
   it->c = tf.c;
   it->a_inv = tf.a_inv;
+  it->phase_shift = -1;
+  if (IsPow2(sig->n)) {
+    int k = 0;
+    while ((int64_t(1) << k) < sig->n) ++k;
+    it->phase_shift = 32 - k;
+  }
   it->trials = trials;
   it->active = 1;
   for (int t = 0; t < trials; ++t) {
@@ -365,11 +440,10 @@ int64_t BinBytes(const SigIter &it, bool fp64) {
 
 // Launch sequence of one iteration for nsig signals whose SigIter array is
 // already on the device.
-constexpr int kKernelsPerIteration = 7;
 
 int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
                     const std::vector<SigIter> &h_its, bool x_c128, bool fp64,
-                    BinTimer *timer) {
+                    BinTimer *timer, int64_t *launched = nullptr) {
   int max_bins = 0, max_bits = 0, max_trials = 0, max_p2 = 0, max_m = 0,
       max_rows = 0;
   for (const SigIter &it : h_its) {
@@ -383,9 +457,19 @@ int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   }
   if (max_bins == 0) return MPSFT_OK;
   cudaStream_t s = ctx->stream;
+  int max_cap = 0;
+  for (const SigIter &it : h_its) {
+    if (it.active) max_cap = std::max(max_cap, it.tab_cap);
+  }
+  // fork: tables, mode preparation and bucketing on the side stream while
+  // the window and the gather/fold run on the main one
+  MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
+  MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+  LaunchBluesteinSetup(d_its, nsig, max_m, fp64, ctx->tw32, ctx->tw64, ctx->side);
+  LaunchModePrep(d_its, nsig, max_cap, ctx->side);
+  LaunchBucket(d_its, nsig, max_bins, max_cap, ctx->side);
+  MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
   LaunchWindow(d_its, nsig, max_p2, s);
-  LaunchBluesteinSetup(d_its, nsig, max_m, fp64, ctx->tw32, ctx->tw64, s);
-  LaunchBucket(d_its, nsig, max_bins, 0, s);
   if (timer) {
     int rc = timer->Begin();
     if (rc) return rc;
@@ -395,10 +479,33 @@ int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     int rc = timer->End();
     if (rc) return rc;
   }
+  MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));  // join
   LaunchRowFFT(d_its, nsig, max_rows, max_trials, max_m, fp64, ctx->tw32,
                ctx->tw64, s);
-  LaunchDecide(d_its, nsig, max_bins, max_trials, false, s);
+  LaunchDecide(d_its, nsig, max_bins, max_trials, !fp64, false, s);
+  if (!fp64) {
+    // near ties of the FP32 pass: listed bins re-binned and re-decided in
+    // FP64; signals with more near ties than the list holds redo the whole
+    // iteration in FP64 (each kernel exits at once for the other signals)
+    bool any_forced = false;
+    for (const SigIter &it : h_its) any_forced |= it.active && it.force_fp64;
+    const bool redo = any_forced && max_m <= kMaxFFT64;
+    LaunchRebin64(d_its, nsig, x_c128, s);
+    LaunchDecideListed(d_its, nsig, max_trials, redo, s);
+    if (launched) *launched += 3;
+    if (redo) {
+      if (launched) *launched += 4;
+      LaunchBluesteinSetup(d_its, nsig, max_m, true, ctx->tw32, ctx->tw64, s,
+                           true);
+      LaunchBinFold(d_its, nsig, max_bins, max_bits, max_trials, x_c128, true, s,
+                    true);
+      LaunchRowFFT(d_its, nsig, max_rows, max_trials, max_m, true, ctx->tw32,
+                   ctx->tw64, s, true);
+      LaunchDecide(d_its, nsig, max_bins, max_trials, false, false, s, true);
+    }
+  }
   LaunchMerge(d_its, nsig, max_bins, s);
+  if (launched) *launched += 8;
   MPSFT_CUDA(ctx, cudaGetLastError());
   return MPSFT_OK;
 }
@@ -432,6 +539,8 @@ int ClearTable(mpsft_ctx *ctx, const SigIter &it, int32_t *ctl) {
   MPSFT_CUDA(ctx, cudaMemsetAsync(it.tab_key, 0xFF,
                                   sizeof(int32_t) * it.tab_cap, ctx->stream));
   MPSFT_CUDA(ctx, cudaMemsetAsync(it.tab_coef, 0, sizeof(double2) * it.tab_cap,
+                                  ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemsetAsync(it.tab_err, 0, sizeof(double) * it.tab_cap,
                                   ctx->stream));
   MPSFT_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(int32_t) * kCtlWords,
                                   ctx->stream));
@@ -500,7 +609,10 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     s.m_cap = 1 << FFTLog2(s.bins_cap);
     s.tab_cap = o.mode_capacity > 0
                     ? NextPow2(o.mode_capacity)
-                    : NextPow2(std::max<int64_t>(64, 4 * (int64_t(o.k) + s.bins_cap)));
+                    : NextPow2(std::max<int64_t>(64, 2 * (int64_t(o.k) + s.bins_cap)));
+    if (s.tab_cap > kMaxTableCap) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "mode table larger than 32768 slots");
+    }
     s.fp64 = fp64;
     Carve probe{nullptr};
     SigIter dummy{};
@@ -509,6 +621,8 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     bytes += probe.off + 256;
   }
   bytes += sizeof(SigIter) * nsig + 256;
+  bytes += (sizeof(double) * kEnergyStride + sizeof(void *) + sizeof(int64_t)) *
+               nsig + 1024;
   int rc = EnsureArena(ctx, bytes);
   if (rc) return rc;
   rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
@@ -516,12 +630,33 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
 
   Carve cv{ctx->arena};
   SigIter *d_its = cv.take<SigIter>(nsig);
+  double *d_energy = cv.take<double>(size_t(kEnergyStride) * nsig);
+  const void **d_xs = cv.take<const void *>(nsig);
+  int64_t *d_ns = cv.take<int64_t>(nsig);
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
   for (int i = 0; i < nsig; ++i) {
     std::memset(&its[i], 0, sizeof(SigIter));
     CarveSignal(cv, shapes[i], &its[i], &ctls[i]);
+    its[i].x_energy = d_energy + size_t(kEnergyStride) * i;
     rc = ClearTable(ctx, its[i], ctls[i]);
+    if (rc) return rc;
+  }
+  std::vector<double> energy(nsig, 0.0);
+  if (!fp64) {
+    // mean |x|^2 of every signal scales the FP32 near-tie margin
+    std::vector<const void *> h_xs(nsig);
+    std::vector<int64_t> h_ns(nsig);
+    for (int i = 0; i < nsig; ++i) {
+      h_xs[i] = sigs[i]->d_x;
+      h_ns[i] = sigs[i]->n;
+    }
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_xs, h_xs.data(), sizeof(void *) * nsig,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_ns, h_ns.data(), sizeof(int64_t) * nsig,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    LaunchEnergy(d_xs, d_ns, nsig, x_c128, d_energy, ctx->stream);
+    rc = ReadEnergy(ctx, d_energy, nsig, &energy);
     if (rc) return rc;
   }
   // All control words are contiguous only per signal; copy them one by one.
@@ -529,6 +664,8 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     int32_t iter = 0, stale = 0, found = 0, status = MPSFT_OK;
     bool done = false;
     int64_t gathers = 0, bin_bytes = 0;
+    int32_t near_ties = 0, unresolved = 0, fp64_iters = 0;
+    int32_t last_bins = -1;  // bins of the previous iteration (tables reuse)
   };
   std::vector<Run> run(nsig);
   BinTimer timer{ctx};
@@ -553,6 +690,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       it.bin_thr = 3.0 * o.sigma / std::sqrt(double(bins));
       it.sv_thr = 1.0 * o.sigma / std::sqrt(double(bins));
       it.win_thr = o.window_threshold;
+      SetNearTie(&it, fp64, o.near_tie_margin, bins, energy[i]);
+      run[i].fp64_iters += it.force_fp64;
+      // same bins as the last iteration: window and Bluestein tables stand
+      // (a forced FP64 iteration leaves the FP32 tables unbuilt)
+      it.tables_valid = (run[i].last_bins == bins && !it.force_fp64) ? 1 : 0;
+      run[i].last_bins = it.force_fp64 ? -1 : bins;
       run[i].gathers += int64_t(it.trials) * it.p * it.rows;
       run[i].bin_bytes += BinBytes(it, fp64);
     }
@@ -560,13 +703,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                     cudaMemcpyHostToDevice, ctx->stream));
     for (int i = 0; i < nsig; ++i) {
       if (!run[i].done) {
-        MPSFT_CUDA(ctx, cudaMemsetAsync(ctls[i], 0, sizeof(int32_t) * 2,
+        MPSFT_CUDA(ctx, cudaMemsetAsync(ctls[i], 0, sizeof(int32_t) * 3,
                                         ctx->stream));
       }
     }
-    rc = LaunchIteration(ctx, d_its, nsig, its, x_c128, fp64, &timer);
+    rc = LaunchIteration(ctx, d_its, nsig, its, x_c128, fp64, &timer, &launches);
     if (rc) return rc;
-    launches += kKernelsPerIteration;
     for (int i = 0; i < nsig; ++i) {
       MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_ctl + kCtlWords * i, ctls[i],
                                       sizeof(int32_t) * kCtlWords,
@@ -579,7 +721,9 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       const int32_t *c = ctx->h_ctl + kCtlWords * i;
       Run &r = run[i];
       r.iter += 1;
-      r.found = c[2];
+      r.found = c[3];
+      r.near_ties += c[2];
+      if (c[1] & kStatusUnresolved) r.unresolved += 1;
       if (c[1] & kStatusCapacity) {
         r.status = MPSFT_ERR_CAPACITY;
       } else if (c[1] & kStatusNonFinite) {
@@ -626,6 +770,9 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       s.bin_ms = bin_ms;
       s.status = st;
       s.kernel_launches = launches;
+      s.escalated = run[i].near_ties;
+      s.unresolved = run[i].unresolved;
+      s.fp64_iterations = run[i].fp64_iters;
     }
     if (st && !first_err) {
       first_err = st;
@@ -664,6 +811,9 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   ctx->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
   if (e != cudaSuccess) {
@@ -691,6 +841,12 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
   if (ctx->tw32) cudaFree(ctx->tw32);
   if (ctx->tw64) cudaFree(ctx->tw64);
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return MPSFT_OK;
@@ -874,7 +1030,10 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   if (!ctx || !out) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
   int rc = CheckSignal(ctx, sig);
   if (rc) return rc;
-  const bool fp64 = precision == MPSFT_PREC_FP64;
+  const bool fp64 = precision != MPSFT_PREC_FP32;
+  if (precision < MPSFT_PREC_FP32 || precision > MPSFT_PREC_FP64_DIRECT) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "unknown precision");
+  }
   rc = CheckWindow(ctx, bins, delta, fp64);
   if (rc) return rc;
   if (bits < 0 || bits > kMaxBits) {
@@ -884,6 +1043,7 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
     return Fail(ctx, MPSFT_ERR_INVALID, "bins * 2^(bits-1) overflows int32");
   }
   const int32_t n = int32_t(sig->n);
+  const bool direct = precision == MPSFT_PREC_FP64_DIRECT;
   Shape s;
   s.n = n;
   s.bins_cap = bins;
@@ -897,7 +1057,10 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   SigIter it{};
   int32_t *ctl;
   CarveSignal(probe, s, &it, &ctl);
-  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 512);
+  const size_t direct_cells = direct ? size_t(bins) * s.rows_cap * kRebinChunks : 0;
+  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 1024 +
+                            direct_cells * sizeof(double2) +
+                            (direct ? sizeof(int32_t) * bins : 0));
   if (rc) return rc;
   Carve cv{ctx->arena};
   SigIter *d_it = cv.take<SigIter>(1);
@@ -905,9 +1068,50 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   CarveSignal(cv, s, &it, &ctl);
   const Transform tf{a, b, c, InverseMod(a, n)};
   FillIter(&it, sig, bins, bits, delta, tf, &q, 1);
+  cudaStream_t st = ctx->stream;
+  if (direct) {
+    // every bin is a listed bin of the FP64 re-binning kernel
+    it.esc_part = cv.take<double2>(direct_cells);
+    it.esc_list = cv.take<int32_t>(bins);
+    it.esc_mask = nullptr;  // every row of every bin
+    it.esc_cap = bins;
+    std::vector<int32_t> iota(bins);
+    for (int32_t i = 0; i < bins; ++i) iota[i] = i;
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(it.esc_list, iota.data(),
+                                    sizeof(int32_t) * bins,
+                                    cudaMemcpyHostToDevice, st));
+    const int32_t h_flags[kCtlWords] = {0, 0, bins, 0};
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(ctl, h_flags, sizeof(h_flags),
+                                    cudaMemcpyHostToDevice, st));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
+                                    st));
+    LaunchWindow(d_it, 1, it.p2, st);
+    LaunchRebin64(d_it, 1, sig->dtype == MPSFT_C128, st);
+    MPSFT_CUDA(ctx, cudaGetLastError());
+    std::vector<double2> part(direct_cells);
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(part.data(), it.esc_part,
+                                    sizeof(double2) * direct_cells,
+                                    cudaMemcpyDeviceToHost, st));
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+    std::vector<double2> res(size_t(it.rows) * bins);
+    for (int32_t bb = 0; bb < bins; ++bb) {
+      for (int32_t r = 0; r < it.rows; ++r) {
+        const double2 *p = &part[(size_t(bb) * it.rows + r) * kRebinChunks];
+        double2 acc = p[0];
+        for (int cc = 1; cc < kRebinChunks; ++cc) {
+          acc.x += p[cc].x;
+          acc.y += p[cc].y;
+        }
+        res[size_t(r) * bins + bb] = acc;
+      }
+    }
+    MPSFT_CUDA(ctx, cudaMemcpy(out, res.data(), sizeof(double2) * res.size(),
+                               out_on_device ? cudaMemcpyHostToDevice
+                                             : cudaMemcpyHostToHost));
+    return MPSFT_OK;
+  }
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   ctx->stream));
-  cudaStream_t st = ctx->stream;
   LaunchWindow(d_it, 1, it.p2, st);
   LaunchBluesteinSetup(d_it, 1, it.fft_m, fp64, ctx->tw32, ctx->tw64, st);
   BinTimer timer{ctx};
@@ -950,7 +1154,10 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   s.trials = 1;
   s.p2_cap = 1;
   s.m_cap = 1;
-  s.tab_cap = NextPow2(std::max<int64_t>(64, 4 * m));
+  s.tab_cap = NextPow2(std::max<int64_t>(64, 2 * m));
+  if (s.tab_cap > kMaxTableCap) {
+    return Fail(ctx, MPSFT_ERR_CAPACITY, "too many modes");
+  }
   Carve probe{nullptr};
   SigIter it{};
   int32_t *ctl;
@@ -985,8 +1192,9 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(it.ubuf, sizeof(double2) * it.bins_cap,
                                     inout, row_bytes, row_bytes, it.rows,
                                     cudaMemcpyHostToDevice, st));
+  LaunchModePrep(d_it, 1, s.tab_cap, st);
   LaunchBucket(d_it, 1, bins, s.tab_cap, st);
-  LaunchDecide(d_it, 1, bins, 1, true, st);
+  LaunchDecide(d_it, 1, bins, 1, false, true, st);
   MPSFT_CUDA(ctx, cudaGetLastError());
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(inout, row_bytes, it.ubuf,
                                     sizeof(double2) * it.bins_cap, row_bytes,
@@ -1059,14 +1267,18 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
   s.trials = opt->trials;
   s.p2_cap = MakeWindow(bins, opt->window_delta).p2;
   s.m_cap = 1 << FFTLog2(bins);
-  s.tab_cap = NextPow2(std::max<int64_t>(64, 4 * (int64_t(*mm_size) + bins)));
+  s.tab_cap = NextPow2(std::max<int64_t>(64, 2 * (int64_t(*mm_size) + bins)));
+  if (s.tab_cap > kMaxTableCap) {
+    return Fail(ctx, MPSFT_ERR_CAPACITY, "mode map larger than the table");
+  }
   s.fp64 = fp64;
   Carve probe{nullptr};
   SigIter it{};
   int32_t *ctl;
   CarveSignal(probe, s, &it, &ctl);
   const int64_t m0 = *mm_size;
-  const size_t extra = size_t(m0) * (sizeof(int32_t) + sizeof(double2)) + 1024;
+  const size_t extra = size_t(m0) * (sizeof(int32_t) + sizeof(double2)) +
+                       sizeof(double) * kEnergyStride + 2048;
   rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + extra);
   if (rc) return rc;
   Carve cv{ctx->arena};
@@ -1075,6 +1287,9 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
   CarveSignal(cv, s, &it, &ctl);
   int32_t *d_k0 = cv.take<int32_t>(size_t(m0));
   double2 *d_coef = cv.take<double2>(size_t(m0));
+  double *d_energy = cv.take<double>(kEnergyStride);
+  const void **d_xs = cv.take<const void *>(1);
+  int64_t *d_ns = cv.take<int64_t>(1);
   const Transform tf = DrawTransform(rng, n);
   int32_t q[kMaxTrials];
   for (int t = 0; t < opt->trials; ++t) q[t] = rng->Draw() % n;
@@ -1082,7 +1297,21 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
   it.bin_thr = opt->bin_threshold;
   it.sv_thr = opt->sv_threshold;
   it.win_thr = opt->window_threshold;
+  it.x_energy = d_energy;
   cudaStream_t st = ctx->stream;
+  std::vector<double> energy(1, 0.0);
+  if (!fp64) {
+    const void *h_x = sig->d_x;
+    const int64_t h_n = sig->n;
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_xs, &h_x, sizeof(h_x),
+                                    cudaMemcpyHostToDevice, st));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_ns, &h_n, sizeof(h_n),
+                                    cudaMemcpyHostToDevice, st));
+    LaunchEnergy(d_xs, d_ns, 1, sig->dtype == MPSFT_C128, d_energy, st);
+    rc = ReadEnergy(ctx, d_energy, 1, &energy);
+    if (rc) return rc;
+  }
+  SetNearTie(&it, fp64, opt->near_tie_margin, bins, energy[0]);
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   st));
   rc = ClearTable(ctx, it, ctl);

@@ -94,7 +94,7 @@ template <typename TX>
 __global__ void __launch_bounds__(256)
     k_bin_fold32(const SigIter *__restrict__ its, int gmax) {
   const SigIter &it = its[blockIdx.z];
-  if (!it.active) return;
+  if (!it.active || it.force_fp64) return;
   const int B = it.bins;
   if (int(blockIdx.x) * 32 >= B) return;
   const int g = blockIdx.y % gmax;
@@ -188,11 +188,13 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// cond: only signals whose iteration is redone in FP64 take part.
 template <typename TX>
 __global__ void __launch_bounds__(256)
-    k_bin_fold64(const SigIter *__restrict__ its, int gmax) {
+    k_bin_fold64(const SigIter *__restrict__ its, int gmax, int cond) {
   const SigIter &it = its[blockIdx.z];
   if (!it.active) return;
+  if (cond ? !RedoFP64(it) : it.force_fp64) return;
   const int B = it.bins;
   if (int(blockIdx.x) * 32 >= B) return;
   const int g = blockIdx.y % gmax;
@@ -258,14 +260,15 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
-                   int max_trials, bool x_c128, bool fp64, cudaStream_t s) {
+                   int max_trials, bool x_c128, bool fp64, cudaStream_t s,
+                   bool cond) {
   const int gmax = max_bits + 1;
   dim3 grid((max_bins + 31) / 32, gmax * max_trials, nsig);
   if (fp64) {
     if (x_c128) {
-      k_bin_fold64<double2><<<grid, 256, 0, s>>>(d_its, gmax);
+      k_bin_fold64<double2><<<grid, 256, 0, s>>>(d_its, gmax, cond ? 1 : 0);
     } else {
-      k_bin_fold64<float2><<<grid, 256, 0, s>>>(d_its, gmax);
+      k_bin_fold64<float2><<<grid, 256, 0, s>>>(d_its, gmax, cond ? 1 : 0);
     }
   } else {
     if (x_c128) {

@@ -1,14 +1,25 @@
-// Mode bucketing, frequency-domain subtraction of found modes, per-bin
-// identification and coefficient estimation, and the mode-table merge.
+// Found-mode preparation and bucketing, frequency-domain subtraction of found
+// modes, per-bin identification and coefficient estimation, and the merge of
+// the new modes into the table.
 //
 // Reference: BinInFreqV1::Run (src/binner.cc:565-591), the bin loop of
 // Iterate (src/iterate.cc:113-175), IdentifyFreq (src/iterate.cc:44-76) and
-// MatPencil (src/freqid.cc:27-48). All of it runs in FP64.
+// MatPencil (src/freqid.cc:27-48).
 //
-// One warp per (bin, signal): lane s holds rows 2s+1 and 2s+2 (bit s) of
-// every trial, all lanes hold row 0. A bin's modes are taken in increasing
-// k0, so the subtraction order does not depend on the table layout and the
-// result is bit-reproducible.
+// k_mode_prep (one thread per table slot) evaluates, once per mode and
+// iteration, what BinInFreq needs from a mode: k1 = (a k0 + b) mod n, its bin,
+// the window response wf (two FP64 erf) and, per trial, the row-0 term
+// wf * coef * e^{2 pi i (q k1 + c k0)/n}. k_bucket (one CTA per signal) sorts
+// the slots by bin. k_decide then works with one warp per (bin, signal):
+// every lane holds row 0, lane s holds rows 2s+1 and 2s+2 (bit s). A bin's
+// modes are subtracted in increasing k0, so the result does not depend on the
+// table layout. The energy test runs on row 0 before anything else, so bins
+// without energy cost a few instructions.
+//
+// Precision: the FP64 path decides in FP64. The FP32 path decides in FP32 and
+// checks every decision against eps, an upper bound on the bins' FP32
+// rounding error (plus the error carried by the modes it subtracted); a
+// decision closer than eps to its threshold lists the bin for FP64 treatment.
 #include "common.cuh"
 #include "launch.h"
 
@@ -16,149 +27,359 @@ namespace mpsft {
 
 namespace {
 
-// ---------------------------------------------------------------- bucket
-// Counting sort of the table's slots by the bin of their mode under the
-// current permutation: bin = ((a k0 + b) mod n) * bins / n.
+// ---------------------------------------------------------------- prep
+// One thread per occupied slot (the table's insertion list), so FP64 work
+// runs on full warps.
+__global__ void k_mode_prep(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *it.tab_count) return;
+  const int s = it.occ_list[i];
+  const int32_t key = it.tab_key[s];
+  const int64_t n = it.n;
+  const int B = it.bins;
+  const int64_t k1 = PosMod(int64_t(it.a) * key + it.b, n);
+  const int bin = int(k1 * B / n);
+  const double xi = (double(bin) + 0.5) / double(B) - double(k1) / double(n);
+  const double wf = WindowInFreq(it, xi);
+  const double2 wc = cscale(it.tab_coef[s], wf);
+  for (int t = 0; t < it.trials; ++t) {
+    const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
+    it.mode_base[size_t(s) * it.trials + t] = cmul(wc, UnitPhase64(ph, n));
+  }
+  it.mode_k1[s] = int32_t(k1);
+  it.mode_wf[s] = wf;
+  it.mode_bin[s] = bin;
+}
+
+// Sorts the occupied slots by (bin, k0): one 64-bit key per slot,
+// bin << 51 | k0 << 20 | slot (bins < 2^13, k0 < 2^31, slots < 2^20), bitonic
+// sort in shared memory, then per-bin start and count from the run
+// boundaries. The subtraction later walks each bin's modes in increasing k0,
+// an order that does not depend on the table layout. Thread 0 also evaluates
+// this iteration's FP32 error scale eps.
 __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its) {
-  extern __shared__ int32_t cnt[];  // bins entries
-  __shared__ int32_t warp_tot[32];
+  extern __shared__ unsigned long long keys[];  // pow2 >= occupied slots
   const SigIter &it = its[blockIdx.x];
   if (!it.active) return;
-  const int B = it.bins, cap = it.tab_cap;
-  const int64_t n = it.n;
-  for (int i = threadIdx.x; i < B; i += blockDim.x) cnt[i] = 0;
-  __syncthreads();
-  for (int s = threadIdx.x; s < cap; s += blockDim.x) {
-    const int32_t key = it.tab_key[s];
-    if (key == kEmptyKey) continue;
-    const int64_t k1 = PosMod(int64_t(it.a) * key + it.b, n);
-    atomicAdd(&cnt[int(k1 * B / n)], 1);
+  const int B = it.bins;
+  const int occ = *it.tab_count;
+  if (threadIdx.x == 0 && it.eps_scale > 0) {
+    *it.eps_dev = float(it.eps_scale * sqrt(*it.x_energy));
   }
-  __syncthreads();
-  // Exclusive scan: each thread owns a contiguous chunk of bins.
-  const int chunk = (B + blockDim.x - 1) / blockDim.x;
-  const int lo = threadIdx.x * chunk;
-  const int hi = min(lo + chunk, B);
-  int local = 0;
-  for (int i = lo; i < hi; ++i) local += cnt[i];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int incl = local;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
+  // shared keys were sized for half the table (BucketKeys); more occupied
+  // slots end the solve with a capacity status instead of overflowing
+  if (occ > BucketKeys(it.tab_cap)) {
+    if (threadIdx.x == 0) atomicOr(&it.flags[1], kStatusCapacity);
+    return;
   }
-  if (lane == 31) warp_tot[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    int w = lane < int(blockDim.x >> 5) ? warp_tot[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += v;
+  int m = 1;
+  while (m < occ) m <<= 1;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    unsigned long long k = ~0ull;
+    if (i < occ) {
+      const int s = it.occ_list[i];
+      k = (static_cast<unsigned long long>(it.mode_bin[s]) << 51) |
+          (static_cast<unsigned long long>(uint32_t(it.tab_key[s])) << 20) |
+          static_cast<unsigned long long>(s);
     }
-    warp_tot[lane] = w;  // inclusive over warps
+    keys[i] = k;
   }
+  for (int i = threadIdx.x; i < B; i += blockDim.x) it.bkt_count[i] = 0;
   __syncthreads();
-  int run = incl - local + (warp > 0 ? warp_tot[warp - 1] : 0);
-  for (int i = lo; i < hi; ++i) {
-    const int c = cnt[i];
-    it.bkt_count[i] = c;
-    it.bkt_start[i] = run;
-    run += c;
+  for (int size = 2; size <= m; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = keys[i], b = keys[j];
+          if ((a > b) == up) {
+            keys[i] = b;
+            keys[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < B; i += blockDim.x) cnt[i] = 0;
-  __syncthreads();
-  for (int s = threadIdx.x; s < cap; s += blockDim.x) {
-    const int32_t key = it.tab_key[s];
-    if (key == kEmptyKey) continue;
-    const int64_t k1 = PosMod(int64_t(it.a) * key + it.b, n);
-    const int bin = int(k1 * B / n);
-    const int pos = it.bkt_start[bin] + atomicAdd(&cnt[bin], 1);
-    it.bkt_list[pos] = s;
+  __syncthreads();  // also orders the bkt_count zeroing when occ <= 1
+  for (int i = threadIdx.x; i < occ; i += blockDim.x) {
+    const unsigned long long k = keys[i];
+    const int bin = int(k >> 51);
+    it.bkt_list[i] = int32_t(k & 0xFFFFFu);
+    if (i == 0 || int(keys[i - 1] >> 51) != bin) {
+      // first slot of its bin: the run ends at the next bin change
+      int e = i + 1;
+      while (e < occ && int(keys[e] >> 51) == bin) ++e;
+      it.bkt_start[bin] = i;
+      it.bkt_count[bin] = e - i;
+    }
   }
 }
 
-__device__ inline double2 ShflXor(double2 v, int o) {
-  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o),
-                      __shfl_xor_sync(0xffffffffu, v.y, o));
+// ---------------------------------------------------------------- decide
+template <typename T> struct Ops;
+template <> struct Ops<float> {
+  using V = float2;
+  __device__ static V load(const double2 &d) {
+    return make_float2(float(d.x), float(d.y));
+  }
+  __device__ static V from(double2 d) { return make_float2(float(d.x), float(d.y)); }
+  __device__ static V phase(int64_t m, int64_t n, int shift) {
+    return UnitPhase32(m, n, shift);
+  }
+};
+template <> struct Ops<double> {
+  using V = double2;
+  __device__ static V load(const double2 &d) { return d; }
+  __device__ static V from(double2 d) { return d; }
+  __device__ static V phase(int64_t m, int64_t n, int) {
+    return UnitPhase64(m, n);
+  }
+};
+
+template <typename V> __device__ inline V vsub2(V a, V b) {
+  V r;
+  r.x = a.x - b.x;
+  r.y = a.y - b.y;
+  return r;
+}
+template <typename V> __device__ inline V vmul2(V a, V b) {
+  V r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename V> __device__ inline V vconj2(V a) {
+  V r;
+  r.x = a.x;
+  r.y = -a.y;
+  return r;
+}
+template <typename T, typename V> __device__ inline T vabs2(V a) {
+  return sqrt(a.x * a.x + a.y * a.y);
 }
 
-// Loads the bin's rows, subtracts the bin's modes (BinInFreqV1), and, unless
-// subtract_only, runs the decisions and writes the candidate.
-template <int TMAX>
-__device__ void DecideBin(const SigIter &it, int beta, bool subtract_only) {
+__device__ inline void Flag(const SigIter &it, int beta, uint32_t mask) {
+  const int pos = atomicAdd(&it.flags[2], 1);
+  if (pos < it.esc_cap) {
+    it.esc_list[pos] = beta;
+    if (it.esc_mask) it.esc_mask[pos] = mask;
+  }
+}
+
+// Row r of a listed bin is re-binned in FP64 when it is row 0 or belongs to
+// a bit whose decisions were near.
+__device__ inline bool RowListed(uint32_t mask, int r) {
+  return r == 0 || ((mask >> ((r - 1) >> 1)) & 1u);
+}
+
+__device__ inline void NoCandidate(const SigIter &it, int beta, int lane) {
+  if (lane == 0) it.cand_valid[beta] = 0;
+}
+
+// Bin values of (trial t, row r) at bin beta, from the size-B FFT output.
+struct FromBins {
+  const SigIter &it;
+  int beta;
+  __device__ double2 get(int t, int r) const {
+    return it.ubuf[(size_t(t) * it.rows + r) * it.bins_cap + beta];
+  }
+};
+
+// Bin values of listed bin e: rows re-binned in FP64 (the chunk partial sums
+// in their fixed order), the other rows from the FP32 pass.
+struct FromRebin {
+  const SigIter &it;
+  int e, beta;
+  uint32_t mask;
+  __device__ double2 get(int t, int r) const {
+    if (!RowListed(mask, r)) {
+      return it.ubuf[(size_t(t) * it.rows + r) * it.bins_cap + beta];
+    }
+    const double2 *p =
+        it.esc_part + ((size_t(e) * it.trials + t) * it.rows + r) * kRebinChunks;
+    double2 s = p[0];
+    for (int c = 1; c < kRebinChunks; ++c) s = cadd(s, p[c]);
+    return s;
+  }
+};
+
+enum DecideMode { kDecide = 0, kSubtractOnly = 1, kDecideExact = 2 };
+
+// The bin loop body of Iterate for one bin (warp-wide). T = float: the FP32
+// path with near-tie detection; T = double: FP64 decisions (the FP64 path, and
+// the near-tie bins after their FP64 re-binning).
+template <typename T, int TMAX, typename Src>
+__device__ void DecideBin(const SigIter &it, int beta, const Src &src,
+                          int mode) {
+  using O = Ops<T>;
+  using V = typename O::V;
   const int lane = threadIdx.x & 31;
-  const int L = it.bits, T = it.trials, rows = it.rows;
+  const int L = it.bits, TR = it.trials, rows = it.rows;
   const int64_t n = it.n;
   const int B = it.bins;
   const bool has_bit = lane < L;
-  const size_t cap = size_t(it.bins_cap);
-  double2 u0[TMAX], up[TMAX], um[TMAX];
+  const bool fp32 = sizeof(T) == 4;
+  const int nm = it.bkt_count[beta];
+  const int st = it.bkt_start[beta];
+
+  // ---- row 0 and its mode subtraction (the bin's modes are in increasing k0).
+  // The first 32 modes are loaded once, one per lane, and shared by shuffles
+  // (the common case); further modes are read directly.
+  V u0[TMAX];
 #pragma unroll
   for (int t = 0; t < TMAX; ++t) {
-    if (t < T) {
-      const double2 *base = it.ubuf + size_t(t) * rows * cap;
-      u0[t] = base[beta];
+    if (t < TR) u0[t] = O::from(src.get(t, 0));
+  }
+  const int npre = min(nm, 32);
+  int pre_k1 = 0;
+  double2 pre_base[TMAX];
+  double mode_err = 0;  // FP32 error carried into this bin by the found modes
+  if (lane < npre) {
+    const int sl = it.bkt_list[st + lane];
+    pre_k1 = it.mode_k1[sl];
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) pre_base[t] = it.mode_base[size_t(sl) * TR + t];
+    }
+    if (fp32) mode_err = it.tab_err[sl] * fabs(it.mode_wf[sl]);
+  }
+  for (int i = 0; i < nm; ++i) {
+    double2 bs[TMAX];
+    if (i < 32) {
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) {
+          bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
+          bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
+        }
+      }
+    } else {
+      const int sl = it.bkt_list[st + i];
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) bs[t] = it.mode_base[size_t(sl) * TR + t];
+      }
+      if (fp32 && lane == 0) mode_err += it.tab_err[sl] * fabs(it.mode_wf[sl]);
+    }
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) u0[t] = vsub2(u0[t], O::from(bs[t]));
+    }
+  }
+  if (fp32) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mode_err += __shfl_xor_sync(0xffffffffu, mode_err, o);
+  }
+  // FP32 error bound of this lane's values (see kEpsRms and friends)
+  float eps_base = 0.f, rm0 = 0.f, rml = 0.f;
+  if (fp32) {
+    eps_base = *it.eps_dev + float(mode_err);
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        const float *rm = it.row_max + size_t(t) * rows;
+        rm0 = fmaxf(rm0, rm[0]);
+        if (has_bit) rml = fmaxf(rml, fmaxf(rm[2 * lane + 1], rm[2 * lane + 2]));
+      }
+    }
+    rml = fmaxf(rml, rm0);
+  }
+  bool e_near = false;  // energy decision near its threshold (warp-uniform)
+
+  if (mode != kSubtractOnly) {
+    // ---- energy threshold (src/iterate.cc:114-124) on row 0 only
+    T e = 0;
+    T amax = 0;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        e += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
+        amax = max(amax, vabs2<T, V>(u0[t]));
+      }
+    }
+    e /= T(TR);
+    if (!isfinite(e)) {
+      if (lane == 0) {
+        atomicOr(&it.flags[1], kStatusNonFinite);
+        it.cand_valid[beta] = 0;
+      }
+      return;
+    }
+    if (it.bin_thr > 0) {
+      const T thr2 = T(it.bin_thr * it.bin_thr);
+      if (fp32) {
+        const T eps0 = T(eps_base + it.eps_rel * (kEpsRowMax * rm0 +
+                                                  kEpsValue * float(amax)));
+        // |d e| <= 2 max|u0| eps + eps^2
+        e_near = fabs(e - thr2) <= T(2) * amax * eps0 + eps0 * eps0;
+      }
+      if (e < thr2) {
+        if (e_near && lane == 0) Flag(it, beta, 0u);
+        NoCandidate(it, beta, lane);
+        return;
+      }
+    }
+  }
+
+  // ---- rows 2s+1, 2s+2 of this lane's bit and their mode subtraction
+  V up[TMAX], um[TMAX];
+#pragma unroll
+  for (int t = 0; t < TMAX; ++t) {
+    if (t < TR) {
       if (has_bit) {
-        up[t] = base[(2 * lane + 1) * cap + beta];
-        um[t] = base[(2 * lane + 2) * cap + beta];
+        up[t] = O::from(src.get(t, 2 * lane + 1));
+        um[t] = O::from(src.get(t, 2 * lane + 2));
       } else {
-        up[t] = um[t] = make_double2(0, 0);
+        up[t].x = up[t].y = um[t].x = um[t].y = T(0);
       }
     }
   }
   const int64_t off = has_bit ? (int64_t(B) << lane) : 0;
-
-  // ---- subtraction of the modes found so far, in increasing k0
-  const int nm = it.bkt_count[beta];
-  const int st = it.bkt_start[beta];
-  int32_t last = INT32_MIN;
-  bool have_last = false;
   for (int i = 0; i < nm; ++i) {
-    int32_t best = INT32_MAX;
-    int best_slot = -1;
-    for (int j = 0; j < nm; ++j) {
-      const int sl = it.bkt_list[st + j];
-      const int32_t key = it.tab_key[sl];
-      if ((!have_last || key > last) && (best_slot < 0 || key < best)) {
-        best = key;
-        best_slot = sl;
+    double2 bs[TMAX];
+    int64_t k1m;
+    if (i < 32) {
+      k1m = __shfl_sync(0xffffffffu, pre_k1, i);
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) {
+          bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
+          bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
+        }
+      }
+    } else {
+      const int sl = it.bkt_list[st + i];
+      k1m = it.mode_k1[sl];
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) bs[t] = it.mode_base[size_t(sl) * TR + t];
       }
     }
-    last = best;
-    have_last = true;
-    const int32_t k0 = best;
-    const double2 coef = it.tab_coef[best_slot];
-    const int64_t k1 = PosMod(int64_t(it.a) * k0 + it.b, n);
-    const double xi = (double(beta) + 0.5) / double(B) - double(k1) / double(n);
-    const double wf = WindowInFreq(it, xi);
-    const double2 wc = cscale(coef, wf);
-    double2 fac = make_double2(1, 0);
-    if (has_bit) fac = UnitPhase64(off * k1, n);
+    if (has_bit) {
+      const V fac = O::phase(off * k1m, n, it.phase_shift);
 #pragma unroll
-    for (int t = 0; t < TMAX; ++t) {
-      if (t < T) {
-        const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * k0;
-        const double2 bs = cmul(wc, UnitPhase64(ph, n));
-        u0[t] = csub(u0[t], bs);
-        if (has_bit) {
-          up[t] = csub(up[t], cmul(bs, fac));
-          um[t] = csub(um[t], cmul(bs, cconj(fac)));
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) {
+          const V b = O::from(bs[t]);
+          up[t] = vsub2(up[t], vmul2(b, fac));
+          um[t] = vsub2(um[t], vmul2(b, vconj2(fac)));
         }
       }
     }
   }
-  if (subtract_only) {
+  if (mode == kSubtractOnly) {
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
-      if (t < T) {
-        double2 *base = it.ubuf + size_t(t) * rows * cap;
-        if (lane == 0) base[beta] = u0[t];
+      if (t < TR) {
+        double2 *base = it.ubuf + size_t(t) * rows * it.bins_cap;
+        if (lane == 0) base[beta] = make_double2(u0[t].x, u0[t].y);
         if (has_bit) {
-          base[(2 * lane + 1) * cap + beta] = up[t];
-          base[(2 * lane + 2) * cap + beta] = um[t];
+          base[(2 * lane + 1) * it.bins_cap + beta] = make_double2(up[t].x, up[t].y);
+          base[(2 * lane + 2) * it.bins_cap + beta] = make_double2(um[t].x, um[t].y);
         }
       }
     }
@@ -169,10 +390,9 @@ __device__ void DecideBin(const SigIter &it, int beta, bool subtract_only) {
   bool finite = true;
 #pragma unroll
   for (int t = 0; t < TMAX; ++t) {
-    if (t < T) {
-      finite = finite && isfinite(u0[t].x) && isfinite(u0[t].y) &&
-               isfinite(up[t].x) && isfinite(up[t].y) && isfinite(um[t].x) &&
-               isfinite(um[t].y);
+    if (t < TR) {
+      finite = finite && isfinite(up[t].x) && isfinite(up[t].y) &&
+               isfinite(um[t].x) && isfinite(um[t].y);
     }
   }
   if (__any_sync(0xffffffffu, !finite)) {
@@ -183,36 +403,39 @@ __device__ void DecideBin(const SigIter &it, int beta, bool subtract_only) {
     return;
   }
 
-  // ---- energy threshold (src/iterate.cc:114-124)
-  double e = 0;
-#pragma unroll
-  for (int t = 0; t < TMAX; ++t) {
-    if (t < T) e += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
-  }
-  e /= T;
-  if (it.bin_thr > 0 && e < it.bin_thr * it.bin_thr) {
-    if (lane == 0) it.cand_valid[beta] = 0;
-    return;
-  }
-
   // ---- IdentifyFreq: per-bit majority of the pencil votes, sv rejection
   int count = 0;
-  bool sv_fail = false;
+  bool sv_fail = false, near = false;
   if (has_bit) {
+    const T sv_thr = T(it.sv_thr);
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
-      if (t < T) {
-        double s0, s1;
-        if (Pencil(u0[t], up[t], um[t], &s0, &s1)) ++count;
-        if (it.sv_thr > 0 && s1 * 0.5 > it.sv_thr) sv_fail = true;
+      if (t < TR) {
+        T s0, s1, im;
+        if (PencilT<T, V>(u0[t], up[t], um[t], &s0, &s1, &im)) ++count;
+        if (sv_thr > T(0) && s1 * T(0.5) > sv_thr) sv_fail = true;
+        if (fp32) {
+          const T a0 = vabs2<T, V>(u0[t]), a1 = vabs2<T, V>(up[t]),
+                  a2 = vabs2<T, V>(um[t]);
+          const T eps = T(eps_base + it.eps_rel * (kEpsRowMax * rml +
+                                                   kEpsValue * float(max(a0, max(a1, a2)))));
+          // |d Im(m01)| <= eps (2|u0| + |u1| + |u2|) + 4 eps^2;
+          // |d sigma1| <= ||dA||_2 <= 2 eps.
+          if (fabs(im) <= eps * (T(2) * a0 + a1 + a2) + T(4) * eps * eps) near = true;
+          if (sv_thr > T(0) && fabs(s1 * T(0.5) - sv_thr) <= eps) near = true;
+        }
       }
     }
   }
+  if (fp32) {
+    const uint32_t near_bits = __ballot_sync(0xffffffffu, has_bit && near);
+    if ((near_bits || e_near) && lane == 0) Flag(it, beta, near_bits);
+  }
   if (__any_sync(0xffffffffu, sv_fail)) {
-    if (lane == 0) it.cand_valid[beta] = 0;
+    NoCandidate(it, beta, lane);
     return;
   }
-  const uint32_t mask = __ballot_sync(0xffffffffu, has_bit && count > T / 2);
+  const uint32_t mask = __ballot_sync(0xffffffffu, has_bit && count > TR / 2);
   // bit 0 is the most significant digit of xi
   const uint32_t xs = L > 0 ? (__brev(mask) >> (32 - L)) : 0u;
   const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
@@ -221,62 +444,251 @@ __device__ void DecideBin(const SigIter &it, int beta, bool subtract_only) {
   const double xi0 = double(k1) / double(n) - (double(beta) + 0.5) / double(B);
   const double wf = WindowInFreq(it, xi0);
   if (fabs(wf) < it.win_thr) {
-    if (lane == 0) it.cand_valid[beta] = 0;
+    NoCandidate(it, beta, lane);
     return;
   }
 
   // ---- coefficient (src/iterate.cc:146-171)
-  double2 acc = make_double2(0, 0);
-  double2 fac2 = make_double2(1, 0);
-  if (has_bit) fac2 = UnitPhase64(-off * k1, n);
+  V fac_t[TMAX];
+  {
+    // lane t evaluates e^{-2 pi i (q_t k1 mod n)/n}; the warp shares it
+    V mine;
+    mine.x = T(1);
+    mine.y = T(0);
+    if (lane < TR) mine = O::phase(-int64_t(it.q[lane]) * k1, n, it.phase_shift);
 #pragma unroll
-  for (int t = 0; t < TMAX; ++t) {
-    if (t < T) {
-      const double2 fac = UnitPhase64(-int64_t(it.q[t]) * k1, n);
-      if (lane == 0) acc = cadd(acc, cmul(u0[t], fac));
-      if (has_bit) {
-        acc = cadd(acc, cmul(up[t], cmul(fac, fac2)));
-        acc = cadd(acc, cmul(um[t], cmul(fac, cconj(fac2))));
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        fac_t[t].x = __shfl_sync(0xffffffffu, mine.x, t);
+        fac_t[t].y = __shfl_sync(0xffffffffu, mine.y, t);
       }
     }
   }
+  V acc;
+  acc.x = acc.y = T(0);
+  V fac2;
+  fac2.x = T(1);
+  fac2.y = T(0);
+  if (has_bit) fac2 = O::phase(-off * k1, n, it.phase_shift);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc = cadd(acc, ShflXor(acc, o));
+  for (int t = 0; t < TMAX; ++t) {
+    if (t < TR) {
+      if (lane == 0) {
+        const V p0 = vmul2(u0[t], fac_t[t]);
+        acc.x += p0.x;
+        acc.y += p0.y;
+      }
+      if (has_bit) {
+        const V p1 = vmul2(up[t], vmul2(fac_t[t], fac2));
+        const V p2 = vmul2(um[t], vmul2(fac_t[t], vconj2(fac2)));
+        acc.x += p1.x + p2.x;
+        acc.y += p1.y + p2.y;
+      }
+    }
+  }
+  double ax = acc.x, ay = acc.y;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ax += __shfl_xor_sync(0xffffffffu, ax, o);
+    ay += __shfl_xor_sync(0xffffffffu, ay, o);
+  }
+  // the coefficient's FP32 error: every averaged value carries at most the
+  // bound of the rows involved
+  float eps_c = 0.f;
+  if (fp32) {
+    T amax = 0;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        amax = max(amax, max(vabs2<T, V>(u0[t]),
+                             max(vabs2<T, V>(up[t]), vabs2<T, V>(um[t]))));
+      }
+    }
+    eps_c = eps_base + it.eps_rel * (kEpsRowMax * rml + kEpsValue * float(amax));
+    for (int o = 16; o > 0; o >>= 1) {
+      eps_c = fmaxf(eps_c, __shfl_xor_sync(0xffffffffu, eps_c, o));
+    }
+  }
   if (lane == 0) {
-    double2 coef = cscale(acc, 1.0 / double(T * (1 + 2 * L)));
+    double2 coef = make_double2(ax / double(TR * (1 + 2 * L)),
+                                ay / double(TR * (1 + 2 * L)));
     const int32_t k0 =
         int32_t(PosMod(int64_t(it.a_inv) * (int64_t(k1) - it.b), n));
     coef = cmul(coef, UnitPhase64(-int64_t(it.c) * k0, n));
     coef = make_double2(coef.x / wf, coef.y / wf);
     it.cand_k0[beta] = k0;
     it.cand_coef[beta] = coef;
+    it.cand_err[beta] = fp32 ? double(eps_c) / fabs(wf) : 0.0;
     it.cand_valid[beta] = 1;
     it.flags[0] = 1;
   }
 }
 
-template <int TMAX>
+// One warp per bin. cond: only signals whose iteration is redone in FP64
+// (more near-tie bins than their list holds) take part.
+template <typename T, int TMAX>
 __global__ void __launch_bounds__(256)
-    k_decide(const SigIter *__restrict__ its, int subtract_only) {
+    k_decide(const SigIter *__restrict__ its, int mode, int cond) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
+  if (cond ? !RedoFP64(it) : it.force_fp64) return;
   const int beta = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (beta >= it.bins) return;
-  DecideBin<TMAX>(it, beta, subtract_only != 0);
+  DecideBin<T, TMAX>(it, beta, FromBins{it, beta}, mode);
+}
+
+// One warp per listed near-tie bin: FP64 decision on the FP64 re-binned
+// values. Signals whose list overflowed are redone whole instead.
+template <int TMAX>
+__global__ void __launch_bounds__(256)
+    k_decide_listed(const SigIter *__restrict__ its, int redo) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active) return;
+  if (it.force_fp64) return;
+  const int nf = *(volatile int32_t *)&it.flags[2];
+  if (nf > it.esc_cap) {
+    // the whole iteration is redone in FP64 when the redo kernels run
+    if (!redo && blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicOr(&it.flags[1], kStatusUnresolved);
+    }
+    return;
+  }
+  const int e = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (e >= nf) return;
+  const int beta = it.esc_list[e];
+  DecideBin<double, TMAX>(it, beta, FromRebin{it, e, beta, it.esc_mask[e]},
+                          kDecideExact);
+}
+
+// ---------------------------------------------------------------- rebin
+// Direct FP64 evaluation of listed bins:
+//   U_r[beta] = sum_{t=-p2}^{p2} x[(a (tau_r + t) + c) mod n] wt(t)
+//               e^{2 pi i ((b (tau_r + t) mod n)/n - (2 beta + 1) t/(2B))}
+// (the fold and the size-B DFT in one sum). Work item = (signal, listed bin,
+// trial, row, chunk of the support); each thread sums a contiguous run of t,
+// anchoring the phase exactly from integers at the run's start and stepping
+// it by one complex multiplication per sample.
+template <typename TX>
+__global__ void __launch_bounds__(256)
+    k_rebin64(const SigIter *__restrict__ its, int nsig) {
+  __shared__ double red_re[256], red_im[256];
+  for (int64_t w = blockIdx.x;; w += gridDim.x) {
+    int sig = -1;
+    int64_t base = 0, local = 0;
+    for (int s = 0; s < nsig; ++s) {
+      const SigIter &q = its[s];
+      if (!q.active || q.force_fp64) continue;
+      const int nf = *(volatile int32_t *)&q.flags[2];
+      if (nf > q.esc_cap) continue;
+      const int64_t items = int64_t(nf) * q.trials * q.rows * kRebinChunks;
+      if (w < base + items) {
+        sig = s;
+        local = w - base;
+        break;
+      }
+      base += items;
+    }
+    if (sig < 0) return;  // every block agrees: w is uniform
+    const SigIter &it = its[sig];
+    const int c = int(local % kRebinChunks);
+    local /= kRebinChunks;
+    const int r = int(local % it.rows);
+    local /= it.rows;
+    const int t = int(local % it.trials);
+    const int e = int(local / it.trials);
+    const int beta = it.esc_list[e];
+    if (it.esc_mask != nullptr && !RowListed(it.esc_mask[e], r)) continue;
+    const int64_t n = it.n;
+    const int64_t B = it.bins;
+    int64_t off = 0;
+    if (r > 0) {
+      const int s = (r - 1) / 2;
+      off = (r & 1) ? (B << s) : -(B << s);
+    }
+    const int64_t tau = int64_t(it.q[t]) + off;
+    const int64_t p = it.p;
+    const int64_t chunk = (p + kRebinChunks - 1) / kRebinChunks;
+    const int64_t c0 = -int64_t(it.p2) + c * chunk;
+    const int64_t c1 = min(c0 + chunk, int64_t(it.p2) + 1);
+    const int64_t per = (chunk + blockDim.x - 1) / blockDim.x;
+    const int64_t t0 = c0 + int64_t(threadIdx.x) * per;
+    const int64_t t1 = min(t0 + per, c1);
+    double ar = 0, ai = 0;
+    if (t0 < t1) {
+      const int64_t twoB = 2 * B;
+      const int64_t g = 2 * int64_t(beta) + 1;
+      uint32_t j = uint32_t(PosMod(int64_t(it.a) * PosMod(tau + t0, n) + it.c, n));
+      const uint32_t astep = uint32_t(PosMod(it.a, n));
+      const int64_t m0 = PosMod(int64_t(it.b) * PosMod(tau + t0, n), n);
+      const int64_t r0 = PosMod(g * t0, twoB);
+      double s, co;
+      sincospi(2.0 * (double(m0) / double(n) - double(r0) / double(twoB)), &s, &co);
+      double pr = co, pi = s;
+      const double dth = double(PosMod(it.b, n)) / double(n) -
+                         double(PosMod(g, twoB)) / double(twoB);
+      sincospi(2.0 * dth, &s, &co);
+      const double dr = co, di = s;
+      const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
+      const uint32_t nn = uint32_t(n);
+      // batches of 8 samples: indices and loads first, then the FP64 sums
+      for (int64_t tb = t0; tb < t1; tb += 8) {
+        TX v[8];
+        double w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int64_t tt = tb + k;
+          if (tt < t1) {
+            v[k] = __ldg(&x[j]);
+            w[k] = __ldg(&it.wt64[tt < 0 ? -tt : tt]);
+            j += astep;
+            if (j >= nn) j -= nn;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (tb + k < t1) {
+            const double vx = double(v[k].x) * w[k], vy = double(v[k].y) * w[k];
+            ar += vx * pr - vy * pi;
+            ai += vx * pi + vy * pr;
+            const double npr = pr * dr - pi * di;
+            pi = pr * di + pi * dr;
+            pr = npr;
+          }
+        }
+      }
+    }
+    red_re[threadIdx.x] = ar;
+    red_im[threadIdx.x] = ai;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        red_re[threadIdx.x] += red_re[threadIdx.x + o];
+        red_im[threadIdx.x] += red_im[threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      it.esc_part[((size_t(e) * it.trials + t) * it.rows + r) * kRebinChunks + c] =
+          make_double2(red_re[0], red_im[0]);
+    }
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------- merge
-__device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef) {
+__device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef,
+                           double err) {
   const int cap = it.tab_cap;
   uint32_t slot = KeySlot(k0, cap);
   for (int probe = 0; probe < cap; ++probe) {
     const int32_t prev = atomicCAS(&it.tab_key[slot], kEmptyKey, k0);
     if (prev == kEmptyKey) {
-      atomicAdd(it.tab_count, 1);
+      it.occ_list[atomicAdd(it.tab_count, 1)] = int32_t(slot);
     }
     if (prev == kEmptyKey || prev == k0) {
       atomicAdd(&it.tab_coef[slot].x, coef.x);
       atomicAdd(&it.tab_coef[slot].y, coef.y);
+      if (err != 0.0) atomicAdd(&it.tab_err[slot], err);
       return;
     }
     slot = (slot + 1) & uint32_t(cap - 1);
@@ -289,7 +701,7 @@ __global__ void k_merge(const SigIter *__restrict__ its) {
   if (!it.active) return;
   const int beta = blockIdx.x * blockDim.x + threadIdx.x;
   if (beta >= it.bins || !it.cand_valid[beta]) return;
-  InsertMode(it, it.cand_k0[beta], it.cand_coef[beta]);
+  InsertMode(it, it.cand_k0[beta], it.cand_coef[beta], it.cand_err[beta]);
 }
 
 __global__ void k_table_insert(const SigIter *__restrict__ it,
@@ -297,7 +709,7 @@ __global__ void k_table_insert(const SigIter *__restrict__ it,
                                const double2 *__restrict__ coef, int64_t m) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  InsertMode(*it, k0[i], coef[i]);
+  InsertMode(*it, k0[i], coef[i], 0.0);
 }
 
 __global__ void k_pencil(const double2 *__restrict__ u3, int64_t count,
@@ -310,31 +722,75 @@ __global__ void k_pencil(const double2 *__restrict__ u3, int64_t count,
   sigma[2 * i + 1] = s1;
 }
 
-template <int TMAX>
-void LaunchDecideT(const SigIter *d_its, int nsig, int max_bins, int sub,
-                   cudaStream_t s) {
+template <typename T, int TMAX>
+void LaunchDecideT(const SigIter *d_its, int nsig, int max_bins, int mode,
+                   int cond, cudaStream_t s) {
   dim3 grid((max_bins + 7) / 8, nsig);
-  k_decide<TMAX><<<grid, 256, 0, s>>>(d_its, sub);
+  k_decide<T, TMAX><<<grid, 256, 0, s>>>(d_its, mode, cond);
+}
+
+template <typename T>
+void LaunchDecideP(const SigIter *d_its, int nsig, int max_bins, int max_trials,
+                   int mode, int cond, cudaStream_t s) {
+  if (max_trials <= 1) {
+    LaunchDecideT<T, 1>(d_its, nsig, max_bins, mode, cond, s);
+  } else if (max_trials <= 5) {
+    LaunchDecideT<T, 5>(d_its, nsig, max_bins, mode, cond, s);
+  } else {
+    LaunchDecideT<T, kMaxTrials>(d_its, nsig, max_bins, mode, cond, s);
+  }
 }
 
 }  // namespace
 
-void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
-                  cudaStream_t s) {
-  (void)max_cap;
-  k_bucket<<<nsig, 1024, size_t(max_bins) * sizeof(int32_t), s>>>(d_its);
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap,
+                    cudaStream_t s) {
+  // the occupied count is only known on the device: cover the whole table,
+  // blocks past the count exit at once
+  dim3 grid((max_cap + 255) / 256, nsig);
+  k_mode_prep<<<grid, 256, 0, s>>>(d_its);
 }
 
-// The trial count selects the register footprint of the decide kernel.
+void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
+                  cudaStream_t s) {
+  (void)max_bins;
+  const size_t sm = size_t(BucketKeys(max_cap)) * sizeof(unsigned long long);
+  cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(sm));
+  k_bucket<<<nsig, 1024, sm, s>>>(d_its);
+}
+
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
-                  bool subtract_only, cudaStream_t s) {
-  const int sub = subtract_only ? 1 : 0;
-  if (max_trials <= 1) {
-    LaunchDecideT<1>(d_its, nsig, max_bins, sub, s);
-  } else if (max_trials <= 5) {
-    LaunchDecideT<5>(d_its, nsig, max_bins, sub, s);
+                  bool fp32, bool subtract_only, cudaStream_t s, bool cond) {
+  const int mode = subtract_only ? kSubtractOnly : kDecide;
+  if (fp32) {
+    LaunchDecideP<float>(d_its, nsig, max_bins, max_trials, mode, 0, s);
   } else {
-    LaunchDecideT<kMaxTrials>(d_its, nsig, max_bins, sub, s);
+    LaunchDecideP<double>(d_its, nsig, max_bins, max_trials, mode, cond ? 1 : 0,
+                          s);
+  }
+}
+
+void LaunchRebin64(const SigIter *d_its, int nsig, bool x_c128, cudaStream_t s) {
+  // persistent grid: blocks stride over the (few) work items
+  const int blocks = 152 * 4;
+  if (x_c128) {
+    k_rebin64<double2><<<blocks, 256, 0, s>>>(d_its, nsig);
+  } else {
+    k_rebin64<float2><<<blocks, 256, 0, s>>>(d_its, nsig);
+  }
+}
+
+void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
+                        bool redo, cudaStream_t s) {
+  dim3 grid((kMaxListed + 7) / 8, nsig);
+  const int r = redo ? 1 : 0;
+  if (max_trials <= 1) {
+    k_decide_listed<1><<<grid, 256, 0, s>>>(d_its, r);
+  } else if (max_trials <= 5) {
+    k_decide_listed<5><<<grid, 256, 0, s>>>(d_its, r);
+  } else {
+    k_decide_listed<kMaxTrials><<<grid, 256, 0, s>>>(d_its, r);
   }
 }
 

@@ -43,7 +43,7 @@ __device__ double SincPi(double x) {
 
 __global__ void k_window(const SigIter *__restrict__ its) {
   const SigIter &it = its[blockIdx.y];
-  if (!it.active) return;
+  if (!it.active || it.tables_valid) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i > it.p2) return;
   double v;
@@ -60,16 +60,24 @@ __global__ void k_window(const SigIter *__restrict__ its) {
   it.wt32[i] = float(v);
 }
 
+__device__ inline float2 *ChirpOf(const SigIter &it, float2 *) { return it.chirp32; }
+__device__ inline double2 *ChirpOf(const SigIter &it, double2 *) { return it.chirp64; }
+__device__ inline float2 *ChatOf(const SigIter &it, float2 *) { return it.chat32; }
+__device__ inline double2 *ChatOf(const SigIter &it, double2 *) { return it.chat64; }
+
+// cond: only signals with more near-tie bins than their list holds (whose
+// iteration is redone in FP64) take part.
 template <typename V>
 __global__ void k_bluestein_setup(const SigIter *__restrict__ its,
-                                  const V *__restrict__ tw) {
+                                  const V *__restrict__ tw, int cond) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *a = reinterpret_cast<V *>(smem_raw);
   const SigIter &it = its[blockIdx.x];
   if (!it.active) return;
+  if (cond ? !RedoFP64(it) : (it.force_fp64 || it.tables_valid)) return;
   const int B = it.bins, M = it.fft_m;
-  V *chirp = reinterpret_cast<V *>(it.chirp);
-  V *chat = reinterpret_cast<V *>(it.chat);
+  V *chirp = ChirpOf(it, (V *)nullptr);
+  V *chat = ChatOf(it, (V *)nullptr);
   const int64_t twoB = 2 * int64_t(B);
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     a[j] = vmake2(0.0, 0.0, (V *)nullptr);
@@ -103,18 +111,78 @@ void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
 
 void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
                           const float2 *tw32, const double2 *tw64,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool cond) {
   if (fp64) {
     const size_t sm = size_t(max_m) * sizeof(double2);
     cudaFuncSetAttribute(k_bluestein_setup<double2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_bluestein_setup<double2><<<nsig, 1024, sm, s>>>(d_its, tw64);
+    k_bluestein_setup<double2><<<nsig, 1024, sm, s>>>(d_its, tw64, cond ? 1 : 0);
   } else {
     const size_t sm = size_t(max_m) * sizeof(float2);
     cudaFuncSetAttribute(k_bluestein_setup<float2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_bluestein_setup<float2><<<nsig, 1024, sm, s>>>(d_its, tw32);
+    k_bluestein_setup<float2><<<nsig, 1024, sm, s>>>(d_its, tw32, cond ? 1 : 0);
   }
+}
+
+}  // namespace mpsft
+
+namespace mpsft {
+
+namespace {
+
+// Deterministic mean |x|^2: block b of signal s sums a fixed grid-stride
+// share in a fixed tree order, then one block adds the partials in order.
+template <typename TX>
+__global__ void k_energy_partial(const void *const *__restrict__ xs,
+                                 const int64_t *__restrict__ ns,
+                                 double *__restrict__ energy) {
+  __shared__ double red[256];
+  const int sig = blockIdx.y;
+  const TX *x = reinterpret_cast<const TX *>(xs[sig]);
+  const int64_t n = ns[sig];
+  // per-thread sums in FP32 (a few thousand terms), combined in FP64
+  float acc = 0.f;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const TX v = x[i];
+    const float re = float(v.x), im = float(v.y);
+    acc = fmaf(re, re, fmaf(im, im, acc));
+  }
+  red[threadIdx.x] = double(acc);
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) energy[size_t(sig) * kEnergyStride + 1 + blockIdx.x] = red[0];
+}
+
+__global__ void k_energy_final(const int64_t *__restrict__ ns,
+                               double *__restrict__ energy) {
+  __shared__ double red[kEnergyBlocks];
+  const int sig = blockIdx.x;
+  double *e = energy + size_t(sig) * kEnergyStride;
+  red[threadIdx.x] = e[1 + threadIdx.x];
+  __syncthreads();
+  for (int o = kEnergyBlocks / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) e[0] = red[0] / double(ns[sig]);
+}
+
+}  // namespace
+
+void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
+                  double *energy, cudaStream_t s) {
+  dim3 grid(kEnergyBlocks, nsig);
+  if (c128) {
+    k_energy_partial<double2><<<grid, 256, 0, s>>>(x, n, energy);
+  } else {
+    k_energy_partial<float2><<<grid, 256, 0, s>>>(x, n, energy);
+  }
+  k_energy_final<<<nsig, kEnergyBlocks, 0, s>>>(n, energy);
 }
 
 }  // namespace mpsft

@@ -15,19 +15,33 @@ void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s);
 
 // Bluestein chirp and FFT(conjugate chirp) of every active signal.
 // fp64 selects double tables.
+// cond: only signals whose iteration is redone in FP64 (more near-tie bins
+// than their list holds) take part (here and in the launchers below).
 void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
                           const float2 *tw32, const double2 *tw64,
-                          cudaStream_t s);
+                          cudaStream_t s, bool cond = false);
 
 // Fold of the windowed, modulated, permuted samples (the time-domain part of
 // BinInTime::Run). x_c128 selects double2 input, fp64 the FP64 arithmetic.
 void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
-                   int max_trials, bool x_c128, bool fp64, cudaStream_t s);
+                   int max_trials, bool x_c128, bool fp64, cudaStream_t s,
+                   bool cond = false);
 
 // Size-B FFT of every folded row, times e^{2 pi i b q / n}, into ubuf.
 void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
                   int max_trials, int max_m, bool fp64, const float2 *tw32,
-                  const double2 *tw64, cudaStream_t s);
+                  const double2 *tw64, cudaStream_t s, bool cond = false);
+
+// Per found mode: k1, bin, window response and the per-trial row-0 term.
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap,
+                    cudaStream_t s);
+
+// mean |x|^2 of each signal into energy[sig * kEnergyStride] (two
+// deterministic passes).
+constexpr int kEnergyBlocks = 256;
+constexpr int kEnergyStride = kEnergyBlocks + 1;
+void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
+                  double *energy, cudaStream_t s);
 
 // Lists of table slots per bin (counting sort by bin).
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
@@ -38,7 +52,16 @@ void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
 // subtract_only, only the mode subtraction of BinInFreq::Run is applied to
 // ubuf in place.
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
-                  bool subtract_only, cudaStream_t s);
+                  bool fp32, bool subtract_only, cudaStream_t s,
+                  bool cond = false);
+
+// FP64 re-binning of the near-tie bins listed by the FP32 decide pass (direct
+// sums over the window support) and their FP64 decisions.
+void LaunchRebin64(const SigIter *d_its, int nsig, bool x_c128, cudaStream_t s);
+// redo: the conditional FP64 kernels follow (signals whose list overflowed are
+// redone whole); without them such signals are reported unresolved.
+void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
+                        bool redo, cudaStream_t s);
 
 // Candidates -> mode table (mm[k0] += coef).
 void LaunchMerge(const SigIter *d_its, int nsig, int max_bins, cudaStream_t s);

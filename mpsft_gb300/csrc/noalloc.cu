@@ -150,8 +150,11 @@ extern "C" int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n,
   it.fold = base + kOffFold;
   it.ubuf = reinterpret_cast<double2 *>(out_device);
   it.bins_cap = bins;
-  it.chirp = base + kOffChirp;
-  it.chat = base + kOffChat;
+  // one region serves the FP32 or the FP64 tables (a call uses one kind)
+  it.chirp32 = reinterpret_cast<float2 *>(base + kOffChirp);
+  it.chat32 = reinterpret_cast<float2 *>(base + kOffChat);
+  it.chirp64 = reinterpret_cast<double2 *>(base + kOffChirp);
+  it.chat64 = reinterpret_cast<double2 *>(base + kOffChat);
 
   SigIter *d_it = reinterpret_cast<SigIter *>(base + kOffIter);
   if (cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice, st) !=

@@ -78,6 +78,21 @@ def test_random_bins(ctx, golden, case, prec):
     assert rel_err(u, golden[f"rb_{name}"]) < TOL_BINS[prec]
 
 
+SMALL_BINS = [c for c in cases.RANDOM_BINS if c[2] <= 101]
+
+
+@pytest.mark.parametrize("case", SMALL_BINS, ids=[c[0] for c in SMALL_BINS])
+def test_direct_bins(ctx, golden, case):
+    """The FP64 direct summation used for the FP32 path's near-tie bins gives
+    the reference's bins (no fold, no size-B FFT)."""
+    name, n, bins, delta, a, b, c, q, seed = case
+    x = cases.random_signal(n, seed)
+    sig = ctx.upload(x)
+    bits = m.load_library().mpsft_num_bits(n, bins)
+    u = ctx.bin_in_time(sig, bins, bits, delta, a, b, c, q, precision=m.FP64_DIRECT)
+    assert rel_err(u, golden[f"rb_{name}"]) < TOL_BINS[m.FP64]
+
+
 @pytest.mark.parametrize("case", cases.RANDOM_BINS, ids=[c[0] for c in cases.RANDOM_BINS])
 def test_bin_in_freq(ctx, golden, case):
     name, n, bins, delta, a, b, c, q, seed = case
