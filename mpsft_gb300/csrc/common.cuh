@@ -27,6 +27,7 @@ constexpr int kMaxFFT64 = 8192;    // largest Bluestein transform (FP64)
 constexpr int32_t kEmptyKey = -1;
 constexpr int kRebinChunks = 16;   // FP64 re-binning: chunks of the support
 constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
+constexpr int kRebinMaxSignals = 256;  // signals per FP64 re-binning launch
 
 // Per-signal status bits written by the device.
 enum : int32_t {
@@ -85,6 +86,8 @@ struct SigIter {
   int32_t *mode_k1;     // (a k0 + b) mod n
   double *mode_wf;      // window response of the mode in its bin
   double2 *mode_base;   // [slot * trials + t]: wf * coef * e^{2 pi i (q_t k1 + c k0)/n}
+  double2 *mode_fac;    // [slot * fac_stride + s]: e^{2 pi i (B 2^s k1 mod n)/n}
+  int32_t fac_stride;   // >= bits of every iteration of the call
   // bucketing of table modes by bin
   int32_t *bkt_count;   // bins_cap
   int32_t *bkt_start;   // bins_cap

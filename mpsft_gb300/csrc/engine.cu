@@ -291,6 +291,8 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->mode_k1 = cv.take<int32_t>(s.tab_cap);
   it->mode_wf = cv.take<double>(s.tab_cap);
   it->mode_base = cv.take<double2>(size_t(s.tab_cap) * s.trials);
+  it->fac_stride = std::max(1, (s.rows_cap - 1) / 2);
+  it->mode_fac = cv.take<double2>(size_t(s.tab_cap) * it->fac_stride);
   it->bkt_count = cv.take<int32_t>(s.bins_cap);
   it->bkt_start = cv.take<int32_t>(s.bins_cap);
   it->bkt_list = cv.take<int32_t>(s.tab_cap);
@@ -466,7 +468,7 @@ int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
   LaunchBluesteinSetup(d_its, nsig, max_m, fp64, ctx->tw32, ctx->tw64, ctx->side);
-  LaunchModePrep(d_its, nsig, max_cap, ctx->side);
+  LaunchModePrep(d_its, nsig, max_cap, max_bits, ctx->side);
   LaunchBucket(d_its, nsig, max_bins, max_cap, ctx->side);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
   LaunchWindow(d_its, nsig, max_p2, s);
@@ -1192,7 +1194,7 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(it.ubuf, sizeof(double2) * it.bins_cap,
                                     inout, row_bytes, row_bytes, it.rows,
                                     cudaMemcpyHostToDevice, st));
-  LaunchModePrep(d_it, 1, s.tab_cap, st);
+  LaunchModePrep(d_it, 1, s.tab_cap, bits, st);
   LaunchBucket(d_it, 1, bins, s.tab_cap, st);
   LaunchDecide(d_it, 1, bins, 1, false, true, st);
   MPSFT_CUDA(ctx, cudaGetLastError());

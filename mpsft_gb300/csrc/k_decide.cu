@@ -20,6 +20,8 @@
 // checks every decision against eps, an upper bound on the bins' FP32
 // rounding error (plus the error carried by the modes it subtracted); a
 // decision closer than eps to its threshold lists the bin for FP64 treatment.
+#include <algorithm>
+
 #include "common.cuh"
 #include "launch.h"
 
@@ -51,6 +53,22 @@ __global__ void k_mode_prep(const SigIter *__restrict__ its) {
   it.mode_k1[s] = int32_t(k1);
   it.mode_wf[s] = wf;
   it.mode_bin[s] = bin;
+}
+
+// Row factors of every found mode: e^{2 pi i (B 2^s k1 mod n)/n} for each bit
+// s (the factor BinInFreqV1 applies to rows 2s+1 / 2s+2, src/binner.cc:584-589),
+// one thread per (occupied slot, bit).
+__global__ void k_mode_fac(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active || it.bits <= 0) return;
+  const int L = it.bits;
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int i = int(idx / L), s = int(idx % L);
+  if (i >= *it.tab_count) return;
+  const int sl = it.occ_list[i];
+  const int64_t off = int64_t(it.bins) << s;
+  it.mode_fac[size_t(sl) * it.fac_stride + s] =
+      UnitPhase64(off * int64_t(it.mode_k1[sl]), it.n);
 }
 
 // Sorts the occupied slots by (bin, k0): one 64-bit key per slot,
@@ -235,12 +253,10 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
     if (t < TR) u0[t] = O::from(src.get(t, 0));
   }
   const int npre = min(nm, 32);
-  int pre_k1 = 0;
   double2 pre_base[TMAX];
   double mode_err = 0;  // FP32 error carried into this bin by the found modes
   if (lane < npre) {
     const int sl = it.bkt_list[st + lane];
-    pre_k1 = it.mode_k1[sl];
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) pre_base[t] = it.mode_base[size_t(sl) * TR + t];
@@ -341,9 +357,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   const int64_t off = has_bit ? (int64_t(B) << lane) : 0;
   for (int i = 0; i < nm; ++i) {
     double2 bs[TMAX];
-    int64_t k1m;
     if (i < 32) {
-      k1m = __shfl_sync(0xffffffffu, pre_k1, i);
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
         if (t < TR) {
@@ -353,14 +367,14 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
       }
     } else {
       const int sl = it.bkt_list[st + i];
-      k1m = it.mode_k1[sl];
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
         if (t < TR) bs[t] = it.mode_base[size_t(sl) * TR + t];
       }
     }
     if (has_bit) {
-      const V fac = O::phase(off * k1m, n, it.phase_shift);
+      const int sl = it.bkt_list[st + i];
+      const V fac = O::from(it.mode_fac[size_t(sl) * it.fac_stride + lane]);
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
         if (t < TR) {
@@ -572,21 +586,31 @@ template <typename TX>
 __global__ void __launch_bounds__(256)
     k_rebin64(const SigIter *__restrict__ its, int nsig) {
   __shared__ double red_re[256], red_im[256];
+  __shared__ int64_t items_end[kRebinMaxSignals];
+  // per-signal item counts, read once per block
+  for (int s = threadIdx.x; s < nsig; s += blockDim.x) {
+    const SigIter &q = its[s];
+    int64_t items = 0;
+    if (q.active && !q.force_fp64) {
+      const int nf = q.flags[2];
+      if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * kRebinChunks;
+    }
+    items_end[s] = items;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int s = 1; s < nsig; ++s) items_end[s] += items_end[s - 1];
+  }
+  __syncthreads();
   for (int64_t w = blockIdx.x;; w += gridDim.x) {
     int sig = -1;
-    int64_t base = 0, local = 0;
+    int64_t local = 0;
     for (int s = 0; s < nsig; ++s) {
-      const SigIter &q = its[s];
-      if (!q.active || q.force_fp64) continue;
-      const int nf = *(volatile int32_t *)&q.flags[2];
-      if (nf > q.esc_cap) continue;
-      const int64_t items = int64_t(nf) * q.trials * q.rows * kRebinChunks;
-      if (w < base + items) {
+      if (w < items_end[s]) {
         sig = s;
-        local = w - base;
+        local = w - (s > 0 ? items_end[s - 1] : 0);
         break;
       }
-      base += items;
     }
     if (sig < 0) return;  // every block agrees: w is uniform
     const SigIter &it = its[sig];
@@ -743,12 +767,16 @@ void LaunchDecideP(const SigIter *d_its, int nsig, int max_bins, int max_trials,
 
 }  // namespace
 
-void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap,
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, int max_bits,
                     cudaStream_t s) {
   // the occupied count is only known on the device: cover the whole table,
   // blocks past the count exit at once
   dim3 grid((max_cap + 255) / 256, nsig);
   k_mode_prep<<<grid, 256, 0, s>>>(d_its);
+  if (max_bits > 0) {
+    dim3 grid2(unsigned((int64_t(max_cap) * max_bits + 255) / 256), nsig);
+    k_mode_fac<<<grid2, 256, 0, s>>>(d_its);
+  }
 }
 
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
@@ -772,8 +800,15 @@ void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
 }
 
 void LaunchRebin64(const SigIter *d_its, int nsig, bool x_c128, cudaStream_t s) {
-  // persistent grid: blocks stride over the (few) work items
+  // persistent grid: blocks stride over the (few) work items; batches are cut
+  // into groups of at most kRebinMaxSignals signals
   const int blocks = 152 * 4;
+  if (nsig > kRebinMaxSignals) {
+    for (int s0 = 0; s0 < nsig; s0 += kRebinMaxSignals) {
+      LaunchRebin64(d_its + s0, std::min(kRebinMaxSignals, nsig - s0), x_c128, s);
+    }
+    return;
+  }
   if (x_c128) {
     k_rebin64<double2><<<blocks, 256, 0, s>>>(d_its, nsig);
   } else {

@@ -33,7 +33,7 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
                   const double2 *tw64, cudaStream_t s, bool cond = false);
 
 // Per found mode: k1, bin, window response and the per-trial row-0 term.
-void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap,
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, int max_bits,
                     cudaStream_t s);
 
 // mean |x|^2 of each signal into energy[sig * kEnergyStride] (two
