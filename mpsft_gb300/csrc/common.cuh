@@ -125,6 +125,30 @@ struct SigIter {
                         // flagged this iteration, [3] mode count
 };
 
+// Per-signal state of a solve run on the device (k_plan / k_finish). The
+// host fills the configuration and the draw table; the device owns the rest.
+enum : int32_t {  // solve status codes (the C ABI's values)
+  kSolveCapacity = 4,
+  kSolveIterCap = 5,
+  kSolveNonFinite = 6,
+};
+struct SolveCtl {
+  // configuration
+  int32_t k, min_bins, trials, draw_stride, max_stale, max_iter;
+  int32_t fp64_path, force_fp64;
+  double sigma, sqrt_c_delta, win_thr, margin;
+  // draws: iteration draw_base + j uses draws[j * (4 + T) ...] =
+  // a, b, c, a_inv, q_0 .. q_{trials-1}, for j < draws_avail, and
+  // draw_bq[(j * T + t) * 2 ...]; T = the largest trials of the batch
+  const int32_t *draws;
+  const double *draw_bq;  // row phase (re, im) per draw and trial, host-made
+  int32_t draw_base, draws_avail;
+  // state
+  int32_t iter, stale, done, status, last_bins;
+  int32_t near_ties, unresolved, fp64_iters;
+  int64_t gathers, bin_bytes;
+};
+
 // ---------------------------------------------------------------- helpers
 __host__ __device__ inline int64_t PosMod(int64_t v, int64_t n) {
   v %= n;

@@ -31,6 +31,17 @@ struct mpsft_ctx {
   // gather/fold (tables, mode preparation and bucketing)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // stream the solve graph is captured on, and the last instantiated graph
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<int64_t> graph_key;
+  // device solve state and draw tables of the current call (in the arena)
+  SolveCtl *d_solve_ctl = nullptr;
+  int32_t *d_draws = nullptr;
+  double *d_draw_bq = nullptr;
+  int64_t graph_body_kernels = 0;
+  bool graph_unavailable = false;
   std::string err;
   bool profiling = false;
   float2 *tw32 = nullptr;
@@ -214,12 +225,27 @@ int CheckN(mpsft_ctx *ctx, int64_t n) {
 // (about 90 dB with the reference's thresholds 3 sigma/sqrt(B), sigma/sqrt(B)).
 constexpr double kPrecisionRatio = 0.01;
 
-// FP32 error-model scalars of an iteration with `bins` bins; `energy` is the
-// signal's mean |x|^2.
+// Precision-policy decision for one signal (FP32 calls): true when its FP32
+// rounding is not small against its noise thresholds. The ratio does not
+// depend on the number of bins, so it is taken once per solve.
+bool PolicyForcesFP64(double margin, int32_t bins, double energy,
+                      double bin_thr, double sv_thr) {
+  const double m = margin > 0 ? margin : kDefaultNearTieMargin;
+  const double eps =
+      m * kEpsRms * std::ldexp(1.0, -24) / std::sqrt(2.0 * bins) * std::sqrt(energy);
+  double scale = 0;
+  if (bin_thr > 0) scale = bin_thr;
+  if (sv_thr > 0) scale = scale > 0 ? std::min(scale, sv_thr) : sv_thr;
+  return scale > 0 && eps > kPrecisionRatio * scale &&
+         (1 << FFTLog2(bins)) <= kMaxFFT64;
+}
+
+// FP32 error-model scalars of an iteration with `bins` bins.
 void SetNearTie(SigIter *it, bool fp64, double margin, int32_t bins,
-                double energy) {
-  it->force_fp64 = 0;
+                bool force) {
+  it->force_fp64 = force ? 1 : 0;
   if (fp64) {
+    it->force_fp64 = 0;
     it->eps_scale = 0;
     it->eps_rel = 0;
     return;
@@ -227,13 +253,6 @@ void SetNearTie(SigIter *it, bool fp64, double margin, int32_t bins,
   const double m = margin > 0 ? margin : kDefaultNearTieMargin;
   it->eps_rel = float(m * std::ldexp(1.0, -24));
   it->eps_scale = m * kEpsRms * std::ldexp(1.0, -24) / std::sqrt(2.0 * bins);
-  double scale = 0;
-  if (it->bin_thr > 0) scale = it->bin_thr;
-  if (it->sv_thr > 0) scale = scale > 0 ? std::min(scale, it->sv_thr) : it->sv_thr;
-  const double eps = it->eps_scale * std::sqrt(energy);
-  if (scale > 0 && eps > kPrecisionRatio * scale && (1 << FFTLog2(bins)) <= kMaxFFT64) {
-    it->force_fp64 = 1;
-  }
 }
 
 // mean |x|^2 of the signals (device values, one synchronisation)
@@ -313,6 +332,11 @@ int EnsureArena(mpsft_ctx *ctx, size_t bytes) {
   if (ctx->arena_size >= bytes) return MPSFT_OK;
   if (ctx->arena) {
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->graph_exec = nullptr;
+    ctx->graph = nullptr;
+    ctx->graph_key.clear();
     cudaFree(ctx->arena);
     ctx->arena = nullptr;
     ctx->arena_size = 0;
@@ -342,6 +366,15 @@ int32_t NextPow2(int64_t v) {
 }
 
 // Fills the per-iteration scalars of it for (bins, bits, transform, q's).
+// bq = e^{2 pi i (b q mod n)/n}, as Sinusoid(MulMod(b, q, n) / n); always
+// computed here on the host so that every loop uses the same values.
+void RowPhase(int32_t b, int32_t q, int32_t n, double *re, double *im) {
+  const int64_t m = (int64_t(b) * q) % n;
+  const double f = double(m) / double(n) * (2.0 * M_PI);
+  *re = std::cos(f);
+  *im = std::sin(f);
+}
+
 void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
               double delta, const Transform &tf, const int32_t *q,
               int32_t trials) {
@@ -368,11 +401,7 @@ void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
   it->active = 1;
   for (int t = 0; t < trials; ++t) {
     it->q[t] = q[t];
-    // bq = e^{2 pi i (b q mod n)/n}, as Sinusoid(MulMod(b, q, n) / n).
-    const int64_t m = (int64_t(tf.b) * q[t]) % sig->n;
-    const double f = double(m) / double(sig->n) * (2.0 * M_PI);
-    it->bq_re[t] = std::cos(f);
-    it->bq_im[t] = std::sin(f);
+    RowPhase(tf.b, q[t], it->n, &it->bq_re[t], &it->bq_im[t]);
   }
   it->width = w.width;
   it->sigma_f = w.sigma_f;
@@ -443,73 +472,88 @@ int64_t BinBytes(const SigIter &it, bool fp64) {
 // Launch sequence of one iteration for nsig signals whose SigIter array is
 // already on the device.
 
-int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
-                    const std::vector<SigIter> &h_its, bool x_c128, bool fp64,
-                    BinTimer *timer, int64_t *launched = nullptr) {
-  int max_bins = 0, max_bits = 0, max_trials = 0, max_p2 = 0, max_m = 0,
-      max_rows = 0;
+// Launch maxima of one iteration (grid sizes and shared memory).
+struct Maxima {
+  int bins = 0, bits = 0, trials = 0, p2 = 0, m = 0, rows = 0, cap = 0;
+};
+
+Maxima MaximaOf(const std::vector<SigIter> &h_its) {
+  Maxima mx;
   for (const SigIter &it : h_its) {
     if (!it.active) continue;
-    max_bins = std::max(max_bins, it.bins);
-    max_bits = std::max(max_bits, it.bits);
-    max_trials = std::max(max_trials, it.trials);
-    max_p2 = std::max(max_p2, it.p2);
-    max_m = std::max(max_m, it.fft_m);
-    max_rows = std::max(max_rows, it.rows);
+    mx.bins = std::max(mx.bins, it.bins);
+    mx.bits = std::max(mx.bits, it.bits);
+    mx.trials = std::max(mx.trials, it.trials);
+    mx.p2 = std::max(mx.p2, it.p2);
+    mx.m = std::max(mx.m, it.fft_m);
+    mx.rows = std::max(mx.rows, it.rows);
+    mx.cap = std::max(mx.cap, it.tab_cap);
   }
-  if (max_bins == 0) return MPSFT_OK;
-  cudaStream_t s = ctx->stream;
-  int max_cap = 0;
-  for (const SigIter &it : h_its) {
-    if (it.active) max_cap = std::max(max_cap, it.tab_cap);
-  }
+  return mx;
+}
+
+// The kernels of one iteration of every active signal, on stream s (and the
+// context's side stream, forked from and joined back into s). any_forced:
+// some signal of an FP32 call takes the FP64 kernels (precision policy).
+int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
+                           const Maxima &mx, bool x_c128, bool fp64,
+                           bool any_forced, BinTimer *timer, int64_t *launched,
+                           cudaStream_t s) {
+  if (mx.bins == 0) return MPSFT_OK;
   // fork: tables, mode preparation and bucketing on the side stream while
   // the window and the gather/fold run on the main one
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-  LaunchBluesteinSetup(d_its, nsig, max_m, fp64, ctx->tw32, ctx->tw64, ctx->side);
-  LaunchModePrep(d_its, nsig, max_cap, max_bits, ctx->side);
-  LaunchBucket(d_its, nsig, max_bins, max_cap, ctx->side);
+  LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
+  LaunchModePrep(d_its, nsig, mx.cap, mx.bits, ctx->side);
+  LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
-  LaunchWindow(d_its, nsig, max_p2, s);
+  LaunchWindow(d_its, nsig, mx.p2, s);
   if (timer) {
     int rc = timer->Begin();
     if (rc) return rc;
   }
-  LaunchBinFold(d_its, nsig, max_bins, max_bits, max_trials, x_c128, fp64, s);
+  LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, fp64, s);
   if (timer) {
     int rc = timer->End();
     if (rc) return rc;
   }
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));  // join
-  LaunchRowFFT(d_its, nsig, max_rows, max_trials, max_m, fp64, ctx->tw32,
-               ctx->tw64, s);
-  LaunchDecide(d_its, nsig, max_bins, max_trials, !fp64, false, s);
+  LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
+               s);
+  LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s);
+  if (launched) *launched += 9;
   if (!fp64) {
     // near ties of the FP32 pass: listed bins re-binned and re-decided in
-    // FP64; signals with more near ties than the list holds redo the whole
-    // iteration in FP64 (each kernel exits at once for the other signals)
-    bool any_forced = false;
-    for (const SigIter &it : h_its) any_forced |= it.active && it.force_fp64;
-    const bool redo = any_forced && max_m <= kMaxFFT64;
+    // FP64; signals that the precision policy sends to FP64 (and signals
+    // whose near-tie list overflowed) run the FP64 kernels
+    const bool redo = any_forced && mx.m <= kMaxFFT64;
     LaunchRebin64(d_its, nsig, x_c128, s);
-    LaunchDecideListed(d_its, nsig, max_trials, redo, s);
-    if (launched) *launched += 3;
+    LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
+    if (launched) *launched += 2;
     if (redo) {
-      if (launched) *launched += 4;
-      LaunchBluesteinSetup(d_its, nsig, max_m, true, ctx->tw32, ctx->tw64, s,
-                           true);
-      LaunchBinFold(d_its, nsig, max_bins, max_bits, max_trials, x_c128, true, s,
+      LaunchBluesteinSetup(d_its, nsig, mx.m, true, ctx->tw32, ctx->tw64, s, true);
+      LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, true, s,
                     true);
-      LaunchRowFFT(d_its, nsig, max_rows, max_trials, max_m, true, ctx->tw32,
+      LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, true, ctx->tw32,
                    ctx->tw64, s, true);
-      LaunchDecide(d_its, nsig, max_bins, max_trials, false, false, s, true);
+      LaunchDecide(d_its, nsig, mx.bins, mx.trials, false, false, s, true);
+      if (launched) *launched += 4;
     }
   }
-  LaunchMerge(d_its, nsig, max_bins, s);
-  if (launched) *launched += 8;
+  LaunchMerge(d_its, nsig, mx.bins, s);
+  if (launched) *launched += 1;
   MPSFT_CUDA(ctx, cudaGetLastError());
   return MPSFT_OK;
+}
+
+int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
+                    const std::vector<SigIter> &h_its, bool x_c128, bool fp64,
+                    BinTimer *timer, int64_t *launched = nullptr) {
+  bool any_forced = false;
+  for (const SigIter &it : h_its) any_forced |= it.active && it.force_fp64;
+  return LaunchIterationKernels(ctx, d_its, nsig, MaximaOf(h_its), x_c128, fp64,
+                                any_forced, timer, launched, ctx->stream);
 }
 
 struct ModeOut {
@@ -555,6 +599,222 @@ int CheckSignal(mpsft_ctx *ctx, const mpsft_signal *sig) {
     return Fail(ctx, MPSFT_ERR_INVALID, "signal belongs to another context");
   }
   return CheckN(ctx, sig->n);
+}
+
+constexpr int kDrawChunk = 32;  // iterations of draws uploaded at a time
+constexpr int kGraphUnavailable = -100;
+static_assert(kSolveCapacity == MPSFT_ERR_CAPACITY &&
+                  kSolveIterCap == MPSFT_ERR_ITER_CAP &&
+                  kSolveNonFinite == MPSFT_ERR_NONFINITE,
+              "device stop codes are the ABI's status codes");
+
+// Fills draws for iterations [base, base + kDrawChunk) of one signal from its
+// RNG, in the reference's order: a, b, c (Transform), then one q per trial;
+// bq gets each trial's row phase (re, im) at [(j * (stride - 4) + t) * 2].
+void FillDraws(mpsft_rng *rng, int32_t n, int32_t trials, int stride,
+               int32_t *out, double *bq) {
+  for (int j = 0; j < kDrawChunk; ++j) {
+    const Transform tf = DrawTransform(rng, n);
+    int32_t *d = out + size_t(j) * stride;
+    double *p = bq + size_t(j) * (stride - 4) * 2;
+    d[0] = tf.a;
+    d[1] = tf.b;
+    d[2] = tf.c;
+    d[3] = tf.a_inv;
+    for (int t = 0; t < trials; ++t) {
+      d[4 + t] = rng->Draw() % n;
+      RowPhase(tf.b, d[4 + t], n, &p[2 * t], &p[2 * t + 1]);
+    }
+  }
+}
+
+// The solve as a CUDA graph: a while node whose body is one iteration of
+// every signal (k_plan, the iteration kernels, k_finish). The host only
+// refills draw tables; the loop ends when every signal has stopped. The RNGs
+// are left exactly where the reference's loop would leave them.
+int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+              const mpsft_solve_options *opts, int nsig,
+              mpsft_rng *const *rngs, const std::vector<Shape> &shapes,
+              SigIter *d_its, std::vector<SigIter> *its,
+              const std::vector<int32_t> &force, bool any_forced, bool fp64,
+              bool x_c128, int64_t *launches) {
+  int tmax = 1;
+  Maxima mx;
+  for (int i = 0; i < nsig; ++i) {
+    tmax = std::max(tmax, opts[i].trials);
+    const Shape &s = shapes[i];
+    mx.bins = std::max(mx.bins, s.bins_cap);
+    mx.bits = std::max(mx.bits, (s.rows_cap - 1) / 2);
+    mx.rows = std::max(mx.rows, s.rows_cap);
+    mx.p2 = std::max(mx.p2, s.p2_cap);
+    mx.m = std::max(mx.m, s.m_cap);
+    mx.cap = std::max(mx.cap, s.tab_cap);
+  }
+  mx.trials = tmax;
+  const int stride = 4 + tmax;
+  // static fields of the iteration descriptors (k_plan fills the rest)
+  for (int i = 0; i < nsig; ++i) {
+    SigIter &it = (*its)[i];
+    it.x = sigs[i]->d_x;
+    it.n = int32_t(sigs[i]->n);
+    it.phase_shift = -1;
+    if (IsPow2(sigs[i]->n)) {
+      int k = 0;
+      while ((int64_t(1) << k) < sigs[i]->n) ++k;
+      it.phase_shift = 32 - k;
+    }
+    it.trials = opts[i].trials;
+    it.active = 0;
+  }
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its->data(), sizeof(SigIter) * nsig,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<SolveCtl> hc(nsig);
+  std::vector<int32_t> hd(size_t(nsig) * kDrawChunk * stride, 0);
+  const size_t bq_per = size_t(kDrawChunk) * tmax * 2;
+  std::vector<double> hb(nsig * bq_per, 0.0);
+  std::vector<mpsft_rng> saved(nsig);
+  for (int i = 0; i < nsig; ++i) {
+    const mpsft_solve_options &o = opts[i];
+    SolveCtl &c = hc[i];
+    std::memset(&c, 0, sizeof(c));
+    c.k = o.k;
+    c.min_bins = o.min_bins;
+    c.trials = o.trials;
+    c.draw_stride = stride;
+    c.max_stale = o.max_stale_iter;
+    c.max_iter = o.max_iter > 0 ? o.max_iter : 64 + 8 * o.k;
+    c.fp64_path = fp64 ? 1 : 0;
+    c.force_fp64 = force[i];
+    c.sigma = o.sigma;
+    c.sqrt_c_delta = std::sqrt(-std::log(o.window_delta));
+    c.win_thr = o.window_threshold;
+    c.margin = o.near_tie_margin > 0 ? o.near_tie_margin : kDefaultNearTieMargin;
+    c.draws = ctx->d_draws + size_t(i) * kDrawChunk * stride;
+    c.draw_bq = ctx->d_draw_bq + i * bq_per;
+    c.draw_base = 0;
+    c.draws_avail = kDrawChunk;
+    c.last_bins = -1;
+    saved[i] = *rngs[i];
+    FillDraws(rngs[i], int32_t(sigs[i]->n), o.trials, stride,
+              hd.data() + size_t(i) * kDrawChunk * stride, hb.data() + i * bq_per);
+  }
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draws, hd.data(), sizeof(int32_t) * hd.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draw_bq, hb.data(), sizeof(double) * hb.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_solve_ctl, hc.data(),
+                                  sizeof(SolveCtl) * nsig, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  // graph (rebuilt when the launch shape or the arena changes)
+  const std::vector<int64_t> key = {
+      int64_t(reinterpret_cast<uintptr_t>(ctx->arena)), nsig, mx.bins, mx.bits,
+      mx.rows, mx.p2, mx.m, mx.cap, mx.trials, fp64, x_c128, any_forced};
+  if (ctx->graph_key != key || ctx->graph_exec == nullptr) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->graph_exec = nullptr;
+    ctx->graph = nullptr;
+    ctx->graph_key.clear();
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaGraph_t g = nullptr;
+    MPSFT_CUDA(ctx, cudaGraphCreate(&g, 0));
+    ctx->graph = g;
+    cudaGraphConditionalHandle handle;
+    MPSFT_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, g, 1,
+                                                     cudaGraphCondAssignDefault));
+    // the params union has no default constructor: zeroed raw storage
+    alignas(cudaGraphNodeParams) unsigned char pbuf[sizeof(cudaGraphNodeParams)];
+    std::memset(pbuf, 0, sizeof(pbuf));
+    cudaGraphNodeParams &p = *reinterpret_cast<cudaGraphNodeParams *>(pbuf);
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = handle;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    MPSFT_CUDA(ctx, cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    MPSFT_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->cap, body, nullptr, nullptr,
+                                                  0, cudaStreamCaptureModeThreadLocal));
+    LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ctx->cap);
+    int64_t per_body = 1;
+    int rc = LaunchIterationKernels(ctx, d_its, nsig, mx, x_c128, fp64, any_forced,
+                                    nullptr, &per_body, ctx->cap);
+    LaunchFinish(ctx->d_solve_ctl, d_its, nsig, handle, true, ctx->cap);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx->cap, &captured);
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ie = cudaErrorUnknown;
+    if (rc == MPSFT_OK && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, g, 0);
+    if (rc != MPSFT_OK || ce != cudaSuccess || ie != cudaSuccess) {
+      // no graph on this device / driver: the host loop takes over
+      cudaGetLastError();
+      cudaGraphDestroy(g);
+      ctx->graph = nullptr;
+      ctx->graph_unavailable = true;
+      for (int i = 0; i < nsig; ++i) *rngs[i] = saved[i];
+      return kGraphUnavailable;
+    }
+    ctx->graph_exec = exec;
+    ctx->graph_key = key;
+    ctx->graph_body_kernels = per_body + 1;
+  }
+  // run until every signal has stopped; refill draw tables in between
+  const int max_launches = 4 + (hc[0].max_iter + kDrawChunk - 1) / kDrawChunk * 2;
+  int64_t body_runs = 0;
+  std::vector<int32_t> prev_iter(nsig, 0);
+  for (int launch = 0;; ++launch) {
+    if (launch > 8 + max_launches * nsig) {
+      return Fail(ctx, MPSFT_ERR_ITER_CAP, "solve graph did not converge");
+    }
+    MPSFT_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(hc.data(), ctx->d_solve_ctl,
+                                    sizeof(SolveCtl) * nsig,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int32_t most = 0;
+    bool all_done = true, refilled = false;
+    for (int i = 0; i < nsig; ++i) {
+      most = std::max(most, hc[i].iter - prev_iter[i]);
+      prev_iter[i] = hc[i].iter;
+      if (hc[i].done) continue;
+      all_done = false;
+      if (hc[i].iter - hc[i].draw_base >= hc[i].draws_avail) {
+        // the next kDrawChunk iterations continue this signal's RNG stream
+        FillDraws(rngs[i], int32_t(sigs[i]->n), opts[i].trials, stride,
+                  hd.data() + size_t(i) * kDrawChunk * stride,
+                  hb.data() + i * bq_per);
+        MPSFT_CUDA(ctx, cudaMemcpyAsync(
+                            ctx->d_draws + size_t(i) * kDrawChunk * stride,
+                            hd.data() + size_t(i) * kDrawChunk * stride,
+                            sizeof(int32_t) * kDrawChunk * stride,
+                            cudaMemcpyHostToDevice, ctx->stream));
+        MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draw_bq + i * bq_per,
+                                        hb.data() + i * bq_per,
+                                        sizeof(double) * bq_per,
+                                        cudaMemcpyHostToDevice, ctx->stream));
+        const int32_t window[2] = {hc[i].iter, kDrawChunk};
+        MPSFT_CUDA(ctx, cudaMemcpyAsync(&ctx->d_solve_ctl[i].draw_base, window,
+                                        sizeof(window), cudaMemcpyHostToDevice,
+                                        ctx->stream));
+        refilled = true;
+      }
+    }
+    body_runs += most;
+    if (all_done) break;
+    if (!refilled) {
+      return Fail(ctx, MPSFT_ERR_CUDA, "solve graph stopped with work left");
+    }
+  }
+  *launches += body_runs * ctx->graph_body_kernels;
+  // leave each RNG as if exactly the used draws had been taken
+  for (int i = 0; i < nsig; ++i) {
+    *rngs[i] = saved[i];
+    for (int32_t j = 0; j < hc[i].iter; ++j) {
+      DrawTransform(rngs[i], int32_t(sigs[i]->n));
+      for (int t = 0; t < opts[i].trials; ++t) rngs[i]->Draw();
+    }
+  }
+  return MPSFT_OK;
 }
 
 // One batched solve; the core of mpsft_solve and mpsft_solve_batched.
@@ -625,6 +885,11 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   bytes += sizeof(SigIter) * nsig + 256;
   bytes += (sizeof(double) * kEnergyStride + sizeof(void *) + sizeof(int64_t)) *
                nsig + 1024;
+  int max_trials_all = 1;
+  for (int i = 0; i < nsig; ++i) max_trials_all = std::max(max_trials_all, opts[i].trials);
+  bytes += (sizeof(SolveCtl) +
+            sizeof(int32_t) * kDrawChunk * (4 + max_trials_all) +
+            sizeof(double) * kDrawChunk * max_trials_all * 2) * nsig + 2048;
   int rc = EnsureArena(ctx, bytes);
   if (rc) return rc;
   rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
@@ -635,6 +900,9 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   double *d_energy = cv.take<double>(size_t(kEnergyStride) * nsig);
   const void **d_xs = cv.take<const void *>(nsig);
   int64_t *d_ns = cv.take<int64_t>(nsig);
+  ctx->d_solve_ctl = cv.take<SolveCtl>(nsig);
+  ctx->d_draws = cv.take<int32_t>(size_t(nsig) * kDrawChunk * (4 + max_trials_all));
+  ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
   for (int i = 0; i < nsig; ++i) {
@@ -661,7 +929,17 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     rc = ReadEnergy(ctx, d_energy, nsig, &energy);
     if (rc) return rc;
   }
-  // All control words are contiguous only per signal; copy them one by one.
+  // precision policy, once per solve (FP32 calls)
+  std::vector<int32_t> force(nsig, 0);
+  bool any_forced = false;
+  for (int i = 0; i < nsig; ++i) {
+    const mpsft_solve_options &o = opts[i];
+    const int32_t b0 = shapes[i].bins_cap;
+    force[i] = !fp64 && PolicyForcesFP64(o.near_tie_margin, b0, energy[i],
+                                         3.0 * o.sigma / std::sqrt(double(b0)),
+                                         o.sigma / std::sqrt(double(b0)));
+    any_forced |= force[i] != 0;
+  }
   struct Run {
     int32_t iter = 0, stale = 0, found = 0, status = MPSFT_OK;
     bool done = false;
@@ -671,8 +949,37 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   };
   std::vector<Run> run(nsig);
   BinTimer timer{ctx};
-  int active = nsig;
   int64_t launches = 0;
+  bool host_loop = ctx->profiling || ctx->graph_unavailable;
+  if (!host_loop) {
+    rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, &its, force,
+                   any_forced, fp64, x_c128, &launches);
+    if (rc == kGraphUnavailable) {
+      // no iteration ran and the tables are untouched; the RNGs are back
+      // where they were
+      host_loop = true;
+    } else if (rc) {
+      return rc;
+    }
+  }
+  if (!host_loop) {
+    std::vector<SolveCtl> h_ctl(nsig);
+    MPSFT_CUDA(ctx, cudaMemcpy(h_ctl.data(), ctx->d_solve_ctl,
+                               sizeof(SolveCtl) * nsig, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nsig; ++i) {
+      Run &r = run[i];
+      const SolveCtl &c = h_ctl[i];
+      r.iter = c.iter;
+      r.stale = c.stale;
+      r.status = c.status;
+      r.gathers = c.gathers;
+      r.bin_bytes = c.bin_bytes;
+      r.near_ties = c.near_ties;
+      r.unresolved = c.unresolved;
+      r.fp64_iters = c.fp64_iters;
+    }
+  }
+  int active = host_loop ? nsig : 0;
   while (active > 0) {
     for (int i = 0; i < nsig; ++i) {
       SigIter &it = its[i];
@@ -692,14 +999,14 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       it.bin_thr = 3.0 * o.sigma / std::sqrt(double(bins));
       it.sv_thr = 1.0 * o.sigma / std::sqrt(double(bins));
       it.win_thr = o.window_threshold;
-      SetNearTie(&it, fp64, o.near_tie_margin, bins, energy[i]);
+      SetNearTie(&it, fp64, o.near_tie_margin, bins, force[i] != 0);
       run[i].fp64_iters += it.force_fp64;
       // same bins as the last iteration: window and Bluestein tables stand
       // (a forced FP64 iteration leaves the FP32 tables unbuilt)
       it.tables_valid = (run[i].last_bins == bins && !it.force_fp64) ? 1 : 0;
       run[i].last_bins = it.force_fp64 ? -1 : bins;
       run[i].gathers += int64_t(it.trials) * it.p * it.rows;
-      run[i].bin_bytes += BinBytes(it, fp64);
+      run[i].bin_bytes += BinBytes(it, fp64 || it.force_fp64);
     }
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
                                     cudaMemcpyHostToDevice, ctx->stream));
@@ -814,6 +1121,7 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
@@ -847,6 +1155,9 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
     cudaStreamSynchronize(ctx->side);
     cudaStreamDestroy(ctx->side);
   }
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  if (ctx->cap) cudaStreamDestroy(ctx->cap);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -1313,7 +1624,9 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
     rc = ReadEnergy(ctx, d_energy, 1, &energy);
     if (rc) return rc;
   }
-  SetNearTie(&it, fp64, opt->near_tie_margin, bins, energy[0]);
+  SetNearTie(&it, fp64, opt->near_tie_margin, bins,
+             !fp64 && PolicyForcesFP64(opt->near_tie_margin, bins, energy[0],
+                                       opt->bin_threshold, opt->sv_threshold));
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   st));
   rc = ClearTable(ctx, it, ctl);

@@ -1,0 +1,157 @@
+// Device-side iteration control of the recovery loop (Demo1::Run,
+// src/demo1.cc:36-59), so that a whole solve runs as one CUDA graph whose
+// iteration body sits under a conditional while node.
+//
+// k_plan (before each iteration, one thread per signal) computes what the
+// reference computes on the host at the start of Iterate: the number of bins
+// B = max(2 (k - found) + 1, min_bins), NumBits, the window scalars
+// (src/window.cc:28-51, with explicitly rounded FP64 operations so that they
+// equal the host's values bit for bit), the thresholds 3 sigma / sqrt(B) and
+// sigma / sqrt(B), and takes the iteration's transform and q's from the draw
+// table the host filled from the signal's RNG in the reference's order
+// (with each trial's row phase e^{2 pi i (b q mod n)/n}, computed there).
+// k_finish (after the merge) applies the stop rule: count the iteration, a
+// stale one when nothing was found, stop after max_stale_iter stale ones (never
+// reset), on a status, or at max_iter; then it sets the while condition to
+// "some signal still has work and draws".
+#include "common.cuh"
+#include "launch.h"
+
+namespace mpsft {
+
+namespace {
+
+__device__ int32_t NumBitsDev(int32_t n, int32_t bins) {
+  if (n < bins) return 1;
+  int32_t out = 0;
+  while (n >= bins) {
+    n >>= 1;
+    ++out;
+  }
+  return out;
+}
+
+__global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
+                       int nsig) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsig) return;
+  SolveCtl &c = ctl[i];
+  SigIter &it = its[i];
+  const int local = c.iter - c.draw_base;
+  if (c.done || local >= c.draws_avail) {
+    it.active = 0;
+    return;
+  }
+  const int32_t found = *it.tab_count;
+  int32_t bins = (c.k - found) * 2 + 1;
+  if (bins < c.min_bins) bins = c.min_bins;
+  const int32_t bits = NumBitsDev(it.n, bins);
+  const double B = double(bins);
+  // Window scalars in the reference's operation order, no contraction.
+  const double width = __ddiv_rn(1.0, __dmul_rn(2.0, B));
+  const double sq = c.sqrt_c_delta;
+  const double sigma_f =
+      __ddiv_rn(0.5, __dmul_rn(__dmul_rn(__dmul_rn(B, 2.0), M_SQRT2), sq));
+  const double sigma_t = __ddiv_rn(1.0, __dmul_rn(2.0 * M_PI, sigma_f));
+  const double tmp =
+      __dadd_rn(__dmul_rn(__dmul_rn(2.0 * M_SQRT2, sigma_t), sq), 1.0);
+  int32_t f = int32_t(ceil(__ddiv_rn(tmp, B)));
+  if (f % 2 == 0) ++f;
+  it.bins = bins;
+  it.bits = bits;
+  it.rows = 1 + 2 * bits;
+  it.folds = f;
+  it.p = f * bins;
+  it.p2 = (it.p - 1) / 2;
+  it.width = width;
+  it.sigma_f = sigma_f;
+  it.erf_d = __dmul_rn(M_SQRT2 * M_PI, sigma_t);
+  const int32_t *d = c.draws + size_t(local) * c.draw_stride;
+  const double *bq = c.draw_bq + size_t(local) * (c.draw_stride - 4) * 2;
+  it.a = d[0];
+  it.b = d[1];
+  it.c = d[2];
+  it.a_inv = d[3];
+  it.trials = c.trials;
+  for (int t = 0; t < c.trials; ++t) {
+    it.q[t] = d[4 + t];
+    it.bq_re[t] = bq[2 * t];
+    it.bq_im[t] = bq[2 * t + 1];
+  }
+  const double rb = __dsqrt_rn(B);
+  it.bin_thr = __ddiv_rn(__dmul_rn(3.0, c.sigma), rb);
+  it.sv_thr = __ddiv_rn(c.sigma, rb);
+  it.win_thr = c.win_thr;
+  int l = 0;
+  while ((1 << l) < 2 * bins - 1) ++l;
+  it.fft_log2m = l;
+  it.fft_m = 1 << l;
+  it.force_fp64 = c.force_fp64;
+  if (!c.fp64_path) {
+    it.eps_rel = float(c.margin * 5.9604644775390625e-08);  // margin * 2^-24
+    it.eps_scale = c.margin * double(kEpsRms) * 5.9604644775390625e-08 / sqrt(2.0 * B);
+  } else {
+    it.eps_rel = 0.f;
+    it.eps_scale = 0.0;
+  }
+  it.tables_valid = (c.last_bins == bins && !c.force_fp64) ? 1 : 0;
+  it.flags[0] = 0;
+  it.flags[1] = 0;
+  it.flags[2] = 0;
+  it.active = 1;
+}
+
+__global__ void __launch_bounds__(1024)
+    k_finish(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its, int nsig,
+             cudaGraphConditionalHandle handle, int set_condition) {
+  int any = 0;
+  for (int i = threadIdx.x; i < nsig; i += blockDim.x) {
+    SolveCtl &c = ctl[i];
+    SigIter &it = its[i];
+    if (it.active) {
+      const int32_t *fl = it.flags;
+      c.iter += 1;
+      c.near_ties += fl[2];
+      if (fl[1] & kStatusUnresolved) c.unresolved += 1;
+      c.fp64_iters += it.force_fp64;
+      const int64_t g = int64_t(it.trials) * it.p * it.rows;
+      const bool f64 = c.fp64_path || it.force_fp64;
+      c.gathers += g;
+      c.bin_bytes += 32 * g + int64_t(f64 ? 8 : 4) * (it.p2 + 1) +
+                     int64_t(it.trials) * (f64 ? 16 : 8) * it.rows * it.bins;
+      if (fl[1] & kStatusCapacity) {
+        c.status = kSolveCapacity;
+      } else if (fl[1] & kStatusNonFinite) {
+        c.status = kSolveNonFinite;
+      } else if (int64_t(fl[3]) * 2 > it.tab_cap) {
+        c.status = kSolveCapacity;
+      }
+      if (!fl[0]) c.stale += 1;
+      if (c.status == 0 && c.stale < c.max_stale && c.iter >= c.max_iter) {
+        c.status = kSolveIterCap;
+      }
+      if (c.status != 0 || c.stale >= c.max_stale) c.done = 1;
+      c.last_bins = it.force_fp64 ? -1 : it.bins;
+      it.active = 0;
+    }
+    if (!c.done && c.iter - c.draw_base < c.draws_avail) any = 1;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0 && set_condition) {
+    cudaGraphSetConditional(handle, any ? 1u : 0u);
+  }
+}
+
+}  // namespace
+
+void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, cudaStream_t s) {
+  k_plan<<<(nsig + 127) / 128, 128, 0, s>>>(ctl, its, nsig);
+}
+
+void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
+                  cudaGraphConditionalHandle handle, bool set_condition,
+                  cudaStream_t s) {
+  k_finish<<<1, 1024, 0, s>>>(ctl, its, nsig, handle, set_condition ? 1 : 0);
+}
+
+}  // namespace mpsft

@@ -70,6 +70,13 @@ void LaunchMerge(const SigIter *d_its, int nsig, int max_bins, cudaStream_t s);
 void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,
                        const double2 *coef, int64_t m, cudaStream_t s);
 
+// Device-side control of a solve: iteration planning and the stop rule
+// (sets the while condition of the solve graph when set_condition).
+void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, cudaStream_t s);
+void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
+                  cudaGraphConditionalHandle handle, bool set_condition,
+                  cudaStream_t s);
+
 // Batched 2x2 pencils.
 void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
                   int32_t *vote, cudaStream_t s);

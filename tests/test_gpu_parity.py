@@ -193,11 +193,13 @@ def test_batched_equals_single(ctx):
     from mpsft_gb300.signals import make_signal
 
     sigs, opts, rngs, singles = [], [], [], []
-    for i, (n, s) in enumerate([(1 << 16, 40), (1 << 18, 120), (65537, 60)]):
+    # different trials per signal share one batch (one draw table stride)
+    for i, (n, s, tr) in enumerate([(1 << 16, 40, 3), (1 << 18, 120, 7),
+                                    (65537, 60, 5)]):
         sg = make_signal(n, s, 100 + i, sigma=1e-5)
         sigs.append(ctx.upload(sg.x))
         opts.append(ctx.solve_options(s, sg.sigma, min_bins=51, window_delta=1e-5,
-                                      max_stale_iter=5))
+                                      max_stale_iter=5, trials=tr))
         rngs.append(m.Rng(777 + i))
         singles.append(ctx.solve(sigs[-1], m.Rng(777 + i), opts[-1])[0])
     out, stats = ctx.solve_batched(sigs, rngs, opts)
@@ -219,6 +221,33 @@ def test_deterministic(ctx, prec):
     k2, c2, _ = ctx.solve_arrays(sig, m.Rng(9), opt)
     assert np.array_equal(k1, k2) and np.array_equal(c1.view(np.uint64),
                                                      c2.view(np.uint64))
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+def test_graph_loop_equals_host_loop(ctx, prec):
+    """The solve as one CUDA graph (device-side stop rule, draw tables refilled
+    between launches) against the host-driven loop that profiling selects:
+    same modes bit for bit, same iteration count, RNG left at the same draw.
+    max_stale_iter=40 runs past one table of 32 draws."""
+    from mpsft_gb300.signals import make_signal
+
+    sg = make_signal(1 << 16, 30, 21, sigma=1e-5)
+    sig = ctx.upload(sg.x)
+    opt = ctx.solve_options(30, sg.sigma, min_bins=51, window_delta=1e-5,
+                            max_stale_iter=40, precision=prec)
+    r1, r2 = m.Rng(31), m.Rng(31)
+    k1, c1, s1 = ctx.solve_arrays(sig, r1, opt)
+    ctx.set_profiling(True)
+    try:
+        k2, c2, s2 = ctx.solve_arrays(sig, r2, opt)
+    finally:
+        ctx.set_profiling(False)
+    assert s1.iterations == s2.iterations > 40
+    assert np.array_equal(k1, k2)
+    assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64))
+    assert [r1.int32() for _ in range(4)] == [r2.int32() for _ in range(4)]
+    assert s1.gathers == s2.gathers and s1.bin_bytes == s2.bin_bytes
+    assert s1.escalated == s2.escalated and s1.status == s2.status == 0
 
 
 # ------------------------------------------------------------ error paths
