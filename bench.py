@@ -51,13 +51,16 @@ WORKLOAD = ("MPSFT recovery (Demo1::Run loop), N=2^22 complex64, S=1000, "
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--batch", type=int, default=8, help="signals per step per GPU")
     p.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="bounded CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile-case", action="store_true",
+                   help="one batched solve with the host-driven loop and "
+                        "nothing else (the case the ncu summaries capture)")
     return p.parse_args()
 
 
@@ -86,7 +89,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -259,44 +262,61 @@ def run_gpu(args) -> None:
         rngs = [m.Rng(SEED_RNG + i) for i in range(G)]
         return ctx.solve_batched(sigs, rngs, opts)
 
+    if args.profile_case:
+        ctx.set_profiling(True)
+        step()
+        torch.cuda.synchronize()
+        return
+
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
 
-    # ---- device-resident timed region (also times every binning launch)
-    ctx.set_profiling(True)
+    # ---- device-resident timed region: solves exactly as a user runs them
     clocks = ClockSampler(local)
     clocks.start()
+    time.sleep(0.3)  # first nvidia-smi sample before the region starts
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    bin_ms = 0.0
-    bin_bytes = 0
-    bin_launches = 0
     iters = []
     launches = 0
     near = 0
     for _ in range(args.steps):
         out, stats = step()
         near += sum(s["escalated"] for s in stats)
-        bin_ms += stats[0]["bin_ms"]
-        bin_launches += stats[0]["bin_launches"]
-        bin_bytes += sum(s["bin_bytes"] for s in stats)
         iters += [s["iterations"] for s in stats]
         launches += stats[0]["kernel_launches"]
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ctx.set_profiling(False)
     ms = ev0.elapsed_time(ev1)
     t_rank = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t_rank, op=dist.ReduceOp.MAX)
     ms_max = float(t_rank.item())
     value = world * G * args.steps / (ms_max / 1e3)
+
+    # ---- the same steps again with an event pair around every binning
+    # launch (the host drives the iterations here); gives the binning roofline
+    ctx.set_profiling(True)
+    bin_ms = 0.0
+    bin_bytes = 0
+    bin_launches = 0
+    bin_gathers = 0
+    for _ in range(args.steps):
+        out, stats = step()
+        bin_ms += stats[0]["bin_ms"]
+        bin_launches += stats[0]["bin_launches"]
+        bin_bytes += sum(s["bin_bytes"] for s in stats)
+        bin_gathers += sum(s["gathers"] for s in stats)
+    torch.cuda.synchronize()
+    ctx.set_profiling(False)
 
     # ---- end to end through the public API from pinned host buffers
     h2d = G * N * 8
@@ -344,6 +364,10 @@ def run_gpu(args) -> None:
         achieved = (bin_bytes / (bin_ms / 1e3)) / 1e9 if bin_ms > 0 else None
         gathers_per_launch = None
         traffic_per_gather = profile_traffic()
+        # DRAM bytes of an average binning launch: the captured launch's bytes
+        # per gathered sample times the gathers of an average launch
+        traffic = (traffic_per_gather * bin_gathers / bin_launches
+                   if traffic_per_gather and bin_launches else None)
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3),
@@ -361,7 +385,9 @@ def run_gpu(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-                         "traffic": traffic_per_gather,
+                         "traffic": traffic,
+                         "achieved_bytes_per_launch": (bin_bytes / bin_launches
+                                                       if bin_launches else None),
                          "kernel": "k_bin_fold32 (gather/window/modulate/fold)",
                          "bytes_model": "32 B sector per gathered sample + window "
                                         "table + fold output",

@@ -47,9 +47,11 @@ enum { MPSFT_C64 = 1, MPSFT_C128 = 2 };
 /* FP32: binning, fold (compensated) and size-B FFT in FP32; mode subtraction,
  *       pencil, thresholds and coefficients in FP64.
  * FP64: everything in FP64 (the plain per-signal path). */
-/* FP64_DIRECT (mpsft_bin_in_time only): every bin as a direct FP64 sum over
- * the window support, without the fold and the size-B FFT (the evaluation the
- * FP32 path uses for its near-tie bins); slow, for checking. */
+/* FP64_DIRECT (mpsft_bin_in_time only): every bin as a direct sum over the
+ * window support, without the fold and the size-B FFT (the evaluation the
+ * FP32 path uses for its near-tie bins): float-float products and 64-sample
+ * block sums (about 2^-47 relative), block totals in FP64; slow, for
+ * checking. */
 enum { MPSFT_PREC_FP32 = 0, MPSFT_PREC_FP64 = 1, MPSFT_PREC_FP64_DIRECT = 2 };
 
 typedef struct mpsft_ctx mpsft_ctx;

@@ -67,6 +67,7 @@ struct SigIter {
   // buffers
   float *wt32;
   double *wt64;
+  float2 *wtff;         // wt64 as float-float (hi, lo); may be null
   void *fold;           // FP32: float2, FP64: double2
   double2 *ubuf;
   int32_t bins_cap;     // row stride of fold / ubuf
@@ -106,9 +107,13 @@ struct SigIter {
   const double *x_energy;
   float *eps_dev;       // eps_scale * sqrt(*x_energy), set by k_bucket
   float *row_max;       // [t * rows + r]: max |U| of the row (k_row_fft)
-  // FP64 re-binning of listed bins: [((e * trials + t) * rows + r) * chunks
-  // + c] partial sums over chunk c of the window support
+  // re-binning of listed bins: [((e * trials + t) * rows + r) * chunks + c]
+  // partial sums over chunk c of the window support
   double2 *esc_part;
+  // per listed bin e: s^k, k < 64, with s = e^{2 pi i (b/n - (2 beta + 1)/(2B))}
+  // as float-float {re.hi, im.hi, re.lo, im.lo} at [e * 64 + k], and s^64
+  float4 *esc_pow;
+  double2 *esc_step;
   // per-value part of the FP32 error bound: eps_rel * (kEpsRowMax * max |U|
   // of the rows involved + kEpsValue * |value|)
   float eps_rel;

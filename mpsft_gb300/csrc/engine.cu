@@ -289,6 +289,7 @@ struct Shape {
 void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->wt32 = cv.take<float>(size_t(s.p2_cap) + 1);
   it->wt64 = cv.take<double>(size_t(s.p2_cap) + 1);
+  it->wtff = cv.take<float2>(size_t(s.p2_cap) + 1);
   const size_t cells = size_t(s.trials) * s.rows_cap * s.bins_cap;
   // 16-byte cells: the FP32 path may redo an iteration in FP64
   it->fold = cv.take<double2>(cells);
@@ -319,6 +320,8 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->cand_k0 = cv.take<int32_t>(s.bins_cap);
   it->cand_coef = cv.take<double2>(s.bins_cap);
   it->cand_err = cv.take<double>(s.bins_cap);
+  it->esc_pow = cv.take<float4>(size_t(kMaxListed) * 64);
+  it->esc_step = cv.take<double2>(kMaxListed);
   it->esc_list = cv.take<int32_t>(kMaxListed);
   it->esc_mask = cv.take<uint32_t>(kMaxListed);
   it->esc_cap = kMaxListed;
@@ -528,7 +531,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     // FP64; signals that the precision policy sends to FP64 (and signals
     // whose near-tie list overflowed) run the FP64 kernels
     const bool redo = any_forced && mx.m <= kMaxFFT64;
-    LaunchRebin64(d_its, nsig, x_c128, s);
+    LaunchRebin(d_its, nsig, kMaxListed, x_c128, s);
     LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
     if (launched) *launched += 2;
     if (redo) {
@@ -1373,7 +1376,9 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   const size_t direct_cells = direct ? size_t(bins) * s.rows_cap * kRebinChunks : 0;
   rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 1024 +
                             direct_cells * sizeof(double2) +
-                            (direct ? sizeof(int32_t) * bins : 0));
+                            (direct ? (sizeof(int32_t) + sizeof(double2) +
+                                       64 * sizeof(float4)) * size_t(bins) + 1024
+                                    : 0));
   if (rc) return rc;
   Carve cv{ctx->arena};
   SigIter *d_it = cv.take<SigIter>(1);
@@ -1386,6 +1391,8 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
     // every bin is a listed bin of the FP64 re-binning kernel
     it.esc_part = cv.take<double2>(direct_cells);
     it.esc_list = cv.take<int32_t>(bins);
+    it.esc_pow = cv.take<float4>(size_t(bins) * 64);
+    it.esc_step = cv.take<double2>(bins);
     it.esc_mask = nullptr;  // every row of every bin
     it.esc_cap = bins;
     std::vector<int32_t> iota(bins);
@@ -1399,7 +1406,7 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                     st));
     LaunchWindow(d_it, 1, it.p2, st);
-    LaunchRebin64(d_it, 1, sig->dtype == MPSFT_C128, st);
+    LaunchRebin(d_it, 1, bins, sig->dtype == MPSFT_C128, st);
     MPSFT_CUDA(ctx, cudaGetLastError());
     std::vector<double2> part(direct_cells);
     MPSFT_CUDA(ctx, cudaMemcpyAsync(part.data(), it.esc_part,

@@ -574,131 +574,6 @@ __global__ void __launch_bounds__(256)
                           kDecideExact);
 }
 
-// ---------------------------------------------------------------- rebin
-// Direct FP64 evaluation of listed bins:
-//   U_r[beta] = sum_{t=-p2}^{p2} x[(a (tau_r + t) + c) mod n] wt(t)
-//               e^{2 pi i ((b (tau_r + t) mod n)/n - (2 beta + 1) t/(2B))}
-// (the fold and the size-B DFT in one sum). Work item = (signal, listed bin,
-// trial, row, chunk of the support); each thread sums a contiguous run of t,
-// anchoring the phase exactly from integers at the run's start and stepping
-// it by one complex multiplication per sample.
-template <typename TX>
-__global__ void __launch_bounds__(256)
-    k_rebin64(const SigIter *__restrict__ its, int nsig) {
-  __shared__ double red_re[256], red_im[256];
-  __shared__ int64_t items_end[kRebinMaxSignals];
-  // per-signal item counts, read once per block
-  for (int s = threadIdx.x; s < nsig; s += blockDim.x) {
-    const SigIter &q = its[s];
-    int64_t items = 0;
-    if (q.active && !q.force_fp64) {
-      const int nf = q.flags[2];
-      if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * kRebinChunks;
-    }
-    items_end[s] = items;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int s = 1; s < nsig; ++s) items_end[s] += items_end[s - 1];
-  }
-  __syncthreads();
-  for (int64_t w = blockIdx.x;; w += gridDim.x) {
-    int sig = -1;
-    int64_t local = 0;
-    for (int s = 0; s < nsig; ++s) {
-      if (w < items_end[s]) {
-        sig = s;
-        local = w - (s > 0 ? items_end[s - 1] : 0);
-        break;
-      }
-    }
-    if (sig < 0) return;  // every block agrees: w is uniform
-    const SigIter &it = its[sig];
-    const int c = int(local % kRebinChunks);
-    local /= kRebinChunks;
-    const int r = int(local % it.rows);
-    local /= it.rows;
-    const int t = int(local % it.trials);
-    const int e = int(local / it.trials);
-    const int beta = it.esc_list[e];
-    if (it.esc_mask != nullptr && !RowListed(it.esc_mask[e], r)) continue;
-    const int64_t n = it.n;
-    const int64_t B = it.bins;
-    int64_t off = 0;
-    if (r > 0) {
-      const int s = (r - 1) / 2;
-      off = (r & 1) ? (B << s) : -(B << s);
-    }
-    const int64_t tau = int64_t(it.q[t]) + off;
-    const int64_t p = it.p;
-    const int64_t chunk = (p + kRebinChunks - 1) / kRebinChunks;
-    const int64_t c0 = -int64_t(it.p2) + c * chunk;
-    const int64_t c1 = min(c0 + chunk, int64_t(it.p2) + 1);
-    const int64_t per = (chunk + blockDim.x - 1) / blockDim.x;
-    const int64_t t0 = c0 + int64_t(threadIdx.x) * per;
-    const int64_t t1 = min(t0 + per, c1);
-    double ar = 0, ai = 0;
-    if (t0 < t1) {
-      const int64_t twoB = 2 * B;
-      const int64_t g = 2 * int64_t(beta) + 1;
-      uint32_t j = uint32_t(PosMod(int64_t(it.a) * PosMod(tau + t0, n) + it.c, n));
-      const uint32_t astep = uint32_t(PosMod(it.a, n));
-      const int64_t m0 = PosMod(int64_t(it.b) * PosMod(tau + t0, n), n);
-      const int64_t r0 = PosMod(g * t0, twoB);
-      double s, co;
-      sincospi(2.0 * (double(m0) / double(n) - double(r0) / double(twoB)), &s, &co);
-      double pr = co, pi = s;
-      const double dth = double(PosMod(it.b, n)) / double(n) -
-                         double(PosMod(g, twoB)) / double(twoB);
-      sincospi(2.0 * dth, &s, &co);
-      const double dr = co, di = s;
-      const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
-      const uint32_t nn = uint32_t(n);
-      // batches of 8 samples: indices and loads first, then the FP64 sums
-      for (int64_t tb = t0; tb < t1; tb += 8) {
-        TX v[8];
-        double w[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int64_t tt = tb + k;
-          if (tt < t1) {
-            v[k] = __ldg(&x[j]);
-            w[k] = __ldg(&it.wt64[tt < 0 ? -tt : tt]);
-            j += astep;
-            if (j >= nn) j -= nn;
-          }
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          if (tb + k < t1) {
-            const double vx = double(v[k].x) * w[k], vy = double(v[k].y) * w[k];
-            ar += vx * pr - vy * pi;
-            ai += vx * pi + vy * pr;
-            const double npr = pr * dr - pi * di;
-            pi = pr * di + pi * dr;
-            pr = npr;
-          }
-        }
-      }
-    }
-    red_re[threadIdx.x] = ar;
-    red_im[threadIdx.x] = ai;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (threadIdx.x < o) {
-        red_re[threadIdx.x] += red_re[threadIdx.x + o];
-        red_im[threadIdx.x] += red_im[threadIdx.x + o];
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      it.esc_part[((size_t(e) * it.trials + t) * it.rows + r) * kRebinChunks + c] =
-          make_double2(red_re[0], red_im[0]);
-    }
-    __syncthreads();
-  }
-}
-
 // ---------------------------------------------------------------- merge
 __device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef,
                            double err) {
@@ -796,23 +671,6 @@ void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
   } else {
     LaunchDecideP<double>(d_its, nsig, max_bins, max_trials, mode, cond ? 1 : 0,
                           s);
-  }
-}
-
-void LaunchRebin64(const SigIter *d_its, int nsig, bool x_c128, cudaStream_t s) {
-  // persistent grid: blocks stride over the (few) work items; batches are cut
-  // into groups of at most kRebinMaxSignals signals
-  const int blocks = 152 * 4;
-  if (nsig > kRebinMaxSignals) {
-    for (int s0 = 0; s0 < nsig; s0 += kRebinMaxSignals) {
-      LaunchRebin64(d_its + s0, std::min(kRebinMaxSignals, nsig - s0), x_c128, s);
-    }
-    return;
-  }
-  if (x_c128) {
-    k_rebin64<double2><<<blocks, 256, 0, s>>>(d_its, nsig);
-  } else {
-    k_rebin64<float2><<<blocks, 256, 0, s>>>(d_its, nsig);
   }
 }
 

@@ -1,0 +1,271 @@
+// Re-binning of the near-tie bins listed by the FP32 decide pass, with
+// FP64-class accuracy but on the FP32 pipes (this part has only about 1/64 of
+// the FP32 rate in FP64 arithmetic).
+//
+// A listed bin beta of row r (offset tau_r = q + off) is evaluated directly,
+// without the fold and the FFT:
+//   U_r[beta] = sum_{t=-p2}^{p2} x[(a (tau_r + t) + c) mod n] wt(t) e^{2 pi i phi(t)},
+//   phi(t) = (b (tau_r + t) mod n)/n - (2 beta + 1) t/(2B)
+// (the fold, the size-B DFT and the row factor of BinInTime::Run in one sum,
+// src/binner.cc:394-521). phi advances by the same Delta = b/n - (2 beta + 1)/(2B)
+// (mod 1) per sample, so with s = e^{2 pi i Delta} a run of samples starting
+// at t0 is
+//   sum_{k} x_k w_k e^{2 pi i phi(t0 + k)} = sum_blocks A_blk sum_{k<64} x_k w_k s^k,
+// A_blk = e^{2 pi i phi(t0)} s^{64 blk}. The inner sums run in float-float
+// arithmetic (each value as an unevaluated sum hi + lo of two floats, about
+// 2^-47 relative) against a per-bin table of s^k (k < 64) computed in FP64
+// from exact integer phases; each block sum then enters an FP64 total through
+// A_blk. The window comes from a float-float table of the FP64 window.
+//
+// Work item = (signal, listed bin, trial, listed row, chunk of the support),
+// one warp each; the 32 lanes split the chunk into consecutive runs; lane sums
+// are combined by a fixed shuffle tree and the chunk partials are added in
+// chunk order by the FP64 decision (so the result does not depend on the
+// scheduling).
+#include "common.cuh"
+#include "launch.h"
+
+namespace mpsft {
+
+namespace {
+
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF FFOf(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - double(h))};
+}
+
+// x*y + u*v in float-float: exact products of the high parts (FMA), two-sum
+// of those, the cross terms in the low word, then renormalisation.
+__device__ __forceinline__ FF DotFF(FF x, FF y, FF u, FF v) {
+  const float p1 = __fmul_rn(x.hi, y.hi);
+  const float e1 = fmaf(x.hi, y.hi, -p1);
+  const float p2 = __fmul_rn(u.hi, v.hi);
+  const float e2 = fmaf(u.hi, v.hi, -p2);
+  const float s = __fadd_rn(p1, p2);
+  const float bb = __fsub_rn(s, p1);
+  float lo = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, bb)), __fsub_rn(p2, bb));
+  lo = __fadd_rn(lo, __fadd_rn(e1, e2));
+  lo = fmaf(x.hi, y.lo, lo);
+  lo = fmaf(x.lo, y.hi, lo);
+  lo = fmaf(u.hi, v.lo, lo);
+  lo = fmaf(u.lo, v.hi, lo);
+  const float h = __fadd_rn(s, lo);
+  return {h, __fsub_rn(lo, __fsub_rn(h, s))};
+}
+
+// acc += t (two-sum of the high words, renormalised)
+__device__ __forceinline__ void AccFF(FF &acc, FF t) {
+  const float s = __fadd_rn(acc.hi, t.hi);
+  const float bb = __fsub_rn(s, acc.hi);
+  float lo = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(t.hi, bb));
+  lo = __fadd_rn(lo, __fadd_rn(acc.lo, t.lo));
+  const float h = __fadd_rn(s, lo);
+  acc.lo = __fsub_rn(lo, __fsub_rn(h, s));
+  acc.hi = h;
+}
+
+__device__ __forceinline__ FF Neg(FF a) { return {-a.hi, -a.lo}; }
+
+// x * w with x an input sample and w the float-float window: complex64
+// samples are exact floats (exact product of the high word by FMA); complex128
+// samples are multiplied in FP64 first.
+__device__ __forceinline__ void SampleTimesWindow(float2 v, float2 w, FF *re,
+                                                  FF *im) {
+  float p = __fmul_rn(v.x, w.x);
+  re->hi = p;
+  re->lo = fmaf(v.x, w.y, fmaf(v.x, w.x, -p));
+  p = __fmul_rn(v.y, w.x);
+  im->hi = p;
+  im->lo = fmaf(v.y, w.y, fmaf(v.y, w.x, -p));
+}
+__device__ __forceinline__ void SampleTimesWindow(double2 v, float2 w, FF *re,
+                                                  FF *im) {
+  const double wd = double(w.x) + double(w.y);
+  *re = FFOf(v.x * wd);
+  *im = FFOf(v.y * wd);
+}
+
+constexpr int kPowLen = 64;  // s^k table length = block of samples
+
+// Phase e^{2 pi i k Delta} from exact integer reductions:
+// k Delta = (k b mod n)/n - (k (2 beta + 1) mod 2B)/(2B) (mod 1).
+__device__ inline double2 PowerOfStep(int64_t k, int64_t b, int64_t g,
+                                      int64_t n, int64_t twoB) {
+  const int64_t m = PosMod(k * b, n);
+  const int64_t r = PosMod(k * g, twoB);
+  double s, c;
+  sincospi(2.0 * (double(m) / double(n) - double(r) / double(twoB)), &s, &c);
+  return make_double2(c, s);
+}
+
+// One warp per listed bin: s^k (k < 64) as float-float complex
+// {re.hi, im.hi, re.lo, im.lo} and s^64 in FP64 (esc_pow / esc_step hold
+// esc_cap bins).
+__global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active || it.force_fp64) return;
+  const int nf = *(volatile int32_t *)&it.flags[2];
+  if (nf > it.esc_cap) return;
+  const int e = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (e >= nf) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t n = it.n, twoB = 2 * int64_t(it.bins);
+  const int64_t b = PosMod(it.b, n);
+  const int64_t g = 2 * int64_t(it.esc_list[e]) + 1;
+  float4 *pw = it.esc_pow + size_t(e) * kPowLen;
+  for (int k = lane; k < kPowLen; k += 32) {
+    const double2 z = PowerOfStep(k, b, g, n, twoB);
+    const FF zr = FFOf(z.x), zi = FFOf(z.y);
+    pw[k] = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
+  }
+  if (lane == 0) it.esc_step[e] = PowerOfStep(kPowLen, b, g, n, twoB);
+}
+
+template <typename TX>
+__global__ void __launch_bounds__(256, 2)
+    k_rebin_ff(const SigIter *__restrict__ its, int nsig) {
+  __shared__ int64_t items_end[kRebinMaxSignals];
+  __shared__ float4 pw_s[8][kPowLen];
+  for (int s = threadIdx.x; s < nsig; s += blockDim.x) {
+    const SigIter &q = its[s];
+    int64_t items = 0;
+    if (q.active && !q.force_fp64) {
+      const int nf = *(volatile int32_t *)&q.flags[2];
+      if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * kRebinChunks;
+    }
+    items_end[s] = items;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int s = 1; s < nsig; ++s) items_end[s] += items_end[s - 1];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float4 *pw = pw_s[warp];
+  const int64_t total = items_end[nsig - 1];
+  for (int64_t w = int64_t(blockIdx.x) * 8 + warp; w < total;
+       w += int64_t(gridDim.x) * 8) {
+    int sig = 0;
+    while (w >= items_end[sig]) ++sig;
+    int64_t local = w - (sig > 0 ? items_end[sig - 1] : 0);
+    const SigIter &it = its[sig];
+    const int c = int(local % kRebinChunks);
+    local /= kRebinChunks;
+    const int r = int(local % it.rows);
+    local /= it.rows;
+    const int t = int(local % it.trials);
+    const int e = int(local / it.trials);
+    // row not listed (a null mask lists every row)
+    if (r > 0 && it.esc_mask != nullptr &&
+        !((it.esc_mask[e] >> ((r - 1) >> 1)) & 1u)) {
+      continue;
+    }
+    const int beta = it.esc_list[e];
+    const int64_t n = it.n;
+    const int64_t B = it.bins;
+    int64_t off = 0;
+    if (r > 0) {
+      const int s = (r - 1) / 2;
+      off = (r & 1) ? (B << s) : -(B << s);
+    }
+    const int64_t tau = int64_t(it.q[t]) + off;
+    const int64_t chunk = (int64_t(it.p) + kRebinChunks - 1) / kRebinChunks;
+    const int64_t c0 = -int64_t(it.p2) + c * chunk;
+    const int64_t c1 = min(c0 + chunk, int64_t(it.p2) + 1);
+    const int64_t per = (chunk + 31) / 32;
+    const int64_t t0 = c0 + lane * per;
+    const int64_t t1 = min(t0 + per, c1);
+    __syncwarp();
+    pw[lane] = it.esc_pow[size_t(e) * kPowLen + lane];
+    pw[lane + 32] = it.esc_pow[size_t(e) * kPowLen + lane + 32];
+    __syncwarp();
+    double tr = 0.0, ti = 0.0;
+    if (t0 < t1) {
+      const int64_t twoB = 2 * B;
+      const int64_t g = 2 * int64_t(beta) + 1;
+      const int64_t u0 = PosMod(tau + t0, n);
+      uint32_t j = uint32_t(PosMod(int64_t(it.a) * u0 + it.c, n));
+      const uint32_t astep = uint32_t(PosMod(it.a, n));
+      const uint32_t nn = uint32_t(n);
+      const int64_t m0 = PosMod(int64_t(it.b) * u0, n);
+      const int64_t r0 = PosMod(g * t0, twoB);
+      double ar, ai;
+      sincospi(2.0 * (double(m0) / double(n) - double(r0) / double(twoB)), &ai, &ar);
+      const double2 S = it.esc_step[e];
+      const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
+      const float2 *__restrict__ wff = it.wtff;
+      for (int64_t tb = t0; tb < t1; tb += kPowLen) {
+        const int len = int(min(int64_t(kPowLen), t1 - tb));
+        FF sr{0.f, 0.f}, si{0.f, 0.f};
+        for (int kb = 0; kb < len; kb += 8) {
+          TX v[8];
+          float2 wv[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            if (kb + u < len) {
+              const int64_t tt = tb + kb + u;
+              v[u] = __ldg(&x[j]);
+              wv[u] = __ldg(&wff[tt < 0 ? -tt : tt]);
+              j += astep;
+              if (j >= nn) j -= nn;
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            if (kb + u < len) {
+              FF xr, xi;
+              SampleTimesWindow(v[u], wv[u], &xr, &xi);
+              const float4 p = pw[kb + u];
+              const FF pr{p.x, p.z}, pi{p.y, p.w};
+              // (xr + i xi)(pr + i pi)
+              AccFF(sr, DotFF(xr, pr, Neg(xi), pi));
+              AccFF(si, DotFF(xr, pi, xi, pr));
+            }
+          }
+        }
+        const double br = double(sr.hi) + double(sr.lo);
+        const double bi = double(si.hi) + double(si.lo);
+        tr += ar * br - ai * bi;
+        ti += ar * bi + ai * br;
+        const double nar = ar * S.x - ai * S.y;
+        ai = ar * S.y + ai * S.x;
+        ar = nar;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      tr += __shfl_xor_sync(0xffffffffu, tr, o);
+      ti += __shfl_xor_sync(0xffffffffu, ti, o);
+    }
+    if (lane == 0) {
+      it.esc_part[((size_t(e) * it.trials + t) * it.rows + r) * kRebinChunks + c] =
+          make_double2(tr, ti);
+    }
+  }
+}
+
+}  // namespace
+
+void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
+                 cudaStream_t s) {
+  // s^k tables of every listed bin, then a persistent grid whose warps stride
+  // over the work items; batches are cut into groups of at most
+  // kRebinMaxSignals signals
+  dim3 pgrid((max_listed + 7) / 8, nsig);
+  k_rebin_prep<<<pgrid, 256, 0, s>>>(d_its);
+  const int blocks = 152 * 2;  // two resident blocks per SM (124 registers)
+  for (int s0 = 0; s0 < nsig; s0 += kRebinMaxSignals) {
+    const int cnt = nsig - s0 < kRebinMaxSignals ? nsig - s0 : kRebinMaxSignals;
+    if (x_c128) {
+      k_rebin_ff<double2><<<blocks, 256, 0, s>>>(d_its + s0, cnt);
+    } else {
+      k_rebin_ff<float2><<<blocks, 256, 0, s>>>(d_its + s0, cnt);
+    }
+  }
+}
+
+}  // namespace mpsft

@@ -58,6 +58,10 @@ __global__ void k_window(const SigIter *__restrict__ its) {
   }
   it.wt64[i] = v;
   it.wt32[i] = float(v);
+  if (it.wtff != nullptr) {
+    const float h = __double2float_rn(v);
+    it.wtff[i] = make_float2(h, __double2float_rn(v - double(h)));
+  }
 }
 
 __device__ inline float2 *ChirpOf(const SigIter &it, float2 *) { return it.chirp32; }

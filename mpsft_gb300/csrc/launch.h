@@ -55,9 +55,12 @@ void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
                   bool fp32, bool subtract_only, cudaStream_t s,
                   bool cond = false);
 
-// FP64 re-binning of the near-tie bins listed by the FP32 decide pass (direct
-// sums over the window support) and their FP64 decisions.
-void LaunchRebin64(const SigIter *d_its, int nsig, bool x_c128, cudaStream_t s);
+// Re-binning of the near-tie bins listed by the FP32 decide pass (direct sums
+// over the window support in float-float arithmetic with FP64 block totals)
+// and their FP64 decisions.
+// max_listed: the largest esc_cap of the signals.
+void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
+                 cudaStream_t s);
 // redo: the conditional FP64 kernels follow (signals whose list overflowed are
 // redone whole); without them such signals are reported unresolved.
 void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
