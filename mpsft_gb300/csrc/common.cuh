@@ -52,6 +52,10 @@ struct SigIter {
   int32_t p, p2, folds;
   int32_t a, b, c, a_inv;
   int32_t phase_shift;  // 32 - log2(n) when n is a power of two, else -1
+  // 64-bit fixed-point constants of the FP32 binning (SetFixedPoint):
+  // n_inv = floor(2^64 / n) (0 when n is a power of two), phi_b = b/n and
+  // psi = 1/(2 bins) in turns, both rounded to 2^-64
+  uint64_t n_inv, phi_b, psi;
   int32_t trials;
   int32_t active;
   int32_t q[kMaxTrials];
@@ -159,6 +163,42 @@ __host__ __device__ inline int64_t PosMod(int64_t v, int64_t n) {
   v %= n;
   return v < 0 ? v + n : v;
 }
+
+// The fixed-point constants of an iteration (n, b and bins set).
+__host__ __device__ inline void SetFixedPoint(SigIter *it) {
+  const uint64_t n = uint64_t(it->n);
+  const bool pow2 = (n & (n - 1)) == 0;
+  it->n_inv = pow2 ? 0 : uint64_t(((unsigned __int128)1 << 64) / n);
+  const uint64_t bm = uint64_t(PosMod(it->b, int64_t(n)));
+  it->phi_b = uint64_t((((unsigned __int128)bm << 64) + n / 2) / n);
+  const uint64_t twoB = 2 * uint64_t(it->bins);
+  it->psi = uint64_t((((unsigned __int128)1 << 64) + twoB / 2) / twoB);
+}
+
+// v mod n (non-negative) for |v| < 2^63 by Barrett reduction with
+// inv = floor(2^64 / n), or a mask when n is a power of two (inv = 0).
+__host__ __device__ __forceinline__ uint64_t MulHi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return uint64_t(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+struct ModN {
+  uint32_t n;
+  uint64_t inv;
+  __host__ __device__ __forceinline__ uint32_t operator()(int64_t v) const {
+    if (inv == 0) return uint32_t(uint64_t(v) & uint64_t(n - 1));
+    const bool neg = v < 0;
+    const uint64_t a = neg ? uint64_t(-v) : uint64_t(v);
+    uint64_t r = a - MulHi64(a, inv) * n;  // r < 3n
+    if (r >= n) r -= n;
+    if (r >= n) r -= n;
+    return uint32_t(neg && r != 0 ? n - r : r);
+  }
+};
+
 
 __device__ inline float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);

@@ -409,6 +409,7 @@ void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
   it->width = w.width;
   it->sigma_f = w.sigma_f;
   it->erf_d = w.erf_d;
+  SetFixedPoint(it);
   it->fft_log2m = FFTLog2(bins);
   it->fft_m = 1 << it->fft_log2m;
 }

@@ -11,14 +11,14 @@
 // phase per t serves both rows (the symmetry of BinInTimeV1/V4,
 // src/binner.cc:116-138), and it lands in bin (-beta) mod B.
 //
-// Work decomposition: one CTA per (32 bins, row group, trial, signal); eight
-// lanes share a bin and split its f = p/B folds (t, t + 8B, ...). Indices
-// step exactly in uint32 (j += a*8B mod n with one conditional subtract), so no
-// 64-bit division runs per sample. FP32: the phase is carried in 32-bit
-// fixed-point turns (exact reduction mod 1 by wrap-around) and converted only
-// for sincospif; products in FP32; the per-lane sums and the 8-lane tree use
-// compensated (TwoSum) addition. FP64: per-sample double phase and sincospi,
-// plain sums (the straightforward port).
+// Work decomposition: one CTA per (bins tile, row group, trial, signal);
+// several lanes share a bin and split its f = p/B folds (t, t + kB, ...).
+// Indices step exactly in uint32 (j += a*kB mod n with one conditional
+// subtract), so no 64-bit division runs per sample. FP32: the phase is carried
+// in fixed-point turns (exact reduction mod 1 by wrap-around) and converted
+// only for sincospif; products in FP32; the per-lane sums and the lane tree
+// use compensated (TwoSum) addition. FP64: per-sample double phase and
+// sincospi, plain sums (the straightforward port).
 #include "common.cuh"
 #include "launch.h"
 
@@ -90,79 +90,90 @@ __device__ inline uint32_t StepDown(uint32_t j, uint32_t d, uint32_t n) {
   return j >= d ? j - d : j + (n - d);
 }
 
+// FP32 fold: one CTA per (64 bins, row group, trial, signal); kFoldSplit
+// threads share a bin and take every kFoldSplit-th fold, kFoldBatch folds of
+// both rows in flight at a time. Setup without divisions: indices by Barrett
+// reduction (or a mask), the phase m/n - t/(2B) as a 64-bit fixed-point
+// product phi_b (t + off) - psi t (wrap-around = exact reduction mod 1,
+// error < 2^-33 turns), rounded to 32-bit turns for sincospif.
+constexpr int kFoldSplit = 4;
+constexpr int kFoldBatch = 4;
+constexpr int kFoldBins = 256 / kFoldSplit;  // bins per CTA
+
 template <typename TX>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_bin_fold32(const SigIter *__restrict__ its, int gmax) {
   const SigIter &it = its[blockIdx.z];
   if (!it.active || it.force_fp64) return;
   const int B = it.bins;
-  if (int(blockIdx.x) * 32 >= B) return;
+  if (int(blockIdx.x) * kFoldBins >= B) return;
   const int g = blockIdx.y % gmax;
   const int tr = blockIdx.y / gmax;
   if (tr >= it.trials || g > it.bits) return;
 
-  const int lane8 = threadIdx.x & (kFoldLanes - 1);
-  const int beta = blockIdx.x * 32 + (threadIdx.x >> 3);
+  const int lane = threadIdx.x & (kFoldSplit - 1);
+  const int beta = blockIdx.x * kFoldBins + threadIdx.x / kFoldSplit;
   const bool valid = beta < B;
   const uint32_t n = uint32_t(it.n);
+  const ModN mod{n, it.n_inv};
   const int64_t off = g == 0 ? 0 : (int64_t(B) << (g - 1));
-  const LaneSetup L = MakeLane(it, beta, lane8, valid, off, it.q[tr]);
-
-  // Phase in 32-bit fixed-point turns: m/n - t/(2B). Exact reduction mod 1 by
-  // uint32 wrap-around; the step adds (m8/n) * 2^32 rounded (error < 2^-32
-  // turns per fold).
-  const uint64_t twoB = 2ull * uint64_t(B);
-  const uint32_t ph_m = uint32_t((uint64_t(L.m) << 32) / n);
-  const uint64_t tmod = uint64_t(PosMod(L.t, int64_t(twoB)));
-  const uint32_t ph_t = uint32_t(((tmod << 32) + twoB / 2) / twoB);
-  const uint32_t dph = uint32_t(((uint64_t(L.m8) << 32) + n / 2) / n);
-  uint32_t ph = ph_m - ph_t;  // lane constant -t/(2B) is unchanged by 8B steps
+  const bool pair = g > 0;
+  // first t of this lane: t = beta mod B with |t| <= p2 (-p2 = (B + 1)/2 mod B
+  // since p = f B with f odd), then every kFoldSplit-th fold
+  int tm = beta - (B + 1) / 2;
+  if (tm < 0) tm += B;
+  int64_t t = -int64_t(it.p2) + tm + int64_t(lane) * B;
+  const int f = it.folds;
+  const int cnt = (valid && f > lane) ? (f - lane + kFoldSplit - 1) / kFoldSplit : 0;
+  const int64_t q = it.q[tr];
+  const int64_t a = it.a, c = it.c;
+  uint32_t j1 = mod(a * mod(q + t + off) + c);
+  uint32_t j2 = mod(a * mod(q - t - off) + c);
+  const int64_t D = int64_t(kFoldSplit) * B;
+  const uint32_t aD = mod(a * mod(D));
+  uint64_t ph = it.phi_b * uint64_t(t + off) - it.psi * uint64_t(t);
+  const uint64_t dph = (it.phi_b - it.psi) * uint64_t(D);
 
   const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
   const float *__restrict__ wt = it.wt32;
-  const bool pair = g > 0;
-
-  TX x1[kMaxFoldsPerLane], x2[kMaxFoldsPerLane];
-  uint32_t phs[kMaxFoldsPerLane];
-  int ta[kMaxFoldsPerLane];
-  {
-    uint32_t j1 = L.j1, j2 = L.j2;
-    int64_t t = L.t;
-#pragma unroll
-    for (int k = 0; k < kMaxFoldsPerLane; ++k) {
-      if (k < L.cnt) {
-        x1[k] = __ldg(&x[j1]);
-        if (pair) x2[k] = __ldg(&x[j2]);
-        phs[k] = ph;
-        ta[k] = int(t < 0 ? -t : t);
-        j1 = StepUp(j1, L.a8, n);
-        j2 = StepDown(j2, L.a8, n);
-        ph += dph;
-        t += int64_t(kFoldLanes) * B;
-      }
-    }
-  }
   CompF r1, i1, r2, i2;
+  for (int k0 = 0; k0 < cnt; k0 += kFoldBatch) {
+    TX x1[kFoldBatch], x2[kFoldBatch];
+    float w[kFoldBatch];
+    uint32_t p32[kFoldBatch];
 #pragma unroll
-  for (int k = 0; k < kMaxFoldsPerLane; ++k) {
-    if (k < L.cnt) {
-      const float phi = float(int32_t(phs[k])) * 2.3283064365386963e-10f;
-      float s, c;
-      sincospif(2.0f * phi, &s, &c);
-      const float w = __ldg(&wt[ta[k]]);
-      const float wr = c * w, wi = s * w;
-      const float2 v1 = to_f2(x1[k]);
-      r1.add(v1.x * wr - v1.y * wi);
-      i1.add(v1.x * wi + v1.y * wr);
-      if (pair) {
-        const float2 v2 = to_f2(x2[k]);
-        r2.add(v2.x * wr + v2.y * wi);
-        i2.add(v2.y * wr - v2.x * wi);
+    for (int u = 0; u < kFoldBatch; ++u) {
+      if (k0 + u < cnt) {
+        x1[u] = __ldg(&x[j1]);
+        if (pair) x2[u] = __ldg(&x[j2]);
+        w[u] = __ldg(&wt[t < 0 ? -t : t]);
+        p32[u] = uint32_t((ph + (uint64_t(1) << 31)) >> 32);
+        j1 = StepUp(j1, aD, n);
+        j2 = StepDown(j2, aD, n);
+        ph += dph;
+        t += D;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kFoldBatch; ++u) {
+      if (k0 + u < cnt) {
+        const float phi = float(int32_t(p32[u])) * 2.3283064365386963e-10f;
+        float s, co;
+        sincospif(2.0f * phi, &s, &co);
+        const float wr = co * w[u], wi = s * w[u];
+        const float2 v1 = to_f2(x1[u]);
+        r1.add(v1.x * wr - v1.y * wi);
+        i1.add(v1.x * wi + v1.y * wr);
+        if (pair) {
+          const float2 v2 = to_f2(x2[u]);
+          r2.add(v2.x * wr + v2.y * wi);
+          i2.add(v2.y * wr - v2.x * wi);
+        }
       }
     }
   }
 #pragma unroll
-  for (int o = 1; o < kFoldLanes; o <<= 1) {
+  for (int o = 1; o < kFoldSplit; o <<= 1) {
     r1.merge(__shfl_xor_sync(0xffffffffu, r1.s, o),
              __shfl_xor_sync(0xffffffffu, r1.c, o));
     i1.merge(__shfl_xor_sync(0xffffffffu, i1.s, o),
@@ -174,7 +185,7 @@ __global__ void __launch_bounds__(256)
                __shfl_xor_sync(0xffffffffu, i2.c, o));
     }
   }
-  if (lane8 == 0 && valid) {
+  if (lane == 0 && valid) {
     float2 *fold = reinterpret_cast<float2 *>(it.fold);
     const size_t base = size_t(tr) * it.rows;
     const int rplus = g == 0 ? 0 : 2 * g - 1;
@@ -271,10 +282,11 @@ void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
       k_bin_fold64<float2><<<grid, 256, 0, s>>>(d_its, gmax, cond ? 1 : 0);
     }
   } else {
+    dim3 grid32((max_bins + kFoldBins - 1) / kFoldBins, gmax * max_trials, nsig);
     if (x_c128) {
-      k_bin_fold32<double2><<<grid, 256, 0, s>>>(d_its, gmax);
+      k_bin_fold32<double2><<<grid32, 256, 0, s>>>(d_its, gmax);
     } else {
-      k_bin_fold32<float2><<<grid, 256, 0, s>>>(d_its, gmax);
+      k_bin_fold32<float2><<<grid32, 256, 0, s>>>(d_its, gmax);
     }
   }
 }

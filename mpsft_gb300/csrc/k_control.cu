@@ -73,6 +73,7 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
   it.c = d[2];
   it.a_inv = d[3];
   it.trials = c.trials;
+  SetFixedPoint(&it);
   for (int t = 0; t < c.trials; ++t) {
     it.q[t] = d[4 + t];
     it.bq_re[t] = bq[2 * t];

@@ -145,6 +145,7 @@ extern "C" int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n,
   it.erf_d = M_SQRT2 * M_PI * sigma_t;
   it.fft_log2m = log2m;
   it.fft_m = 1 << log2m;
+  SetFixedPoint(&it);
   it.wt32 = reinterpret_cast<float *>(base + kOffWt32);
   it.wt64 = reinterpret_cast<double *>(base + kOffWt64);
   it.fold = base + kOffFold;
