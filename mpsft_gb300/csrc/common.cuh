@@ -56,6 +56,16 @@ struct SigIter {
   // n_inv = floor(2^64 / n) (0 when n is a power of two), phi_b = b/n and
   // psi = 1/(2 bins) in turns, both rounded to 2^-64
   uint64_t n_inv, phi_b, psi;
+  // round(2^64 / n) (0 for n = 1): r / n in 64-bit fixed-point turns
+  uint64_t n_fix;
+  // erf_d / (4 n bins) in FP32: the FP32 window response's argument scale
+  float wf_scale;
+  // FP64 unit phases e^{2 pi i r / n} = ph_hi[r >> ph_k] * ph_lo[r & (2^ph_k - 1)]
+  // (built once per call, see PhaseTableK)
+  double2 *ph_lo, *ph_hi;
+  int32_t ph_k;
+  // FP32 copies of the thresholds (the near-tie windows include their rounding)
+  float bin_thr2_f, sv_thr_f;
   int32_t trials;
   int32_t active;
   int32_t q[kMaxTrials];
@@ -89,10 +99,12 @@ struct SigIter {
   // per-slot quantities of the current permutation (k_mode_prep)
   int32_t *mode_bin;    // bin of the slot's mode, -1 for an empty slot
   int32_t *mode_k1;     // (a k0 + b) mod n
-  double *mode_wf;      // window response of the mode in its bin
-  double2 *mode_base;   // [slot * trials + t]: wf * coef * e^{2 pi i (q_t k1 + c k0)/n}
-  double2 *mode_fac;    // [slot * fac_stride + s]: e^{2 pi i (B 2^s k1 mod n)/n}
-  int32_t fac_stride;   // >= bits of every iteration of the call
+  // FP64 path: [slot * trials + t] = wf * coef * e^{2 pi i (q_t k1 + c k0)/n}
+  double2 *mode_base;
+  // FP32 path: the same terms in FP32, and per slot the error the mode
+  // carries into its bin
+  float2 *mode_base32;
+  float *mode_errw;
   // bucketing of table modes by bin
   int32_t *bkt_count;   // bins_cap
   int32_t *bkt_start;   // bins_cap
@@ -173,6 +185,25 @@ __host__ __device__ inline void SetFixedPoint(SigIter *it) {
   it->phi_b = uint64_t((((unsigned __int128)bm << 64) + n / 2) / n);
   const uint64_t twoB = 2 * uint64_t(it->bins);
   it->psi = uint64_t((((unsigned __int128)1 << 64) + twoB / 2) / twoB);
+  it->n_fix = n > 1 ? uint64_t((((unsigned __int128)1 << 64) + n / 2) / n) : 0;
+  it->wf_scale = float(it->erf_d / (4.0 * double(n) * double(it->bins)));
+}
+
+// FP32 copies of an iteration's thresholds (bin_thr, sv_thr set).
+__host__ __device__ inline void SetThresholdCopies(SigIter *it) {
+  it->bin_thr2_f = float(it->bin_thr * it->bin_thr);
+  it->sv_thr_f = float(it->sv_thr);
+}
+
+// Bits of the low table of the FP64 unit phases: ceil(log2 n) / 2 rounded up,
+// so both tables hold about sqrt(n) entries.
+__host__ __device__ inline int PhaseTableK(int64_t n) {
+  int l = 0;
+  while ((int64_t(1) << l) < n) ++l;
+  return (l + 1) / 2;
+}
+__host__ __device__ inline int64_t PhaseTableHi(int64_t n) {
+  return ((n - 1) >> PhaseTableK(n)) + 1;
 }
 
 // v mod n (non-negative) for |v| < 2^63 by Barrett reduction with
@@ -196,6 +227,22 @@ struct ModN {
     if (r >= n) r -= n;
     if (r >= n) r -= n;
     return uint32_t(neg && r != 0 ? n - r : r);
+  }
+  // floor(v / n) for 0 <= v < 2^63
+  __host__ __device__ __forceinline__ uint64_t quot(int64_t v) const {
+    const uint64_t a = uint64_t(v);
+    if (inv == 0) {
+#ifdef __CUDA_ARCH__
+      return a >> (__ffs(int(n)) - 1);
+#else
+      return a >> __builtin_ctz(n);
+#endif
+    }
+    uint64_t q = MulHi64(a, inv);  // q <= floor(a / n) <= q + 2
+    uint64_t r = a - q * n;
+    if (r >= n) { r -= n; ++q; }
+    if (r >= n) { ++q; }
+    return q;
   }
 };
 
@@ -236,6 +283,26 @@ __device__ inline float2 UnitPhase32(int64_t m, int64_t n, int shift) {
     const uint64_t r = uint64_t(PosMod(m, n));
     ph = uint32_t((r << 32) / uint64_t(n));
   }
+  float s, c;
+  sincospif(2.0f * (float(int32_t(ph)) * 2.3283064365386963e-10f), &s, &c);
+  return make_float2(c, s);
+}
+
+// e^{2 pi i m / n} from the phase tables (two FP64 table entries and one
+// complex product: about 2.5 ulp), m any integer with |m| < 2^63.
+__device__ inline double2 Phase64(const SigIter &it, int64_t m) {
+  const uint32_t r = ModN{uint32_t(it.n), it.n_inv}(m);
+  const double2 h = it.ph_hi[r >> it.ph_k];
+  const double2 l = it.ph_lo[r & ((1u << it.ph_k) - 1u)];
+  return cmul(h, l);
+}
+
+// e^{2 pi i m / n} in FP32: r = m mod n as 32-bit fixed-point turns
+// round(r 2^32 / n) (error below 2^-33 turns), whose signed value is the angle
+// reduced to [-1/2, 1/2) turns.
+__device__ inline float2 Phase32(const SigIter &it, int64_t m) {
+  const uint64_t r = ModN{uint32_t(it.n), it.n_inv}(m);
+  const uint32_t ph = uint32_t((r * it.n_fix + (uint64_t(1) << 31)) >> 32);
   float s, c;
   sincospif(2.0f * (float(int32_t(ph)) * 2.3283064365386963e-10f), &s, &c);
   return make_float2(c, s);

@@ -309,10 +309,15 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->eps_dev = cv.take<float>(1);
   it->mode_bin = cv.take<int32_t>(s.tab_cap);
   it->mode_k1 = cv.take<int32_t>(s.tab_cap);
-  it->mode_wf = cv.take<double>(s.tab_cap);
+
   it->mode_base = cv.take<double2>(size_t(s.tab_cap) * s.trials);
-  it->fac_stride = std::max(1, (s.rows_cap - 1) / 2);
-  it->mode_fac = cv.take<double2>(size_t(s.tab_cap) * it->fac_stride);
+
+  it->mode_base32 = cv.take<float2>(size_t(s.tab_cap) * s.trials);
+
+  it->mode_errw = cv.take<float>(s.tab_cap);
+  it->ph_k = PhaseTableK(s.n);
+  it->ph_lo = cv.take<double2>(size_t(1) << it->ph_k);
+  it->ph_hi = cv.take<double2>(size_t(PhaseTableHi(s.n)));
   it->bkt_count = cv.take<int32_t>(s.bins_cap);
   it->bkt_start = cv.take<int32_t>(s.bins_cap);
   it->bkt_list = cv.take<int32_t>(s.tab_cap);
@@ -509,7 +514,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
   LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
-  LaunchModePrep(d_its, nsig, mx.cap, mx.bits, ctx->side);
+  LaunchModePrep(d_its, nsig, mx.cap, ctx->side);
   LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
   LaunchWindow(d_its, nsig, mx.p2, s);
@@ -526,7 +531,8 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
   LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s);
-  if (launched) *launched += 9;
+  // Bluestein setup, mode preparation, bucketing, window, fold, FFT, decide
+  if (launched) *launched += 7;
   if (!fp64) {
     // near ties of the FP32 pass: listed bins re-binned and re-decided in
     // FP64; signals that the precision policy sends to FP64 (and signals
@@ -534,7 +540,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     const bool redo = any_forced && mx.m <= kMaxFFT64;
     LaunchRebin(d_its, nsig, kMaxListed, x_c128, s);
     LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
-    if (launched) *launched += 2;
+    if (launched) *launched += 3;  // power tables, re-binning, decisions
     if (redo) {
       LaunchBluesteinSetup(d_its, nsig, mx.m, true, ctx->tw32, ctx->tw64, s, true);
       LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, true, s,
@@ -909,13 +915,20 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
+  int64_t phase_entries = 1;
   for (int i = 0; i < nsig; ++i) {
     std::memset(&its[i], 0, sizeof(SigIter));
     CarveSignal(cv, shapes[i], &its[i], &ctls[i]);
     its[i].x_energy = d_energy + size_t(kEnergyStride) * i;
+    its[i].n = int32_t(sigs[i]->n);
+    phase_entries = std::max(phase_entries, PhaseTableEntries(sigs[i]->n));
     rc = ClearTable(ctx, its[i], ctls[i]);
     if (rc) return rc;
   }
+  // FP64 unit-phase tables (per signal length, for the whole call)
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  LaunchPhaseTables(d_its, nsig, phase_entries, ctx->stream);
   std::vector<double> energy(nsig, 0.0);
   if (!fp64) {
     // mean |x|^2 of every signal scales the FP32 near-tie margin
@@ -1002,6 +1015,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       FillIter(&it, sigs[i], bins, bits, o.window_delta, tf, q, o.trials);
       it.bin_thr = 3.0 * o.sigma / std::sqrt(double(bins));
       it.sv_thr = 1.0 * o.sigma / std::sqrt(double(bins));
+      SetThresholdCopies(&it);
       it.win_thr = o.window_threshold;
       SetNearTie(&it, fp64, o.near_tie_margin, bins, force[i] != 0);
       run[i].fp64_iters += it.force_fp64;
@@ -1500,6 +1514,7 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   cudaStream_t st = ctx->stream;
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   st));
+  LaunchPhaseTables(d_it, 1, PhaseTableEntries(n), st);
   rc = ClearTable(ctx, it, ctl);
   if (rc) return rc;
   if (m > 0) {
@@ -1513,7 +1528,7 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(it.ubuf, sizeof(double2) * it.bins_cap,
                                     inout, row_bytes, row_bytes, it.rows,
                                     cudaMemcpyHostToDevice, st));
-  LaunchModePrep(d_it, 1, s.tab_cap, bits, st);
+  LaunchModePrep(d_it, 1, s.tab_cap, st);
   LaunchBucket(d_it, 1, bins, s.tab_cap, st);
   LaunchDecide(d_it, 1, bins, 1, false, true, st);
   MPSFT_CUDA(ctx, cudaGetLastError());
@@ -1617,6 +1632,7 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
   FillIter(&it, sig, bins, bits, opt->window_delta, tf, q, opt->trials);
   it.bin_thr = opt->bin_threshold;
   it.sv_thr = opt->sv_threshold;
+  SetThresholdCopies(&it);
   it.win_thr = opt->window_threshold;
   it.x_energy = d_energy;
   cudaStream_t st = ctx->stream;
@@ -1637,6 +1653,7 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
                                        opt->bin_threshold, opt->sv_threshold));
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   st));
+  LaunchPhaseTables(d_it, 1, PhaseTableEntries(n), st);
   rc = ClearTable(ctx, it, ctl);
   if (rc) return rc;
   if (m0 > 0) {

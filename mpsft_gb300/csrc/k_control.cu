@@ -82,6 +82,7 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
   const double rb = __dsqrt_rn(B);
   it.bin_thr = __ddiv_rn(__dmul_rn(3.0, c.sigma), rb);
   it.sv_thr = __ddiv_rn(c.sigma, rb);
+  SetThresholdCopies(&it);
   it.win_thr = c.win_thr;
   int l = 0;
   while ((1 << l) < 2 * bins - 1) ++l;

@@ -30,8 +30,22 @@ namespace mpsft {
 namespace {
 
 // ---------------------------------------------------------------- prep
-// One thread per occupied slot (the table's insertion list), so FP64 work
-// runs on full warps.
+// One thread per occupied slot (the table's insertion list): k1 = (a k0 + b)
+// mod n and the mode's bin for the bucketing, and the row-0 term
+// wf c e^{2 pi i (q_t k1 + c k0)/n} of every trial (BinInFreqV1::Run,
+// src/binner.cc:565-591). The FP64 path evaluates the terms in FP64 (unit
+// phases from the FP64 tables); the FP32 path in FP32 only, together with the
+// error the mode carries into its bin: the coefficient's bound tab_err |wf|
+// plus 8 eps_rel |wf c| for the FP32 window response, phase, rounding and
+// subtraction (each a few 2^-24 relative).
+__device__ inline float WindowInFreq32(const SigIter &it, int64_t k1, int bin) {
+  // xi +- 1/(4B) with xi = (bin + 1/2)/B - k1/n, as exact integers over 4nB
+  const int64_t n = it.n, B4 = 4 * int64_t(it.bins);
+  const int64_t np = (4 * int64_t(bin) + 3) * n - k1 * B4;
+  const int64_t nm = (4 * int64_t(bin) + 1) * n - k1 * B4;
+  return 0.5f * (erff(float(np) * it.wf_scale) - erff(float(nm) * it.wf_scale));
+}
+
 __global__ void k_mode_prep(const SigIter *__restrict__ its) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
@@ -41,34 +55,29 @@ __global__ void k_mode_prep(const SigIter *__restrict__ its) {
   const int32_t key = it.tab_key[s];
   const int64_t n = it.n;
   const int B = it.bins;
-  const int64_t k1 = PosMod(int64_t(it.a) * key + it.b, n);
-  const int bin = int(k1 * B / n);
-  const double xi = (double(bin) + 0.5) / double(B) - double(k1) / double(n);
-  const double wf = WindowInFreq(it, xi);
-  const double2 wc = cscale(it.tab_coef[s], wf);
-  for (int t = 0; t < it.trials; ++t) {
-    const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
-    it.mode_base[size_t(s) * it.trials + t] = cmul(wc, UnitPhase64(ph, n));
-  }
+  const ModN mod{uint32_t(n), it.n_inv};
+  const int64_t k1 = mod(int64_t(it.a) * key + it.b);
+  const int bin = int(mod.quot(k1 * B));
   it.mode_k1[s] = int32_t(k1);
-  it.mode_wf[s] = wf;
   it.mode_bin[s] = bin;
-}
-
-// Row factors of every found mode: e^{2 pi i (B 2^s k1 mod n)/n} for each bit
-// s (the factor BinInFreqV1 applies to rows 2s+1 / 2s+2, src/binner.cc:584-589),
-// one thread per (occupied slot, bit).
-__global__ void k_mode_fac(const SigIter *__restrict__ its) {
-  const SigIter &it = its[blockIdx.y];
-  if (!it.active || it.bits <= 0) return;
-  const int L = it.bits;
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int i = int(idx / L), s = int(idx % L);
-  if (i >= *it.tab_count) return;
-  const int sl = it.occ_list[i];
-  const int64_t off = int64_t(it.bins) << s;
-  it.mode_fac[size_t(sl) * it.fac_stride + s] =
-      UnitPhase64(off * int64_t(it.mode_k1[sl]), it.n);
+  if (it.eps_rel > 0.f) {
+    const float wf = WindowInFreq32(it, k1, bin);
+    const double2 cd = it.tab_coef[s];
+    const float2 wc = make_float2(float(cd.x) * wf, float(cd.y) * wf);
+    for (int t = 0; t < it.trials; ++t) {
+      const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
+      it.mode_base32[size_t(s) * it.trials + t] = cmulf(wc, Phase32(it, ph));
+    }
+    it.mode_errw[s] = float(it.tab_err[s]) * fabsf(wf) +
+                      8.f * it.eps_rel * sqrtf(wc.x * wc.x + wc.y * wc.y);
+  } else {
+    const double xi = (double(bin) + 0.5) / double(B) - double(k1) / double(n);
+    const double2 wc = cscale(it.tab_coef[s], WindowInFreq(it, xi));
+    for (int t = 0; t < it.trials; ++t) {
+      const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
+      it.mode_base[size_t(s) * it.trials + t] = cmul(wc, Phase64(it, ph));
+    }
+  }
 }
 
 // Sorts the occupied slots by (bin, k0): one 64-bit key per slot,
@@ -141,20 +150,44 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
 template <typename T> struct Ops;
 template <> struct Ops<float> {
   using V = float2;
-  __device__ static V load(const double2 &d) {
-    return make_float2(float(d.x), float(d.y));
-  }
   __device__ static V from(double2 d) { return make_float2(float(d.x), float(d.y)); }
-  __device__ static V phase(int64_t m, int64_t n, int shift) {
-    return UnitPhase32(m, n, shift);
+  __device__ static V phase(const SigIter &it, int64_t m) { return Phase32(it, m); }
+  // row-0 terms of a found mode, from k_mode_prep's FP32 copies
+  template <int TMAX>
+  __device__ static void terms(const SigIter &it, int sl, V *out) {
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < it.trials) out[t] = it.mode_base32[size_t(sl) * it.trials + t];
+    }
   }
 };
 template <> struct Ops<double> {
   using V = double2;
-  __device__ static V load(const double2 &d) { return d; }
   __device__ static V from(double2 d) { return d; }
-  __device__ static V phase(int64_t m, int64_t n, int) {
-    return UnitPhase64(m, n);
+  __device__ static V phase(const SigIter &it, int64_t m) { return Phase64(it, m); }
+  // row-0 terms of a found mode: the FP64 path's k_mode_prep values, or, on
+  // the FP32 path (near-tie bins and bins redone in FP64), evaluated here in
+  // FP64
+  template <int TMAX>
+  __device__ static void terms(const SigIter &it, int sl, V *out) {
+    if (it.eps_rel == 0.f) {
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < it.trials) out[t] = it.mode_base[size_t(sl) * it.trials + t];
+      }
+      return;
+    }
+    const int64_t n = it.n, k1 = it.mode_k1[sl];
+    const int32_t key = it.tab_key[sl];
+    const double xi = (double(it.mode_bin[sl]) + 0.5) / double(it.bins) -
+                      double(k1) / double(n);
+    const double2 wc = cscale(it.tab_coef[sl], WindowInFreq(it, xi));
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < it.trials) {
+        out[t] = cmul(wc, Phase64(it, int64_t(it.q[t]) * k1 + int64_t(it.c) * key));
+      }
+    }
   }
 };
 
@@ -230,6 +263,33 @@ enum DecideMode { kDecide = 0, kSubtractOnly = 1, kDecideExact = 2 };
 // The bin loop body of Iterate for one bin (warp-wide). T = float: the FP32
 // path with near-tie detection; T = double: FP64 decisions (the FP64 path, and
 // the near-tie bins after their FP64 re-binning).
+// k1 = round(n (beta + xi1) / B) with xi1 = (2 xs + 1) / 2^{L+1}, exactly in
+// integers: num = n (beta 2^{L+1} + 2 xs + 1) < 2^64, den = B 2^{L+1} < 2^33
+// (B 2^{L-1} <= n by the definition of L). The reference evaluates this in
+// FP64 (relative error below 2^-52, so at most 2^-21 absolute); when the
+// exact value lies within 2^-18 of a half-integer, that FP64 evaluation is
+// used instead so that the rounding is the reference's.
+__device__ inline int64_t RoundK1(int64_t n, int beta, uint32_t xs, int L, int B) {
+  const uint64_t den = uint64_t(B) << (L + 1);
+  const uint64_t num =
+      uint64_t(n) * ((uint64_t(beta) << (L + 1)) + 2 * uint64_t(xs) + 1);
+  const uint64_t q = num / den;
+  const uint64_t r = num - q * den;
+  const uint64_t d = 2 * r > den ? 2 * r - den : den - 2 * r;  // 2 den |frac - 1/2|
+  if (d <= (den >> 17)) {
+    const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
+    return int64_t(round(double(n) * (double(beta) + xi1) / double(B)));
+  }
+  return int64_t(q) + (2 * r >= den ? 1 : 0);
+}
+
+// The bin loop body of Iterate for one bin (warp-wide). T = float: the FP32
+// path with near-tie detection, FP32 arithmetic only (GB300 runs FP64 at a
+// small fraction of its FP32 rate): a surviving bin leaves a pending
+// candidate (cand_valid = 2: k1 in cand_k0, the unscaled coefficient sum in
+// cand_coef, its error bound in cand_err) that the merge finishes in FP64 on
+// full warps. T = double: FP64 decisions to the end (the FP64 path, and the
+// near-tie bins after their re-binning).
 template <typename T, int TMAX, typename Src>
 __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
                           int mode) {
@@ -253,18 +313,15 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
     if (t < TR) u0[t] = O::from(src.get(t, 0));
   }
   const int npre = min(nm, 32);
-  double2 pre_base[TMAX];
-  double mode_err = 0;  // FP32 error carried into this bin by the found modes
+  V pre_base[TMAX];
+  float mode_err = 0.f;  // FP32 error carried into this bin by the found modes
   if (lane < npre) {
     const int sl = it.bkt_list[st + lane];
-#pragma unroll
-    for (int t = 0; t < TMAX; ++t) {
-      if (t < TR) pre_base[t] = it.mode_base[size_t(sl) * TR + t];
-    }
-    if (fp32) mode_err = it.tab_err[sl] * fabs(it.mode_wf[sl]);
+    O::template terms<TMAX>(it, sl, pre_base);
+    if (fp32) mode_err = it.mode_errw[sl];
   }
   for (int i = 0; i < nm; ++i) {
-    double2 bs[TMAX];
+    V bs[TMAX];
     if (i < 32) {
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
@@ -275,15 +332,12 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
       }
     } else {
       const int sl = it.bkt_list[st + i];
-#pragma unroll
-      for (int t = 0; t < TMAX; ++t) {
-        if (t < TR) bs[t] = it.mode_base[size_t(sl) * TR + t];
-      }
-      if (fp32 && lane == 0) mode_err += it.tab_err[sl] * fabs(it.mode_wf[sl]);
+      O::template terms<TMAX>(it, sl, bs);
+      if (fp32 && lane == 0) mode_err += it.mode_errw[sl];
     }
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
-      if (t < TR) u0[t] = vsub2(u0[t], O::from(bs[t]));
+      if (t < TR) u0[t] = vsub2(u0[t], bs[t]);
     }
   }
   if (fp32) {
@@ -293,7 +347,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   // FP32 error bound of this lane's values (see kEpsRms and friends)
   float eps_base = 0.f, rm0 = 0.f, rml = 0.f;
   if (fp32) {
-    eps_base = *it.eps_dev + float(mode_err);
+    eps_base = *it.eps_dev + mode_err;
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) {
@@ -325,13 +379,17 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
       }
       return;
     }
-    if (it.bin_thr > 0) {
-      const T thr2 = T(it.bin_thr * it.bin_thr);
+    if (fp32 ? it.bin_thr2_f > 0.f : it.bin_thr > 0) {
+      T thr2;
       if (fp32) {
+        thr2 = it.bin_thr2_f;
         const T eps0 = T(eps_base + it.eps_rel * (kEpsRowMax * rm0 +
                                                   kEpsValue * float(amax)));
-        // |d e| <= 2 max|u0| eps + eps^2
-        e_near = fabs(e - thr2) <= T(2) * amax * eps0 + eps0 * eps0;
+        // |d e| <= 2 max|u0| eps + eps^2, plus the threshold's FP32 rounding
+        e_near = fabs(e - thr2) <= T(2) * amax * eps0 + eps0 * eps0 +
+                                       thr2 * T(1.2e-7);
+      } else {
+        thr2 = T(it.bin_thr * it.bin_thr);
       }
       if (e < thr2) {
         if (e_near && lane == 0) Flag(it, beta, 0u);
@@ -356,7 +414,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   }
   const int64_t off = has_bit ? (int64_t(B) << lane) : 0;
   for (int i = 0; i < nm; ++i) {
-    double2 bs[TMAX];
+    V bs[TMAX];
     if (i < 32) {
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
@@ -367,20 +425,18 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
       }
     } else {
       const int sl = it.bkt_list[st + i];
-#pragma unroll
-      for (int t = 0; t < TMAX; ++t) {
-        if (t < TR) bs[t] = it.mode_base[size_t(sl) * TR + t];
-      }
+      O::template terms<TMAX>(it, sl, bs);
     }
     if (has_bit) {
+      // row factor e^{2 pi i (B 2^s k1 mod n)/n} of this lane's bit
+      // (src/binner.cc:584-589)
       const int sl = it.bkt_list[st + i];
-      const V fac = O::from(it.mode_fac[size_t(sl) * it.fac_stride + lane]);
+      const V fac = O::phase(it, off * int64_t(it.mode_k1[sl]));
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
         if (t < TR) {
-          const V b = O::from(bs[t]);
-          up[t] = vsub2(up[t], vmul2(b, fac));
-          um[t] = vsub2(um[t], vmul2(b, vconj2(fac)));
+          up[t] = vsub2(up[t], vmul2(bs[t], fac));
+          um[t] = vsub2(um[t], vmul2(bs[t], vconj2(fac)));
         }
       }
     }
@@ -421,7 +477,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   int count = 0;
   bool sv_fail = false, near = false;
   if (has_bit) {
-    const T sv_thr = T(it.sv_thr);
+    const T sv_thr = fp32 ? T(it.sv_thr_f) : T(it.sv_thr);
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) {
@@ -434,9 +490,12 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
           const T eps = T(eps_base + it.eps_rel * (kEpsRowMax * rml +
                                                    kEpsValue * float(max(a0, max(a1, a2)))));
           // |d Im(m01)| <= eps (2|u0| + |u1| + |u2|) + 4 eps^2;
-          // |d sigma1| <= ||dA||_2 <= 2 eps.
+          // |d sigma1| <= ||dA||_2 <= 2 eps, plus the threshold's rounding.
           if (fabs(im) <= eps * (T(2) * a0 + a1 + a2) + T(4) * eps * eps) near = true;
-          if (sv_thr > T(0) && fabs(s1 * T(0.5) - sv_thr) <= eps) near = true;
+          if (sv_thr > T(0) &&
+              fabs(s1 * T(0.5) - sv_thr) <= eps + sv_thr * T(1.2e-7)) {
+            near = true;
+          }
         }
       }
     }
@@ -452,14 +511,19 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   const uint32_t mask = __ballot_sync(0xffffffffu, has_bit && count > TR / 2);
   // bit 0 is the most significant digit of xi
   const uint32_t xs = L > 0 ? (__brev(mask) >> (32 - L)) : 0u;
-  const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
-  const int32_t k1 =
-      int32_t(round(double(n) * (double(beta) + xi1) / double(B)));
-  const double xi0 = double(k1) / double(n) - (double(beta) + 0.5) / double(B);
-  const double wf = WindowInFreq(it, xi0);
-  if (fabs(wf) < it.win_thr) {
-    NoCandidate(it, beta, lane);
-    return;
+  int64_t k1;
+  double wf = 0.0;
+  if (fp32) {
+    k1 = RoundK1(n, beta, xs, L, B);
+  } else {
+    const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
+    k1 = int64_t(round(double(n) * (double(beta) + xi1) / double(B)));
+    const double xi0 = double(k1) / double(n) - (double(beta) + 0.5) / double(B);
+    wf = WindowInFreq(it, xi0);
+    if (fabs(wf) < it.win_thr) {
+      NoCandidate(it, beta, lane);
+      return;
+    }
   }
 
   // ---- coefficient (src/iterate.cc:146-171)
@@ -469,7 +533,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
     V mine;
     mine.x = T(1);
     mine.y = T(0);
-    if (lane < TR) mine = O::phase(-int64_t(it.q[lane]) * k1, n, it.phase_shift);
+    if (lane < TR) mine = O::phase(it, -int64_t(it.q[lane]) * k1);
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) {
@@ -483,7 +547,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   V fac2;
   fac2.x = T(1);
   fac2.y = T(0);
-  if (has_bit) fac2 = O::phase(-off * k1, n, it.phase_shift);
+  if (has_bit) fac2 = O::phase(it, -off * k1);
 #pragma unroll
   for (int t = 0; t < TMAX; ++t) {
     if (t < TR) {
@@ -500,16 +564,16 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
       }
     }
   }
-  double ax = acc.x, ay = acc.y;
+  T ax = acc.x, ay = acc.y;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     ax += __shfl_xor_sync(0xffffffffu, ax, o);
     ay += __shfl_xor_sync(0xffffffffu, ay, o);
   }
-  // the coefficient's FP32 error: every averaged value carries at most the
-  // bound of the rows involved
-  float eps_c = 0.f;
   if (fp32) {
+    // the coefficient's FP32 error: every averaged value carries at most the
+    // bound of the rows involved (the FP32 sums and phases add a few ulp of
+    // the largest value, inside the kEpsValue share)
     T amax = 0;
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
@@ -518,21 +582,49 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
                              max(vabs2<T, V>(up[t]), vabs2<T, V>(um[t]))));
       }
     }
-    eps_c = eps_base + it.eps_rel * (kEpsRowMax * rml + kEpsValue * float(amax));
+    float eps_c = eps_base + it.eps_rel * (kEpsRowMax * rml + kEpsValue * float(amax));
     for (int o = 16; o > 0; o >>= 1) {
       eps_c = fmaxf(eps_c, __shfl_xor_sync(0xffffffffu, eps_c, o));
     }
+    if (lane == 0) {
+      it.cand_k0[beta] = int32_t(k1);
+      it.cand_coef[beta] = make_double2(double(ax), double(ay));
+      it.cand_err[beta] = double(eps_c);
+      it.cand_valid[beta] = 2;
+    }
+    return;
+  }
+  // near-tie bins of the FP32 path: the rows that were not re-binned carry
+  // the FP32 binning bound into the coefficient
+  double err = 0.0;
+  if (it.eps_rel > 0.f) {
+    float rm = 0.f, am = 0.f;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        const float *r = it.row_max + size_t(t) * rows;
+        rm = fmaxf(rm, r[0]);
+        am = fmaxf(am, float(vabs2<T, V>(u0[t])));
+        if (has_bit) {
+          rm = fmaxf(rm, fmaxf(r[2 * lane + 1], r[2 * lane + 2]));
+          am = fmaxf(am, float(max(vabs2<T, V>(up[t]), vabs2<T, V>(um[t]))));
+        }
+      }
+    }
+    float e = *it.eps_dev + it.eps_rel * (kEpsRowMax * rm + kEpsValue * am);
+    for (int o = 16; o > 0; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+    err = double(e) / fabs(wf);
   }
   if (lane == 0) {
-    double2 coef = make_double2(ax / double(TR * (1 + 2 * L)),
-                                ay / double(TR * (1 + 2 * L)));
-    const int32_t k0 =
-        int32_t(PosMod(int64_t(it.a_inv) * (int64_t(k1) - it.b), n));
-    coef = cmul(coef, UnitPhase64(-int64_t(it.c) * k0, n));
+    double2 coef = make_double2(double(ax) / double(TR * (1 + 2 * L)),
+                                double(ay) / double(TR * (1 + 2 * L)));
+    const ModN mod{uint32_t(n), it.n_inv};
+    const int32_t k0 = int32_t(mod(int64_t(it.a_inv) * mod(k1 - it.b)));
+    coef = cmul(coef, Phase64(it, -int64_t(it.c) * k0));
     coef = make_double2(coef.x / wf, coef.y / wf);
     it.cand_k0[beta] = k0;
     it.cand_coef[beta] = coef;
-    it.cand_err[beta] = fp32 ? double(eps_c) / fabs(wf) : 0.0;
+    it.cand_err[beta] = err;
     it.cand_valid[beta] = 1;
     it.flags[0] = 1;
   }
@@ -595,12 +687,44 @@ __device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef,
   atomicOr(&it.flags[1], kStatusCapacity);
 }
 
+// Candidates -> table. Pending FP32 candidates are finished here in FP64 on
+// full warps (src/iterate.cc:139-171): the window response at
+// xi0 = k1/n - (beta + 1/2)/B and its threshold, the average over the
+// T (1 + 2L) values, k0 = a^-1 (k1 - b) mod n, the factor e^{-2 pi i c k0/n}
+// and the division by the window response.
 __global__ void k_merge(const SigIter *__restrict__ its) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   const int beta = blockIdx.x * blockDim.x + threadIdx.x;
-  if (beta >= it.bins || !it.cand_valid[beta]) return;
-  InsertMode(it, it.cand_k0[beta], it.cand_coef[beta], it.cand_err[beta]);
+  if (beta >= it.bins) return;
+  const int v = it.cand_valid[beta];
+  if (!v) return;
+  int32_t k0 = it.cand_k0[beta];
+  double2 coef = it.cand_coef[beta];
+  double err = it.cand_err[beta];
+  if (v == 2) {
+    const int64_t n = it.n, k1 = k0;
+    const int B = it.bins;
+    const double xi0 = double(k1) / double(n) - (double(beta) + 0.5) / double(B);
+    const double wf = WindowInFreq(it, xi0);
+    if (fabs(wf) < it.win_thr) {
+      it.cand_valid[beta] = 0;
+      return;
+    }
+    const double m = double(it.trials * (1 + 2 * it.bits));
+    coef = make_double2(coef.x / m, coef.y / m);
+    const ModN mod{uint32_t(n), it.n_inv};
+    k0 = int32_t(mod(int64_t(it.a_inv) * mod(k1 - it.b)));
+    coef = cmul(coef, Phase64(it, -int64_t(it.c) * k0));
+    coef = make_double2(coef.x / wf, coef.y / wf);
+    err = err / fabs(wf);
+    it.cand_k0[beta] = k0;
+    it.cand_coef[beta] = coef;
+    it.cand_err[beta] = err;
+    it.cand_valid[beta] = 1;
+  }
+  it.flags[0] = 1;
+  InsertMode(it, k0, coef, err);
 }
 
 __global__ void k_table_insert(const SigIter *__restrict__ it,
@@ -642,16 +766,11 @@ void LaunchDecideP(const SigIter *d_its, int nsig, int max_bins, int max_trials,
 
 }  // namespace
 
-void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, int max_bits,
-                    cudaStream_t s) {
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s) {
   // the occupied count is only known on the device: cover the whole table,
   // blocks past the count exit at once
   dim3 grid((max_cap + 255) / 256, nsig);
   k_mode_prep<<<grid, 256, 0, s>>>(d_its);
-  if (max_bits > 0) {
-    dim3 grid2(unsigned((int64_t(max_cap) * max_bits + 255) / 256), nsig);
-    k_mode_fac<<<grid2, 256, 0, s>>>(d_its);
-  }
 }
 
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,

@@ -64,6 +64,23 @@ __global__ void k_window(const SigIter *__restrict__ its) {
   }
 }
 
+// ph_lo[l] = e^{2 pi i l / n} for l < 2^ph_k and ph_hi[h] = e^{2 pi i h 2^ph_k / n}
+// for h <= (n - 1) >> ph_k, from exact integer phases.
+__global__ void k_phase_tables(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  const int64_t n = it.n;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  double s, c;
+  if (i < (int64_t(1) << it.ph_k)) {
+    sincospi(2.0 * (double(i) / double(n)), &s, &c);
+    it.ph_lo[i] = make_double2(c, s);
+  }
+  if (i <= ((n - 1) >> it.ph_k)) {
+    sincospi(2.0 * (double(i << it.ph_k) / double(n)), &s, &c);
+    it.ph_hi[i] = make_double2(c, s);
+  }
+}
+
 __device__ inline float2 *ChirpOf(const SigIter &it, float2 *) { return it.chirp32; }
 __device__ inline double2 *ChirpOf(const SigIter &it, double2 *) { return it.chirp64; }
 __device__ inline float2 *ChatOf(const SigIter &it, float2 *) { return it.chat32; }
@@ -106,6 +123,12 @@ __global__ void k_bluestein_setup(const SigIter *__restrict__ its,
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s) {
   const int n = kMaxFFT / 2;
   k_twiddles<<<(n + 255) / 256, 256, 0, s>>>(tw32, tw64);
+}
+
+void LaunchPhaseTables(const SigIter *d_its, int nsig, int64_t entries,
+                       cudaStream_t s) {
+  dim3 grid(unsigned((entries + 255) / 256), nsig);
+  k_phase_tables<<<grid, 256, 0, s>>>(d_its);
 }
 
 void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {

@@ -10,6 +10,16 @@ namespace mpsft {
 // e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2, for the FFT twiddles.
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s);
 
+// FP64 unit-phase tables ph_lo / ph_hi of every signal (n and the table
+// pointers set); entries = the largest table length of the signals.
+void LaunchPhaseTables(const SigIter *d_its, int nsig, int64_t entries,
+                       cudaStream_t s);
+inline int64_t PhaseTableEntries(int64_t n) {
+  const int64_t lo = int64_t(1) << PhaseTableK(n);
+  const int64_t hi = PhaseTableHi(n);
+  return lo > hi ? lo : hi;
+}
+
 // Window tables wt32 / wt64 at |t| in [0, p2] of every active signal.
 void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s);
 
@@ -33,8 +43,7 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
                   const double2 *tw64, cudaStream_t s, bool cond = false);
 
 // Per found mode: k1, bin, window response and the per-trial row-0 term.
-void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, int max_bits,
-                    cudaStream_t s);
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s);
 
 // mean |x|^2 of each signal into energy[sig * kEnergyStride] (two
 // deterministic passes).
