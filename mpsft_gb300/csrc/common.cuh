@@ -29,6 +29,8 @@ constexpr int kRebinChunks = 16;   // FP64 re-binning: chunks of the support
 constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
 constexpr int kRebinMaxSignals = 256;  // signals per FP64 re-binning launch
 
+constexpr int kCtlWords = 4;  // found flag, status bits, near ties, mode count
+
 // Per-signal status bits written by the device.
 enum : int32_t {
   kStatusCapacity = 1,   // mode table full

@@ -52,6 +52,9 @@ struct mpsft_ctx {
   // pinned host staging for per-iteration control words
   int32_t *h_ctl = nullptr;
   size_t h_ctl_n = 0;
+  // pinned staging of exported mode tables
+  unsigned char *h_stage = nullptr;
+  size_t h_stage_n = 0;
   std::vector<cudaEvent_t> events;
 };
 
@@ -71,7 +74,6 @@ struct mpsft_rng {
 
 namespace {
 
-constexpr int kCtlWords = 4;  // found flag, status bits, near ties, mode count
 // FP32 near-tie margin: the safety factor on the FP32 error model of the bins
 // (kEpsRms, kEpsRowMax, kEpsValue in units of 2^-24; the rms of the bins is
 // estimated as sqrt(mean|x|^2 / (2 bins))).
@@ -364,6 +366,16 @@ int EnsureHostCtl(mpsft_ctx *ctx, size_t words) {
   ctx->h_ctl = nullptr;
   MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_ctl, words * sizeof(int32_t)));
   ctx->h_ctl_n = words;
+  return MPSFT_OK;
+}
+
+int EnsureHostStage(mpsft_ctx *ctx, size_t bytes) {
+  if (ctx->h_stage_n >= bytes) return MPSFT_OK;
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  ctx->h_stage = nullptr;
+  ctx->h_stage_n = 0;
+  MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_stage, bytes));
+  ctx->h_stage_n = bytes;
   return MPSFT_OK;
 }
 
@@ -900,6 +912,11 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   bytes += (sizeof(SolveCtl) +
             sizeof(int32_t) * kDrawChunk * (4 + max_trials_all) +
             sizeof(double) * kDrawChunk * max_trials_all * 2) * nsig + 2048;
+  int max_cap = 1;
+  for (int i = 0; i < nsig; ++i) max_cap = std::max(max_cap, shapes[i].tab_cap);
+  // table export staging
+  bytes += (sizeof(int32_t) + sizeof(double2)) * size_t(max_cap) * nsig +
+           sizeof(int32_t) * nsig + 1024;
   int rc = EnsureArena(ctx, bytes);
   if (rc) return rc;
   rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
@@ -913,6 +930,9 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   ctx->d_solve_ctl = cv.take<SolveCtl>(nsig);
   ctx->d_draws = cv.take<int32_t>(size_t(nsig) * kDrawChunk * (4 + max_trials_all));
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
+  int32_t *d_exp_keys = cv.take<int32_t>(size_t(max_cap) * nsig);
+  double2 *d_exp_coefs = cv.take<double2>(size_t(max_cap) * nsig);
+  int32_t *d_exp_counts = cv.take<int32_t>(nsig);
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
   int64_t phase_entries = 1;
@@ -922,12 +942,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     its[i].x_energy = d_energy + size_t(kEnergyStride) * i;
     its[i].n = int32_t(sigs[i]->n);
     phase_entries = std::max(phase_entries, PhaseTableEntries(sigs[i]->n));
-    rc = ClearTable(ctx, its[i], ctls[i]);
-    if (rc) return rc;
   }
-  // FP64 unit-phase tables (per signal length, for the whole call)
+  // empty tables and the FP64 unit-phase tables (per signal length, for the
+  // whole call)
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
                                   cudaMemcpyHostToDevice, ctx->stream));
+  LaunchClearTables(d_its, nsig, max_cap, ctx->stream);
   LaunchPhaseTables(d_its, nsig, phase_entries, ctx->stream);
   std::vector<double> energy(nsig, 0.0);
   if (!fp64) {
@@ -1072,10 +1092,46 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   int first_err = MPSFT_OK;
   const double bin_ms = timer.TotalMs();
+  // every table's entries in two copies: counts first, then the
+  // (signals x largest count) block of keys and coefficients
+  LaunchExportTables(d_its, nsig, max_cap, d_exp_keys, d_exp_coefs,
+                     d_exp_counts, ctx->stream);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  rc = EnsureHostStage(ctx, sizeof(int32_t) * nsig);
+  if (rc) return rc;
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, d_exp_counts,
+                                  sizeof(int32_t) * nsig,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<int32_t> counts(nsig);
+  std::memcpy(counts.data(), ctx->h_stage, sizeof(int32_t) * nsig);
+  int32_t maxc = 0;
+  for (int i = 0; i < nsig; ++i) maxc = std::max(maxc, counts[i]);
+  const size_t kbytes = sizeof(int32_t) * size_t(maxc) * nsig;
+  rc = EnsureHostStage(ctx, kbytes + sizeof(double2) * size_t(maxc) * nsig + 64);
+  if (rc) return rc;
+  int32_t *h_keys = reinterpret_cast<int32_t *>(ctx->h_stage);
+  double2 *h_coefs =
+      reinterpret_cast<double2 *>(ctx->h_stage + ((kbytes + 15) & ~size_t(15)));
+  if (maxc > 0) {
+    MPSFT_CUDA(ctx, cudaMemcpy2DAsync(h_keys, sizeof(int32_t) * maxc, d_exp_keys,
+                                      sizeof(int32_t) * max_cap,
+                                      sizeof(int32_t) * maxc, nsig,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaMemcpy2DAsync(h_coefs, sizeof(double2) * maxc,
+                                      d_exp_coefs, sizeof(double2) * max_cap,
+                                      sizeof(double2) * maxc, nsig,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
   for (int i = 0; i < nsig; ++i) {
-    std::vector<std::pair<int32_t, double2>> modes;
-    rc = DownloadTable(ctx, its[i], &modes);
-    if (rc) return rc;
+    std::vector<std::pair<int32_t, double2>> modes(counts[i]);
+    for (int32_t j = 0; j < counts[i]; ++j) {
+      modes[j] = {h_keys[size_t(i) * maxc + j], h_coefs[size_t(i) * maxc + j]};
+    }
+    std::sort(modes.begin(), modes.end(),
+              [](const std::pair<int32_t, double2> &l,
+                 const std::pair<int32_t, double2> &r) { return l.first < r.first; });
     int st = run[i].status;
     const int32_t m = int32_t(modes.size());
     if (m > cap[i]) st = st ? st : MPSFT_ERR_CAPACITY;
@@ -1167,6 +1223,7 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->tw32) cudaFree(ctx->tw32);
   if (ctx->tw64) cudaFree(ctx->tw64);
   if (ctx->side) {

@@ -745,6 +745,32 @@ __global__ void k_pencil(const double2 *__restrict__ u3, int64_t count,
   sigma[2 * i + 1] = s1;
 }
 
+// Empty tables and control words of every signal.
+__global__ void k_clear_tables(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < it.tab_cap) {
+    it.tab_key[i] = kEmptyKey;
+    it.tab_coef[i] = make_double2(0.0, 0.0);
+    it.tab_err[i] = 0.0;
+  }
+  if (i < kCtlWords) it.flags[i] = 0;
+}
+
+// The occupied entries of every table, in insertion order, into a staging
+// area: signal s at [s * stride, s * stride + count_s).
+__global__ void k_export_tables(const SigIter *__restrict__ its, int32_t *keys,
+                                double2 *coefs, int32_t *counts, int stride) {
+  const SigIter &it = its[blockIdx.y];
+  const int cnt = *it.tab_count;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) counts[blockIdx.y] = cnt;
+  if (i >= cnt) return;
+  const int sl = it.occ_list[i];
+  keys[size_t(blockIdx.y) * stride + i] = it.tab_key[sl];
+  coefs[size_t(blockIdx.y) * stride + i] = it.tab_coef[sl];
+}
+
 template <typename T, int TMAX>
 void LaunchDecideT(const SigIter *d_its, int nsig, int max_bins, int mode,
                    int cond, cudaStream_t s) {
@@ -765,6 +791,19 @@ void LaunchDecideP(const SigIter *d_its, int nsig, int max_bins, int max_trials,
 }
 
 }  // namespace
+
+void LaunchClearTables(const SigIter *d_its, int nsig, int max_cap,
+                       cudaStream_t s) {
+  dim3 grid((std::max(max_cap, int(kCtlWords)) + 255) / 256, nsig);
+  k_clear_tables<<<grid, 256, 0, s>>>(d_its);
+}
+
+void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
+                        int32_t *keys, double2 *coefs, int32_t *counts,
+                        cudaStream_t s) {
+  dim3 grid((max_cap + 255) / 256, nsig);
+  k_export_tables<<<grid, 256, 0, s>>>(d_its, keys, coefs, counts, max_cap);
+}
 
 void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s) {
   // the occupied count is only known on the device: cover the whole table,

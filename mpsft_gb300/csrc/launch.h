@@ -45,6 +45,15 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
 // Per found mode: k1, bin, window response and the per-trial row-0 term.
 void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s);
 
+// Empty mode tables and control words of every signal.
+void LaunchClearTables(const SigIter *d_its, int nsig, int max_cap,
+                       cudaStream_t s);
+// Occupied table entries of signal s (insertion order) to keys / coefs
+// [s * max_cap, ...), their number to counts[s].
+void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
+                        int32_t *keys, double2 *coefs, int32_t *counts,
+                        cudaStream_t s);
+
 // mean |x|^2 of each signal into energy[sig * kEnergyStride] (two
 // deterministic passes).
 constexpr int kEnergyBlocks = 256;
