@@ -287,11 +287,13 @@ def run_gpu(args) -> None:
     iters = []
     launches = 0
     near = 0
+    loop_ms = 0.0
     for _ in range(args.steps):
         out, stats = step()
         near += sum(s["escalated"] for s in stats)
         iters += [s["iterations"] for s in stats]
         launches += stats[0]["kernel_launches"]
+        loop_ms += stats[0]["loop_ms"]
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -378,7 +380,8 @@ def run_gpu(args) -> None:
                        "l2": f"inputs larger than L2: {G} x 32 MiB signals resident",
                        "parallelism": f"replicas x{world}",
                        "iterations_mean": float(np.mean(iters)),
-                       "near_tie_bins_per_solve": near / (G * args.steps)},
+                       "near_tie_bins_per_solve": near / (G * args.steps),
+                       "loop_ms_per_step": loop_ms / args.steps},
             "e2e": {"value": e2e_value, "unit": "solves/s",
                     "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(d2h // max(args.steps, 1))},

@@ -202,6 +202,9 @@ typedef struct {
                           /* redone in FP64 (bins > 4096); 0 otherwise       */
   int32_t fp64_iterations;/* FP32 path: iterations run on the FP64 kernels   */
                           /* because rounding was not small against noise    */
+  double loop_ms;         /* device time of the call's iteration loop (from  */
+                          /* the first iteration's start to the last one's   */
+                          /* end; the rest of the call is setup and results) */
 } mpsft_stats;
 
 /* One full recovery (the Demo1::Run loop) of sig. Draws 3 + trials values

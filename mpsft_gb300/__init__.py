@@ -65,7 +65,7 @@ class Stats(ctypes.Structure):
                 ("bin_launches", ctypes.c_int32), ("bin_ms", ctypes.c_double),
                 ("escalated", ctypes.c_int32), ("status", ctypes.c_int32),
                 ("kernel_launches", ctypes.c_int64), ("unresolved", ctypes.c_int32),
-                ("fp64_iterations", ctypes.c_int32)]
+                ("fp64_iterations", ctypes.c_int32), ("loop_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -128,6 +128,10 @@ struct SigIter {
   // re-binning of listed bins: [((e * trials + t) * rows + r) * chunks + c]
   // partial sums over chunk c of the window support
   double2 *esc_part;
+  // [(e * trials + t) * rows + r]: the chunk partials summed in chunk order
+  // (by the warp that finishes the row's last chunk) and the arrival counter
+  double2 *esc_sum;
+  int32_t *esc_cnt;
   // per listed bin e: s^k, k < 64, with s = e^{2 pi i (b/n - (2 beta + 1)/(2B))}
   // as float-float {re.hi, im.hi, re.lo, im.lo} at [e * 64 + k], and s^64
   float4 *esc_pow;
@@ -344,6 +348,25 @@ __device__ inline bool PencilT(V u0, V u1, V u2, T *s0_out, T *s1_out,
   const T di = (T(2) * u0.x * u0.y) - (u2.x * u1.y + u2.y * u1.x);
   *s0_out = s0;
   *s1_out = s0 > T(0) ? sqrt(dr * dr + di * di) / s0 : T(0);
+  *im_m01 = mi;
+  return mi > T(0);
+}
+
+// The same vote with |det A|^2 and sigma0^2 = lmax instead of sigma1, for a
+// threshold test sigma1 / 2 > s as |det|^2 > 4 s^2 lmax.
+template <typename T, typename V>
+__device__ inline bool PencilSq(V u0, V u1, V u2, T *det2, T *lmax_out,
+                                T *im_m01) {
+  const T m00 = u0.x * u0.x + u0.y * u0.y + u1.x * u1.x + u1.y * u1.y;
+  const T m11 = u2.x * u2.x + u2.y * u2.y + u0.x * u0.x + u0.y * u0.y;
+  const T mr = (u0.x * u2.x + u0.y * u2.y) + (u1.x * u0.x + u1.y * u0.y);
+  const T mi = (u0.x * u2.y - u0.y * u2.x) + (u1.x * u0.y - u1.y * u0.x);
+  const T hd = T(0.5) * (m00 - m11);
+  const T lmax = T(0.5) * (m00 + m11) + sqrt(hd * hd + (mr * mr + mi * mi));
+  const T dr = (u0.x * u0.x - u0.y * u0.y) - (u2.x * u1.x - u2.y * u1.y);
+  const T di = (T(2) * u0.x * u0.y) - (u2.x * u1.y + u2.y * u1.x);
+  *det2 = dr * dr + di * di;
+  *lmax_out = lmax > T(0) ? lmax : T(0);
   *im_m01 = mi;
   return mi > T(0);
 }

@@ -31,6 +31,7 @@ struct mpsft_ctx {
   // gather/fold (tables, mode preparation and bucketing)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
   // stream the solve graph is captured on, and the last instantiated graph
   cudaStream_t cap = nullptr;
   cudaGraph_t graph = nullptr;
@@ -303,6 +304,8 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->chat64 = cv.take<double2>(s.m_cap);
   it->esc_part =
       cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap * kRebinChunks);
+  it->esc_sum = cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap);
+  it->esc_cnt = cv.take<int32_t>(size_t(kMaxListed) * s.trials * s.rows_cap);
   it->tab_key = cv.take<int32_t>(s.tab_cap);
   it->tab_coef = cv.take<double2>(s.tab_cap);
   it->tab_err = cv.take<double>(s.tab_cap);
@@ -916,7 +919,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   for (int i = 0; i < nsig; ++i) max_cap = std::max(max_cap, shapes[i].tab_cap);
   // table export staging
   bytes += (sizeof(int32_t) + sizeof(double2)) * size_t(max_cap) * nsig +
-           sizeof(int32_t) * nsig + 1024;
+           2 * sizeof(int32_t) * nsig + 1024;
   int rc = EnsureArena(ctx, bytes);
   if (rc) return rc;
   rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
@@ -932,7 +935,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
   int32_t *d_exp_keys = cv.take<int32_t>(size_t(max_cap) * nsig);
   double2 *d_exp_coefs = cv.take<double2>(size_t(max_cap) * nsig);
-  int32_t *d_exp_counts = cv.take<int32_t>(nsig);
+  int32_t *d_exp_counts = cv.take<int32_t>(2 * size_t(nsig));  // counts, sorted
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
   int64_t phase_entries = 1;
@@ -988,6 +991,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   BinTimer timer{ctx};
   int64_t launches = 0;
   bool host_loop = ctx->profiling || ctx->graph_unavailable;
+  MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
   if (!host_loop) {
     rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, &its, force,
                    any_forced, fp64, x_c128, &launches);
@@ -1090,21 +1094,24 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       }
     }
   }
+  MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
   int first_err = MPSFT_OK;
   const double bin_ms = timer.TotalMs();
   // every table's entries in two copies: counts first, then the
   // (signals x largest count) block of keys and coefficients
   LaunchExportTables(d_its, nsig, max_cap, d_exp_keys, d_exp_coefs,
-                     d_exp_counts, ctx->stream);
+                     d_exp_counts, d_exp_counts + nsig, ctx->stream);
   MPSFT_CUDA(ctx, cudaGetLastError());
-  rc = EnsureHostStage(ctx, sizeof(int32_t) * nsig);
+  rc = EnsureHostStage(ctx, 2 * sizeof(int32_t) * nsig);
   if (rc) return rc;
   MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, d_exp_counts,
-                                  sizeof(int32_t) * nsig,
+                                  2 * sizeof(int32_t) * nsig,
                                   cudaMemcpyDeviceToHost, ctx->stream));
   MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  std::vector<int32_t> counts(nsig);
+  std::vector<int32_t> counts(nsig), sorted(nsig);
   std::memcpy(counts.data(), ctx->h_stage, sizeof(int32_t) * nsig);
+  std::memcpy(sorted.data(), ctx->h_stage + sizeof(int32_t) * nsig,
+              sizeof(int32_t) * nsig);
   int32_t maxc = 0;
   for (int i = 0; i < nsig; ++i) maxc = std::max(maxc, counts[i]);
   const size_t kbytes = sizeof(int32_t) * size_t(maxc) * nsig;
@@ -1124,22 +1131,27 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                       cudaMemcpyDeviceToHost, ctx->stream));
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   }
+  float loop_ms = 0.f;
+  MPSFT_CUDA(ctx, cudaEventElapsedTime(&loop_ms, ctx->ev_loop0, ctx->ev_loop1));
   for (int i = 0; i < nsig; ++i) {
-    std::vector<std::pair<int32_t, double2>> modes(counts[i]);
-    for (int32_t j = 0; j < counts[i]; ++j) {
-      modes[j] = {h_keys[size_t(i) * maxc + j], h_coefs[size_t(i) * maxc + j]};
+    const int32_t *ki = h_keys + size_t(i) * maxc;
+    const double2 *ci = h_coefs + size_t(i) * maxc;
+    std::vector<int32_t> order;
+    if (!sorted[i]) {
+      order.resize(counts[i]);
+      for (int32_t j = 0; j < counts[i]; ++j) order[j] = j;
+      std::sort(order.begin(), order.end(),
+                [ki](int32_t l, int32_t r) { return ki[l] < ki[r]; });
     }
-    std::sort(modes.begin(), modes.end(),
-              [](const std::pair<int32_t, double2> &l,
-                 const std::pair<int32_t, double2> &r) { return l.first < r.first; });
     int st = run[i].status;
-    const int32_t m = int32_t(modes.size());
+    const int32_t m = counts[i];
     if (m > cap[i]) st = st ? st : MPSFT_ERR_CAPACITY;
     const int32_t w = std::min(m, cap[i]);
     for (int32_t j = 0; j < w; ++j) {
-      out_k[i][j] = modes[j].first;
-      out_c[i][2 * j] = modes[j].second.x;
-      out_c[i][2 * j + 1] = modes[j].second.y;
+      const int32_t s = sorted[i] ? j : order[j];
+      out_k[i][j] = ki[s];
+      out_c[i][2 * j] = ci[s].x;
+      out_c[i][2 * j + 1] = ci[s].y;
     }
     count[i] = m;
     if (stats) {
@@ -1156,6 +1168,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       s.escalated = run[i].near_ties;
       s.unresolved = run[i].unresolved;
       s.fp64_iterations = run[i].fp64_iters;
+      s.loop_ms = loop_ms;
     }
     if (st && !first_err) {
       first_err = st;
@@ -1197,6 +1210,8 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop1);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
@@ -1206,6 +1221,13 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
     return MPSFT_ERR_CUDA;
   }
   ctx->stream = ctx->own;
+  if (!(WindowKernelsLaunchable() && FftKernelsLaunchable() &&
+        DecideKernelsLaunchable() && RebinKernelsLaunchable() &&
+        ControlKernelsLaunchable())) {
+    cudaGetLastError();
+    mpsft_ctx_destroy(ctx);
+    return MPSFT_ERR_CUDA;
+  }
   LaunchTwiddles(ctx->tw32, ctx->tw64, ctx->stream);
   e = cudaStreamSynchronize(ctx->stream);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -1234,6 +1256,8 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   if (ctx->cap) cudaStreamDestroy(ctx->cap);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_loop0) cudaEventDestroy(ctx->ev_loop0);
+  if (ctx->ev_loop1) cudaEventDestroy(ctx->ev_loop1);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
@@ -1449,7 +1473,9 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 1024 +
                             direct_cells * sizeof(double2) +
                             (direct ? (sizeof(int32_t) + sizeof(double2) +
-                                       64 * sizeof(float4)) * size_t(bins) + 1024
+                                       64 * sizeof(float4)) * size_t(bins) +
+                                          (sizeof(double2) + sizeof(int32_t)) *
+                                              (direct_cells / kRebinChunks) + 2048
                                     : 0));
   if (rc) return rc;
   Carve cv{ctx->arena};
@@ -1462,6 +1488,8 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   if (direct) {
     // every bin is a listed bin of the FP64 re-binning kernel
     it.esc_part = cv.take<double2>(direct_cells);
+    it.esc_sum = cv.take<double2>(direct_cells / kRebinChunks);
+    it.esc_cnt = cv.take<int32_t>(direct_cells / kRebinChunks);
     it.esc_list = cv.take<int32_t>(bins);
     it.esc_pow = cv.take<float4>(size_t(bins) * 64);
     it.esc_step = cv.take<double2>(bins);
@@ -1480,21 +1508,15 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
     LaunchWindow(d_it, 1, it.p2, st);
     LaunchRebin(d_it, 1, bins, sig->dtype == MPSFT_C128, st);
     MPSFT_CUDA(ctx, cudaGetLastError());
-    std::vector<double2> part(direct_cells);
-    MPSFT_CUDA(ctx, cudaMemcpyAsync(part.data(), it.esc_part,
-                                    sizeof(double2) * direct_cells,
+    std::vector<double2> sum(direct_cells / kRebinChunks);
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(sum.data(), it.esc_sum,
+                                    sizeof(double2) * sum.size(),
                                     cudaMemcpyDeviceToHost, st));
     MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
     std::vector<double2> res(size_t(it.rows) * bins);
     for (int32_t bb = 0; bb < bins; ++bb) {
       for (int32_t r = 0; r < it.rows; ++r) {
-        const double2 *p = &part[(size_t(bb) * it.rows + r) * kRebinChunks];
-        double2 acc = p[0];
-        for (int cc = 1; cc < kRebinChunks; ++cc) {
-          acc.x += p[cc].x;
-          acc.y += p[cc].y;
-        }
-        res[size_t(r) * bins + bb] = acc;
+        res[size_t(r) * bins + bb] = sum[size_t(bb) * it.rows + r];
       }
     }
     MPSFT_CUDA(ctx, cudaMemcpy(out, res.data(), sizeof(double2) * res.size(),

@@ -1,4 +1,4 @@
-// Shared-memory radix-2 FFT used by the Bluestein size-B transform.
+// Shared-memory FFTs used by the Bluestein size-B transform.
 #pragma once
 
 #include "common.cuh"
@@ -33,38 +33,128 @@ __device__ inline float2 vmake2(double re, double im, float2 *) {
 __device__ inline double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
 __device__ inline double2 to_d2(double2 a) { return a; }
 
-// In-place FFT of a[0..m) in shared memory (m = 2^log2m <= kMaxFFT), natural
-// order in and out, unnormalised. tw[e] = e^{-2 pi i e / kMaxFFT} for
-// e < kMaxFFT / 2 (global, read through the read-only cache). inverse selects
-// the conjugate twiddles. Every thread of the block must call it.
+// Shared-memory layout of the transforms: element i at Pad(i), one empty
+// slot after every 8 elements, so that the threads of the first DIT / last
+// DIF pass (8 consecutive elements each) hit distinct banks. An array of m
+// elements occupies PadLen(m) slots.
+__device__ __forceinline__ int Pad(int i) { return i + (i >> 3); }
+__host__ __device__ inline int PadLen(int m) { return m + (m >> 3) + 1; }
+
+// W_N^e = e^{-2 pi i e / N} (conjugated for the inverse) from the table
+// tw[e'] = e^{-2 pi i e' / kMaxFFT}, e < N / 2.
 template <typename V>
-__device__ void BlockFFT(V *a, int m, int log2m, const V *__restrict__ tw,
-                         bool inverse) {
-  if (log2m == 0) return;  // a 1-point transform is the identity
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    const int j = int(__brev(uint32_t(i)) >> (32 - log2m));
-    if (j > i) {
-      const V t = a[i];
-      a[i] = a[j];
-      a[j] = t;
+__device__ __forceinline__ V Twiddle(const V *__restrict__ tw, int N, int e,
+                                     bool inverse) {
+  V w = __ldg(&tw[e * (kMaxFFT / N)]);
+  if (inverse) w.y = -w.y;
+  return w;
+}
+
+// In-place radix-2 FFTs of a[0..m) (padded layout) in shared memory (m = 2^log2m <=
+// kMaxFFT), unnormalised, with up to three radix-2 stages fused per pass: a
+// thread loads R = 2^r elements spaced h apart, runs the r stages in
+// registers and stores them back, so a pass costs one barrier.
+//   BlockFFTDif: decimation in frequency, natural order in, bit-reversed out.
+//   BlockFFTDit: decimation in time, bit-reversed in, natural order out.
+// A DIF forward transform, a pointwise product in bit-reversed order and a
+// DIT inverse transform make a circular convolution without any reordering.
+// Every thread of the block must call them.
+template <typename V, int R>
+__device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
+                                        bool inverse) {
+  const int groups = m / R;
+  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    const int k = g & (h - 1);
+    const int base = (g / h) * (R * h) + k;
+    V x[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) x[j] = a[Pad(base + j * h)];
+    // stages of span S h, S = R/2 .. 1: pairs (j, j + S), twiddle
+    // W_{2Sh}^{k + (j mod S) h} on the difference
+#pragma unroll
+    for (int S = R / 2; S >= 1; S >>= 1) {
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        if ((j & S) == 0) {
+          const V u = x[j], v = x[j + S];
+          x[j] = vadd(u, v);
+          x[j + S] = vmul(vsub(u, v),
+                          Twiddle(tw, 2 * S * h, k + (j & (S - 1)) * h, inverse));
+        }
+      }
     }
+#pragma unroll
+    for (int j = 0; j < R; ++j) a[Pad(base + j * h)] = x[j];
   }
   __syncthreads();
-  for (int s = 0; s < log2m; ++s) {
-    const int h = 1 << s;
-    const int stride = kMaxFFT >> (s + 1);
-    for (int bf = threadIdx.x; bf < (m >> 1); bf += blockDim.x) {
-      const int j = bf & (h - 1);
-      const int i0 = ((bf >> s) << (s + 1)) + j;
-      const int i1 = i0 + h;
-      V w = __ldg(&tw[j * stride]);
-      if (inverse) w.y = -w.y;
-      const V u = a[i0];
-      const V v = vmul(a[i1], w);
-      a[i0] = vadd(u, v);
-      a[i1] = vsub(u, v);
+}
+
+template <typename V, int R>
+__device__ __forceinline__ void DitPass(V *a, int m, int h, const V *tw,
+                                        bool inverse) {
+  const int groups = m / R;
+  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+    const int k = g & (h - 1);
+    const int base = (g / h) * (R * h) + k;
+    V x[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) x[j] = a[Pad(base + j * h)];
+    // stages of span S h, S = 1 .. R/2: twiddle W_{2Sh}^{k + (j mod S) h}
+    // on the upper input
+#pragma unroll
+    for (int S = 1; S < R; S <<= 1) {
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        if ((j & S) == 0) {
+          const V u = x[j];
+          const V v = vmul(x[j + S],
+                           Twiddle(tw, 2 * S * h, k + (j & (S - 1)) * h, inverse));
+          x[j] = vadd(u, v);
+          x[j + S] = vsub(u, v);
+        }
+      }
     }
-    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < R; ++j) a[Pad(base + j * h)] = x[j];
+  }
+  __syncthreads();
+}
+
+template <typename V>
+__device__ void BlockFFTDif(V *a, int m, int log2m, const V *__restrict__ tw,
+                            bool inverse) {
+  // spans m/2, m/4, ..., 1 in passes of up to three stages
+  int left = log2m;
+  while (left > 0) {
+    const int r = left >= 3 ? 3 : left;
+    const int h = 1 << (left - r);  // smallest span of this pass
+    if (r == 3) {
+      DifPass<V, 8>(a, m, h, tw, inverse);
+    } else if (r == 2) {
+      DifPass<V, 4>(a, m, h, tw, inverse);
+    } else {
+      DifPass<V, 2>(a, m, h, tw, inverse);
+    }
+    left -= r;
+  }
+}
+
+template <typename V>
+__device__ void BlockFFTDit(V *a, int m, int log2m, const V *__restrict__ tw,
+                            bool inverse) {
+  // spans 1, 2, ..., m/2 in passes of up to three stages
+  int done = 0;
+  while (done < log2m) {
+    const int r = log2m - done >= 3 ? 3 : log2m - done;
+    const int h = 1 << done;  // smallest span of this pass
+    if (r == 3) {
+      DitPass<V, 8>(a, m, h, tw, inverse);
+    } else if (r == 2) {
+      DitPass<V, 4>(a, m, h, tw, inverse);
+    } else {
+      DitPass<V, 2>(a, m, h, tw, inverse);
+    }
+    done += r;
   }
 }
 

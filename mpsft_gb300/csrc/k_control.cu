@@ -156,4 +156,10 @@ void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
   k_finish<<<1, 1024, 0, s>>>(ctl, its, nsig, handle, set_condition ? 1 : 0);
 }
 
+bool ControlKernelsLaunchable() {
+  int a = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_finish, 1024, 0);
+  return a > 0;
+}
+
 }  // namespace mpsft

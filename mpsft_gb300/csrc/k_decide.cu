@@ -33,10 +33,10 @@ namespace {
 // One thread per occupied slot (the table's insertion list): k1 = (a k0 + b)
 // mod n and the mode's bin for the bucketing, and the row-0 term
 // wf c e^{2 pi i (q_t k1 + c k0)/n} of every trial (BinInFreqV1::Run,
-// src/binner.cc:565-591). The FP64 path evaluates the terms in FP64 (unit
-// phases from the FP64 tables); the FP32 path in FP32 only, together with the
-// error the mode carries into its bin: the coefficient's bound tab_err |wf|
-// plus 8 eps_rel |wf c| for the FP32 window response, phase, rounding and
+// src/binner.cc:565-591) in FP64 (unit phases from the FP64 tables). The
+// FP32 path also gets FP32 terms, computed in FP32, together with the error
+// the mode carries into its bin: the coefficient's bound tab_err |wf| plus
+// 8 eps_rel |wf c| for the FP32 window response, phase, rounding and
 // subtraction (each a few 2^-24 relative).
 __device__ inline float WindowInFreq32(const SigIter &it, int64_t k1, int bin) {
   // xi +- 1/(4B) with xi = (bin + 1/2)/B - k1/n, as exact integers over 4nB
@@ -70,12 +70,34 @@ __global__ void k_mode_prep(const SigIter *__restrict__ its) {
     }
     it.mode_errw[s] = float(it.tab_err[s]) * fabsf(wf) +
                       8.f * it.eps_rel * sqrtf(wc.x * wc.x + wc.y * wc.y);
-  } else {
-    const double xi = (double(bin) + 0.5) / double(B) - double(k1) / double(n);
-    const double2 wc = cscale(it.tab_coef[s], WindowInFreq(it, xi));
-    for (int t = 0; t < it.trials; ++t) {
-      const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
-      it.mode_base[size_t(s) * it.trials + t] = cmul(wc, Phase64(it, ph));
+  }
+  // FP64 terms: the FP64 path's subtraction, and on the FP32 path the
+  // near-tie bins' (this kernel runs beside the binning, off the critical path)
+  const double xi = (double(bin) + 0.5) / double(B) - double(k1) / double(n);
+  const double2 wc = cscale(it.tab_coef[s], WindowInFreq(it, xi));
+  for (int t = 0; t < it.trials; ++t) {
+    const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
+    it.mode_base[size_t(s) * it.trials + t] = cmul(wc, Phase64(it, ph));
+  }
+}
+
+// Ascending bitonic sort of keys[0..m) in shared memory (m a power of two),
+// by the whole block; ends with a barrier.
+__device__ void BitonicSort(unsigned long long *keys, int m) {
+  for (int size = 2; size <= m; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = keys[i], b = keys[j];
+          if ((a > b) == up) {
+            keys[i] = b;
+            keys[j] = a;
+          }
+        }
+      }
+      __syncthreads();
     }
   }
 }
@@ -115,22 +137,7 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
   }
   for (int i = threadIdx.x; i < B; i += blockDim.x) it.bkt_count[i] = 0;
   __syncthreads();
-  for (int size = 2; size <= m; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const int j = i ^ stride;
-        if (j > i) {
-          const bool up = (i & size) == 0;
-          const unsigned long long a = keys[i], b = keys[j];
-          if ((a > b) == up) {
-            keys[i] = b;
-            keys[j] = a;
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
+  BitonicSort(keys, m);
   __syncthreads();  // also orders the bkt_count zeroing when occ <= 1
   for (int i = threadIdx.x; i < occ; i += blockDim.x) {
     const unsigned long long k = keys[i];
@@ -165,28 +172,12 @@ template <> struct Ops<double> {
   using V = double2;
   __device__ static V from(double2 d) { return d; }
   __device__ static V phase(const SigIter &it, int64_t m) { return Phase64(it, m); }
-  // row-0 terms of a found mode: the FP64 path's k_mode_prep values, or, on
-  // the FP32 path (near-tie bins and bins redone in FP64), evaluated here in
-  // FP64
+  // row-0 terms of a found mode (k_mode_prep's FP64 values)
   template <int TMAX>
   __device__ static void terms(const SigIter &it, int sl, V *out) {
-    if (it.eps_rel == 0.f) {
-#pragma unroll
-      for (int t = 0; t < TMAX; ++t) {
-        if (t < it.trials) out[t] = it.mode_base[size_t(sl) * it.trials + t];
-      }
-      return;
-    }
-    const int64_t n = it.n, k1 = it.mode_k1[sl];
-    const int32_t key = it.tab_key[sl];
-    const double xi = (double(it.mode_bin[sl]) + 0.5) / double(it.bins) -
-                      double(k1) / double(n);
-    const double2 wc = cscale(it.tab_coef[sl], WindowInFreq(it, xi));
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
-      if (t < it.trials) {
-        out[t] = cmul(wc, Phase64(it, int64_t(it.q[t]) * k1 + int64_t(it.c) * key));
-      }
+      if (t < it.trials) out[t] = it.mode_base[size_t(sl) * it.trials + t];
     }
   }
 };
@@ -250,11 +241,7 @@ struct FromRebin {
     if (!RowListed(mask, r)) {
       return it.ubuf[(size_t(t) * it.rows + r) * it.bins_cap + beta];
     }
-    const double2 *p =
-        it.esc_part + ((size_t(e) * it.trials + t) * it.rows + r) * kRebinChunks;
-    double2 s = p[0];
-    for (int c = 1; c < kRebinChunks; ++c) s = cadd(s, p[c]);
-    return s;
+    return it.esc_sum[(size_t(e) * it.trials + t) * it.rows + r];
   }
 };
 
@@ -482,8 +469,16 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) {
         T s0, s1, im;
-        if (PencilT<T, V>(u0[t], up[t], um[t], &s0, &s1, &im)) ++count;
-        if (sv_thr > T(0) && s1 * T(0.5) > sv_thr) sv_fail = true;
+        if (fp32) {
+          if (PencilT<T, V>(u0[t], up[t], um[t], &s0, &s1, &im)) ++count;
+          if (sv_thr > T(0) && s1 * T(0.5) > sv_thr) sv_fail = true;
+        } else {
+          // sigma1 / 2 > sv_thr as |det|^2 > 4 sv_thr^2 sigma0^2 (one square
+          // root instead of three and a division)
+          T det2, lmax;
+          if (PencilSq<T, V>(u0[t], up[t], um[t], &det2, &lmax, &im)) ++count;
+          if (sv_thr > T(0) && det2 > T(4) * sv_thr * sv_thr * lmax) sv_fail = true;
+        }
         if (fp32) {
           const T a0 = vabs2<T, V>(u0[t]), a1 = vabs2<T, V>(up[t]),
                   a2 = vabs2<T, V>(um[t]);
@@ -511,9 +506,12 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   const uint32_t mask = __ballot_sync(0xffffffffu, has_bit && count > TR / 2);
   // bit 0 is the most significant digit of xi
   const uint32_t xs = L > 0 ? (__brev(mask) >> (32 - L)) : 0u;
+  // the FP32 path (also in its FP64 kernels) leaves pending candidates that
+  // the merge finishes on full warps; the FP64 path finishes them here
+  const bool pending = fp32 || it.eps_rel > 0.f;
   int64_t k1;
   double wf = 0.0;
-  if (fp32) {
+  if (pending) {
     k1 = RoundK1(n, beta, xs, L, B);
   } else {
     const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
@@ -597,7 +595,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
   // near-tie bins of the FP32 path: the rows that were not re-binned carry
   // the FP32 binning bound into the coefficient
   double err = 0.0;
-  if (it.eps_rel > 0.f) {
+  if (!fp32 && mode == kDecideExact) {
     float rm = 0.f, am = 0.f;
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
@@ -613,7 +611,16 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
     }
     float e = *it.eps_dev + it.eps_rel * (kEpsRowMax * rm + kEpsValue * am);
     for (int o = 16; o > 0; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
-    err = double(e) / fabs(wf);
+    err = double(e);
+  }
+  if (pending) {
+    if (lane == 0) {
+      it.cand_k0[beta] = int32_t(k1);
+      it.cand_coef[beta] = make_double2(double(ax), double(ay));
+      it.cand_err[beta] = err;
+      it.cand_valid[beta] = 2;
+    }
+    return;
   }
   if (lane == 0) {
     double2 coef = make_double2(double(ax) / double(TR * (1 + 2 * L)),
@@ -624,7 +631,7 @@ __device__ void DecideBin(const SigIter &it, int beta, const Src &src,
     coef = make_double2(coef.x / wf, coef.y / wf);
     it.cand_k0[beta] = k0;
     it.cand_coef[beta] = coef;
-    it.cand_err[beta] = err;
+    it.cand_err[beta] = 0.0;
     it.cand_valid[beta] = 1;
     it.flags[0] = 1;
   }
@@ -757,18 +764,49 @@ __global__ void k_clear_tables(const SigIter *__restrict__ its) {
   if (i < kCtlWords) it.flags[i] = 0;
 }
 
-// The occupied entries of every table, in insertion order, into a staging
-// area: signal s at [s * stride, s * stride + count_s).
-__global__ void k_export_tables(const SigIter *__restrict__ its, int32_t *keys,
-                                double2 *coefs, int32_t *counts, int stride) {
-  const SigIter &it = its[blockIdx.y];
+// The occupied entries of every table into a staging area, signal s at
+// [s * stride, s * stride + count_s), sorted by k0 (one block per signal,
+// bitonic sort of (k0, slot) in shared memory); a table with more entries
+// than the sort holds (only after a capacity status) is written in insertion
+// order and sorted[s] = 0.
+__global__ void __launch_bounds__(1024)
+    k_export_tables(const SigIter *__restrict__ its, int32_t *keys,
+                    double2 *coefs, int32_t *counts, int32_t *sorted, int stride) {
+  extern __shared__ unsigned long long sk[];
+  const SigIter &it = its[blockIdx.x];
   const int cnt = *it.tab_count;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) counts[blockIdx.y] = cnt;
-  if (i >= cnt) return;
-  const int sl = it.occ_list[i];
-  keys[size_t(blockIdx.y) * stride + i] = it.tab_key[sl];
-  coefs[size_t(blockIdx.y) * stride + i] = it.tab_coef[sl];
+  const size_t base = size_t(blockIdx.x) * stride;
+  const bool fits = cnt <= BucketKeys(it.tab_cap);
+  if (threadIdx.x == 0) {
+    counts[blockIdx.x] = cnt;
+    sorted[blockIdx.x] = fits ? 1 : 0;
+  }
+  if (!fits) {
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const int sl = it.occ_list[i];
+      keys[base + i] = it.tab_key[sl];
+      coefs[base + i] = it.tab_coef[sl];
+    }
+    return;
+  }
+  int m = 1;
+  while (m < cnt) m <<= 1;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    unsigned long long k = ~0ull;
+    if (i < cnt) {
+      const int sl = it.occ_list[i];
+      k = (static_cast<unsigned long long>(uint32_t(it.tab_key[sl])) << 32) |
+          static_cast<unsigned long long>(uint32_t(sl));
+    }
+    sk[i] = k;
+  }
+  __syncthreads();
+  BitonicSort(sk, m);
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    const unsigned long long k = sk[i];
+    keys[base + i] = int32_t(k >> 32);
+    coefs[base + i] = it.tab_coef[uint32_t(k)];
+  }
 }
 
 template <typename T, int TMAX>
@@ -800,9 +838,12 @@ void LaunchClearTables(const SigIter *d_its, int nsig, int max_cap,
 
 void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
                         int32_t *keys, double2 *coefs, int32_t *counts,
-                        cudaStream_t s) {
-  dim3 grid((max_cap + 255) / 256, nsig);
-  k_export_tables<<<grid, 256, 0, s>>>(d_its, keys, coefs, counts, max_cap);
+                        int32_t *sorted, cudaStream_t s) {
+  const size_t sm = size_t(BucketKeys(max_cap)) * sizeof(unsigned long long);
+  cudaFuncSetAttribute(k_export_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(sm));
+  k_export_tables<<<nsig, 1024, sm, s>>>(d_its, keys, coefs, counts, sorted,
+                                         max_cap);
 }
 
 void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s) {
@@ -862,6 +903,23 @@ void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
   if (count <= 0) return;
   k_pencil<<<unsigned((count + 255) / 256), 256, 0, s>>>(u3, count, sigma,
                                                           vote);
+}
+
+bool DecideKernelsLaunchable() {
+  int a = 0, b = 0, c = 0, d = 0;
+  const size_t smb = size_t(BucketKeys(kMaxTableCap)) * sizeof(unsigned long long);
+  cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(smb));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_bucket, 1024, smb);
+  int e = 0;
+  cudaFuncSetAttribute(k_export_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(smb));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e, k_export_tables, 1024, smb);
+  a = a < e ? a : e;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_decide<double, kMaxTrials>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_decide<float, kMaxTrials>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_decide_listed<kMaxTrials>, 256, 0);
+  return a > 0 && b > 0 && c > 0 && d > 0;
 }
 
 }  // namespace mpsft

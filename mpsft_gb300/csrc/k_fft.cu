@@ -40,22 +40,24 @@ __global__ void __launch_bounds__(512)
   const V *__restrict__ src = reinterpret_cast<const V *>(it.fold) +
                               (size_t(tr) * it.rows + row) * it.bins_cap;
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
-    a[j] = j < B ? vmul(src[j], __ldg(&chirp[j]))
-                 : vmake2(0.0, 0.0, (V *)nullptr);
+    a[Pad(j)] = j < B ? vmul(src[j], __ldg(&chirp[j]))
+                      : vmake2(0.0, 0.0, (V *)nullptr);
   }
   __syncthreads();
-  BlockFFT(a, M, it.fft_log2m, tw, false);
+  // forward DIF (bit-reversed out), product with chat (stored bit-reversed),
+  // inverse DIT (natural out)
+  BlockFFTDif(a, M, it.fft_log2m, tw, false);
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
-    a[j] = vmul(a[j], __ldg(&chat[j]));
+    a[Pad(j)] = vmul(a[Pad(j)], __ldg(&chat[j]));
   }
   __syncthreads();
-  BlockFFT(a, M, it.fft_log2m, tw, true);
+  BlockFFTDit(a, M, it.fft_log2m, tw, true);
   const double inv_m = 1.0 / double(M);
   const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
   double2 *dst = it.ubuf + (size_t(tr) * it.rows + row) * it.bins_cap;
   float mx = 0.f;
   for (int k = threadIdx.x; k < B; k += blockDim.x) {
-    const double2 y = cscale(to_d2(vmul(a[k], __ldg(&chirp[k]))), inv_m);
+    const double2 y = cscale(to_d2(vmul(a[Pad(k)], __ldg(&chirp[k]))), inv_m);
     dst[k] = cmul(bq, y);
     mx = fmaxf(mx, float(sqrt(y.x * y.x + y.y * y.y)));
   }
@@ -75,18 +77,31 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
                   const double2 *tw64, cudaStream_t s, bool cond) {
   dim3 grid(max_rows, max_trials, nsig);
   if (fp64) {
-    const size_t sm = size_t(max_m) * sizeof(double2);
+    const size_t sm = size_t(PadLen(max_m)) * sizeof(double2);
     cudaFuncSetAttribute(k_row_fft<double2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
     k_row_fft<double2><<<grid, 512, sm, s>>>(d_its, max_trials, tw64,
                                              cond ? 1 : 0);
   } else {
-    const size_t sm = size_t(max_m) * sizeof(float2);
+    const size_t sm = size_t(PadLen(max_m)) * sizeof(float2);
     cudaFuncSetAttribute(k_row_fft<float2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
     k_row_fft<float2><<<grid, 512, sm, s>>>(d_its, max_trials, tw32,
                                             cond ? 1 : 0);
   }
+}
+
+bool FftKernelsLaunchable() {
+  int n1 = 0, n2 = 0;
+  const size_t sm32 = size_t(PadLen(kMaxFFT)) * sizeof(float2);
+  const size_t sm64 = size_t(PadLen(kMaxFFT64)) * sizeof(double2);
+  cudaFuncSetAttribute(k_row_fft<float2>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm32));
+  cudaFuncSetAttribute(k_row_fft<double2>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm64));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_row_fft<float2>, 512, sm32);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_row_fft<double2>, 512, sm64);
+  return n1 > 0 && n2 > 0;
 }
 
 }  // namespace mpsft

@@ -20,8 +20,8 @@
 // Work item = (signal, listed bin, trial, listed row, chunk of the support),
 // one warp each; the 32 lanes split the chunk into consecutive runs; lane sums
 // are combined by a fixed shuffle tree and the chunk partials are added in
-// chunk order by the FP64 decision (so the result does not depend on the
-// scheduling).
+// chunk order by whichever warp finishes a row's last chunk (so the result
+// does not depend on the scheduling).
 #include "common.cuh"
 #include "launch.h"
 
@@ -116,6 +116,10 @@ __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ 
   const int64_t n = it.n, twoB = 2 * int64_t(it.bins);
   const int64_t b = PosMod(it.b, n);
   const int64_t g = 2 * int64_t(it.esc_list[e]) + 1;
+  // arrival counters of this bin's (trial, row) sums
+  for (int i = lane; i < it.trials * it.rows; i += 32) {
+    it.esc_cnt[size_t(e) * it.trials * it.rows + i] = 0;
+  }
   float4 *pw = it.esc_pow + size_t(e) * kPowLen;
   for (int k = lane; k < kPowLen; k += 32) {
     const double2 z = PowerOfStep(k, b, g, n, twoB);
@@ -241,9 +245,24 @@ __global__ void __launch_bounds__(256, 2)
       tr += __shfl_xor_sync(0xffffffffu, tr, o);
       ti += __shfl_xor_sync(0xffffffffu, ti, o);
     }
+    // the warp that completes a (trial, row) adds its chunk partials in
+    // chunk order (the result does not depend on which warp that is)
+    const size_t etr = (size_t(e) * it.trials + t) * it.rows + r;
+    int last = 0;
     if (lane == 0) {
-      it.esc_part[((size_t(e) * it.trials + t) * it.rows + r) * kRebinChunks + c] =
-          make_double2(tr, ti);
+      it.esc_part[etr * kRebinChunks + c] = make_double2(tr, ti);
+      __threadfence();
+      last = atomicAdd(&it.esc_cnt[etr], 1) == kRebinChunks - 1;
+    }
+    if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+      __threadfence();
+      double2 s = __ldcg(&it.esc_part[etr * kRebinChunks]);
+      for (int cc = 1; cc < kRebinChunks; ++cc) {
+        const double2 p = __ldcg(&it.esc_part[etr * kRebinChunks + cc]);
+        s.x += p.x;
+        s.y += p.y;
+      }
+      it.esc_sum[etr] = s;
     }
   }
 }
@@ -266,6 +285,13 @@ void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
       k_rebin_ff<float2><<<blocks, 256, 0, s>>>(d_its + s0, cnt);
     }
   }
+}
+
+bool RebinKernelsLaunchable() {
+  int a = 0, b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_rebin_ff<float2>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rebin_ff<double2>, 256, 0);
+  return a > 0 && b > 0;
 }
 
 }  // namespace mpsft

@@ -8,7 +8,8 @@
 //   X[k] = chirp[k] * sum_j (y[j] chirp[j]) * conj(chirp[k - j]),
 //   chirp[j] = e^{-pi i j^2 / B} with j^2 reduced mod 2B exactly,
 // a circular convolution of length M = 2^ceil(log2(2B - 1)) done with the
-// radix-2 shared-memory FFT; chat = FFT_M of the conjugate chirp sequence.
+// shared-memory FFT; chat = FFT_M of the conjugate chirp sequence, stored in
+// bit-reversed order.
 #include "fft.cuh"
 #include "launch.h"
 
@@ -89,8 +90,9 @@ __device__ inline double2 *ChatOf(const SigIter &it, double2 *) { return it.chat
 // cond: only signals with more near-tie bins than their list holds (whose
 // iteration is redone in FP64) take part.
 template <typename V>
-__global__ void k_bluestein_setup(const SigIter *__restrict__ its,
-                                  const V *__restrict__ tw, int cond) {
+__global__ void __launch_bounds__(512)
+    k_bluestein_setup(const SigIter *__restrict__ its, const V *__restrict__ tw,
+                      int cond) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *a = reinterpret_cast<V *>(smem_raw);
   const SigIter &it = its[blockIdx.x];
@@ -101,7 +103,7 @@ __global__ void k_bluestein_setup(const SigIter *__restrict__ its,
   V *chat = ChatOf(it, (V *)nullptr);
   const int64_t twoB = 2 * int64_t(B);
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
-    a[j] = vmake2(0.0, 0.0, (V *)nullptr);
+    a[Pad(j)] = vmake2(0.0, 0.0, (V *)nullptr);
   }
   __syncthreads();
   for (int j = threadIdx.x; j < B; j += blockDim.x) {
@@ -110,12 +112,13 @@ __global__ void k_bluestein_setup(const SigIter *__restrict__ its,
     sincospi(-double(j2) / double(B), &s, &c);
     chirp[j] = vmake2(c, s, (V *)nullptr);
     const V cc = vmake2(c, -s, (V *)nullptr);  // conj(chirp[j])
-    a[j] = cc;
-    if (j > 0) a[M - j] = cc;
+    a[Pad(j)] = cc;
+    if (j > 0) a[Pad(M - j)] = cc;
   }
   __syncthreads();
-  BlockFFT(a, M, it.fft_log2m, tw, false);
-  for (int j = threadIdx.x; j < M; j += blockDim.x) chat[j] = a[j];
+  // chat in bit-reversed order (the row transforms' forward output order)
+  BlockFFTDif(a, M, it.fft_log2m, tw, false);
+  for (int j = threadIdx.x; j < M; j += blockDim.x) chat[j] = a[Pad(j)];
 }
 
 }  // namespace
@@ -140,15 +143,15 @@ void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
                           const float2 *tw32, const double2 *tw64,
                           cudaStream_t s, bool cond) {
   if (fp64) {
-    const size_t sm = size_t(max_m) * sizeof(double2);
+    const size_t sm = size_t(PadLen(max_m)) * sizeof(double2);
     cudaFuncSetAttribute(k_bluestein_setup<double2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_bluestein_setup<double2><<<nsig, 1024, sm, s>>>(d_its, tw64, cond ? 1 : 0);
+    k_bluestein_setup<double2><<<nsig, 512, sm, s>>>(d_its, tw64, cond ? 1 : 0);
   } else {
-    const size_t sm = size_t(max_m) * sizeof(float2);
+    const size_t sm = size_t(PadLen(max_m)) * sizeof(float2);
     cudaFuncSetAttribute(k_bluestein_setup<float2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_bluestein_setup<float2><<<nsig, 1024, sm, s>>>(d_its, tw32, cond ? 1 : 0);
+    k_bluestein_setup<float2><<<nsig, 512, sm, s>>>(d_its, tw32, cond ? 1 : 0);
   }
 }
 
@@ -210,6 +213,19 @@ void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
     k_energy_partial<float2><<<grid, 256, 0, s>>>(x, n, energy);
   }
   k_energy_final<<<nsig, kEnergyBlocks, 0, s>>>(n, energy);
+}
+
+bool WindowKernelsLaunchable() {
+  int n1 = 0, n2 = 0;
+  const size_t sm32 = size_t(PadLen(kMaxFFT)) * sizeof(float2);
+  const size_t sm64 = size_t(PadLen(kMaxFFT64)) * sizeof(double2);
+  cudaFuncSetAttribute(k_bluestein_setup<float2>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm32));
+  cudaFuncSetAttribute(k_bluestein_setup<double2>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm64));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_bluestein_setup<float2>, 512, sm32);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_bluestein_setup<double2>, 512, sm64);
+  return n1 > 0 && n2 > 0;
 }
 
 }  // namespace mpsft

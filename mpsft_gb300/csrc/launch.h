@@ -48,11 +48,12 @@ void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s)
 // Empty mode tables and control words of every signal.
 void LaunchClearTables(const SigIter *d_its, int nsig, int max_cap,
                        cudaStream_t s);
-// Occupied table entries of signal s (insertion order) to keys / coefs
-// [s * max_cap, ...), their number to counts[s].
+// Occupied table entries of signal s to keys / coefs [s * max_cap, ...),
+// sorted by k0 (sorted[s] = 1; 0: insertion order, the table exceeded half
+// its capacity), their number to counts[s].
 void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
                         int32_t *keys, double2 *coefs, int32_t *counts,
-                        cudaStream_t s);
+                        int32_t *sorted, cudaStream_t s);
 
 // mean |x|^2 of each signal into energy[sig * kEnergyStride] (two
 // deterministic passes).
@@ -101,5 +102,15 @@ void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
 // Batched 2x2 pencils.
 void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
                   int32_t *vote, cudaStream_t s);
+
+// Whether the kernels with large blocks or shared memory can be launched on
+// the current device in their largest configuration (checked when a context
+// is created, so that a resource limit fails loudly instead of silently
+// skipping a launch).
+bool WindowKernelsLaunchable();
+bool FftKernelsLaunchable();
+bool DecideKernelsLaunchable();
+bool RebinKernelsLaunchable();
+bool ControlKernelsLaunchable();
 
 }  // namespace mpsft
