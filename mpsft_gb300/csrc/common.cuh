@@ -25,7 +25,13 @@ constexpr int kMaxFoldsPerLane = 10;  // folds f = p / bins <= 80
 constexpr int kMaxFFT = 16384;     // largest Bluestein transform (FP32)
 constexpr int kMaxFFT64 = 8192;    // largest Bluestein transform (FP64)
 constexpr int32_t kEmptyKey = -1;
-constexpr int kRebinChunks = 16;   // FP64 re-binning: chunks of the support
+constexpr int kRebinChunks = 16;   // re-binning: at most this many chunks of the support
+// chunks of a window support of p samples: runs of at least 64 samples per
+// lane (32 lanes per chunk), at most kRebinChunks
+__host__ __device__ inline int RebinChunks(int p) {
+  const int c = (p + 2047) / 2048;
+  return c < 1 ? 1 : (c > kRebinChunks ? kRebinChunks : c);
+}
 constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
 constexpr int kRebinMaxSignals = 256;  // signals per FP64 re-binning launch
 

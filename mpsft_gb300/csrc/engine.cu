@@ -730,10 +730,31 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_solve_ctl, hc.data(),
                                   sizeof(SolveCtl) * nsig, cudaMemcpyHostToDevice,
                                   ctx->stream));
+  // late-iteration phase: bins up to small_bins (a few times min_bins)
+  int32_t min_bins_max = 1;
+  int32_t min_bins_min = INT32_MAX;
+  for (int i = 0; i < nsig; ++i) {
+    min_bins_max = std::max(min_bins_max, opts[i].min_bins);
+    min_bins_min = std::min(min_bins_min, opts[i].min_bins);
+  }
+  const int32_t small_bins = (4 * min_bins_max) | 1;
+  const bool two_phase = mx.bins > small_bins;
+  Maxima mx_small = mx;
+  if (two_phase) {
+    mx_small.bins = small_bins;
+    mx_small.m = 1 << FFTLog2(small_bins);
+    mx_small.p2 = 0;
+    for (int i = 0; i < nsig; ++i) {
+      for (int32_t bb = min_bins_min | 1; bb <= small_bins; bb += 2) {
+        mx_small.p2 = std::max(mx_small.p2, MakeWindow(bb, opts[i].window_delta).p2);
+      }
+    }
+  }
   // graph (rebuilt when the launch shape or the arena changes)
   const std::vector<int64_t> key = {
       int64_t(reinterpret_cast<uintptr_t>(ctx->arena)), nsig, mx.bins, mx.bits,
-      mx.rows, mx.p2, mx.m, mx.cap, mx.trials, fp64, x_c128, any_forced};
+      mx.rows, mx.p2, mx.m, mx.cap, mx.trials, fp64, x_c128, any_forced,
+      small_bins, mx_small.p2};
   if (ctx->graph_key != key || ctx->graph_exec == nullptr) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -744,29 +765,54 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     cudaGraph_t g = nullptr;
     MPSFT_CUDA(ctx, cudaGraphCreate(&g, 0));
     ctx->graph = g;
-    cudaGraphConditionalHandle handle;
-    MPSFT_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, g, 1,
-                                                     cudaGraphCondAssignDefault));
-    // the params union has no default constructor: zeroed raw storage
-    alignas(cudaGraphNodeParams) unsigned char pbuf[sizeof(cudaGraphNodeParams)];
-    std::memset(pbuf, 0, sizeof(pbuf));
-    cudaGraphNodeParams &p = *reinterpret_cast<cudaGraphNodeParams *>(pbuf);
-    p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = handle;
-    p.conditional.type = cudaGraphCondTypeWhile;
-    p.conditional.size = 1;
-    cudaGraphNode_t node;
-    MPSFT_CUDA(ctx, cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p));
-    cudaGraph_t body = p.conditional.phGraph_out[0];
-    MPSFT_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->cap, body, nullptr, nullptr,
-                                                  0, cudaStreamCaptureModeThreadLocal));
-    LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ctx->cap);
+    // One while node per phase: the first runs every signal with launch
+    // shapes for the largest bins; once no signal needs more than small_bins,
+    // the second runs with shapes for small_bins (the late iterations, where
+    // most of a solve's iterations are, then launch no idle blocks).
+    struct Phase {
+      Maxima shape;
+      int32_t plan_max, cond_lo, cond_hi;
+    };
+    std::vector<Phase> phases;
+    if (two_phase) {
+      phases.push_back({mx, INT32_MAX, small_bins, INT32_MAX});
+      phases.push_back({mx_small, small_bins, 0, small_bins});
+    } else {
+      phases.push_back({mx, INT32_MAX, 0, INT32_MAX});
+    }
+    int rc = MPSFT_OK;
+    cudaError_t ce = cudaSuccess;
     int64_t per_body = 1;
-    int rc = LaunchIterationKernels(ctx, d_its, nsig, mx, x_c128, fp64, any_forced,
-                                    nullptr, &per_body, ctx->cap);
-    LaunchFinish(ctx->d_solve_ctl, d_its, nsig, handle, true, ctx->cap);
-    cudaGraph_t captured = nullptr;
-    const cudaError_t ce = cudaStreamEndCapture(ctx->cap, &captured);
+    cudaGraphNode_t prev = nullptr;
+    for (const Phase &ph : phases) {
+      cudaGraphConditionalHandle handle;
+      MPSFT_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, g, 1,
+                                                       cudaGraphCondAssignDefault));
+      // the params union has no default constructor: zeroed raw storage
+      alignas(cudaGraphNodeParams) unsigned char pbuf[sizeof(cudaGraphNodeParams)];
+      std::memset(pbuf, 0, sizeof(pbuf));
+      cudaGraphNodeParams &p = *reinterpret_cast<cudaGraphNodeParams *>(pbuf);
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = handle;
+      p.conditional.type = cudaGraphCondTypeWhile;
+      p.conditional.size = 1;
+      cudaGraphNode_t node;
+      MPSFT_CUDA(ctx, cudaGraphAddNode(&node, g, prev ? &prev : nullptr, nullptr,
+                                       prev ? 1 : 0, &p));
+      prev = node;
+      cudaGraph_t body = p.conditional.phGraph_out[0];
+      MPSFT_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->cap, body, nullptr, nullptr,
+                                                    0, cudaStreamCaptureModeThreadLocal));
+      LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ph.plan_max, ctx->cap);
+      per_body = 1;
+      rc = LaunchIterationKernels(ctx, d_its, nsig, ph.shape, x_c128, fp64,
+                                  any_forced, nullptr, &per_body, ctx->cap);
+      LaunchFinish(ctx->d_solve_ctl, d_its, nsig, handle, true, ph.cond_lo,
+                   ph.cond_hi, ctx->cap);
+      cudaGraph_t captured = nullptr;
+      ce = cudaStreamEndCapture(ctx->cap, &captured);
+      if (rc != MPSFT_OK || ce != cudaSuccess) break;
+    }
     cudaGraphExec_t exec = nullptr;
     cudaError_t ie = cudaErrorUnknown;
     if (rc == MPSFT_OK && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, g, 0);

@@ -58,12 +58,14 @@ __device__ __forceinline__ V Twiddle(const V *__restrict__ tw, int N, int e,
 //   BlockFFTDit: decimation in time, bit-reversed in, natural order out.
 // A DIF forward transform, a pointwise product in bit-reversed order and a
 // DIT inverse transform make a circular convolution without any reordering.
-// Every thread of the block must call them.
+// Threads tid = 0 .. nth-1 share the transform (several transforms of the
+// same size can run side by side in one block); every thread of the block
+// must call them (each pass ends with a block barrier).
 template <typename V, int R>
 __device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
-                                        bool inverse) {
+                                        bool inverse, int tid, int nth) {
   const int groups = m / R;
-  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+  for (int g = tid; g < groups; g += nth) {
     const int k = g & (h - 1);
     const int base = (g / h) * (R * h) + k;
     V x[R];
@@ -91,9 +93,9 @@ __device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
 
 template <typename V, int R>
 __device__ __forceinline__ void DitPass(V *a, int m, int h, const V *tw,
-                                        bool inverse) {
+                                        bool inverse, int tid, int nth) {
   const int groups = m / R;
-  for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+  for (int g = tid; g < groups; g += nth) {
     const int k = g & (h - 1);
     const int base = (g / h) * (R * h) + k;
     V x[R];
@@ -122,18 +124,18 @@ __device__ __forceinline__ void DitPass(V *a, int m, int h, const V *tw,
 
 template <typename V>
 __device__ void BlockFFTDif(V *a, int m, int log2m, const V *__restrict__ tw,
-                            bool inverse) {
+                            bool inverse, int tid, int nth) {
   // spans m/2, m/4, ..., 1 in passes of up to three stages
   int left = log2m;
   while (left > 0) {
     const int r = left >= 3 ? 3 : left;
     const int h = 1 << (left - r);  // smallest span of this pass
     if (r == 3) {
-      DifPass<V, 8>(a, m, h, tw, inverse);
+      DifPass<V, 8>(a, m, h, tw, inverse, tid, nth);
     } else if (r == 2) {
-      DifPass<V, 4>(a, m, h, tw, inverse);
+      DifPass<V, 4>(a, m, h, tw, inverse, tid, nth);
     } else {
-      DifPass<V, 2>(a, m, h, tw, inverse);
+      DifPass<V, 2>(a, m, h, tw, inverse, tid, nth);
     }
     left -= r;
   }
@@ -141,18 +143,18 @@ __device__ void BlockFFTDif(V *a, int m, int log2m, const V *__restrict__ tw,
 
 template <typename V>
 __device__ void BlockFFTDit(V *a, int m, int log2m, const V *__restrict__ tw,
-                            bool inverse) {
+                            bool inverse, int tid, int nth) {
   // spans 1, 2, ..., m/2 in passes of up to three stages
   int done = 0;
   while (done < log2m) {
     const int r = log2m - done >= 3 ? 3 : log2m - done;
     const int h = 1 << done;  // smallest span of this pass
     if (r == 3) {
-      DitPass<V, 8>(a, m, h, tw, inverse);
+      DitPass<V, 8>(a, m, h, tw, inverse, tid, nth);
     } else if (r == 2) {
-      DitPass<V, 4>(a, m, h, tw, inverse);
+      DitPass<V, 4>(a, m, h, tw, inverse, tid, nth);
     } else {
-      DitPass<V, 2>(a, m, h, tw, inverse);
+      DitPass<V, 2>(a, m, h, tw, inverse, tid, nth);
     }
     done += r;
   }

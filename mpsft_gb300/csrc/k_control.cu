@@ -31,8 +31,17 @@ __device__ int32_t NumBitsDev(int32_t n, int32_t bins) {
   return out;
 }
 
+__device__ inline int32_t NextBins(const SolveCtl &c, const SigIter &it) {
+  const int32_t found = *it.tab_count;
+  int32_t bins = (c.k - found) * 2 + 1;
+  if (bins < c.min_bins) bins = c.min_bins;
+  return bins;
+}
+
+// max_bins: signals needing more bins wait (the launch shapes of this body
+// do not cover them).
 __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
-                       int nsig) {
+                       int nsig, int32_t max_bins) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nsig) return;
   SolveCtl &c = ctl[i];
@@ -42,9 +51,11 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     it.active = 0;
     return;
   }
-  const int32_t found = *it.tab_count;
-  int32_t bins = (c.k - found) * 2 + 1;
-  if (bins < c.min_bins) bins = c.min_bins;
+  const int32_t bins = NextBins(c, it);
+  if (bins > max_bins) {
+    it.active = 0;
+    return;
+  }
   const int32_t bits = NumBitsDev(it.n, bins);
   const double B = double(bins);
   // Window scalars in the reference's operation order, no contraction.
@@ -103,9 +114,12 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
   it.active = 1;
 }
 
+// The while condition: some signal has work (not stopped, draws left) and
+// its next iteration's bins lie in (cond_lo, cond_hi].
 __global__ void __launch_bounds__(1024)
     k_finish(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its, int nsig,
-             cudaGraphConditionalHandle handle, int set_condition) {
+             cudaGraphConditionalHandle handle, int set_condition,
+             int32_t cond_lo, int32_t cond_hi) {
   int any = 0;
   for (int i = threadIdx.x; i < nsig; i += blockDim.x) {
     SolveCtl &c = ctl[i];
@@ -136,7 +150,10 @@ __global__ void __launch_bounds__(1024)
       c.last_bins = it.force_fp64 ? -1 : it.bins;
       it.active = 0;
     }
-    if (!c.done && c.iter - c.draw_base < c.draws_avail) any = 1;
+    if (!c.done && c.iter - c.draw_base < c.draws_avail) {
+      const int32_t nb = NextBins(c, it);
+      if (nb > cond_lo && nb <= cond_hi) any = 1;
+    }
   }
   any = __syncthreads_or(any);
   if (threadIdx.x == 0 && set_condition) {
@@ -146,14 +163,16 @@ __global__ void __launch_bounds__(1024)
 
 }  // namespace
 
-void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, cudaStream_t s) {
-  k_plan<<<(nsig + 127) / 128, 128, 0, s>>>(ctl, its, nsig);
+void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, int32_t max_bins,
+                cudaStream_t s) {
+  k_plan<<<(nsig + 127) / 128, 128, 0, s>>>(ctl, its, nsig, max_bins);
 }
 
 void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
                   cudaGraphConditionalHandle handle, bool set_condition,
-                  cudaStream_t s) {
-  k_finish<<<1, 1024, 0, s>>>(ctl, its, nsig, handle, set_condition ? 1 : 0);
+                  int32_t cond_lo, int32_t cond_hi, cudaStream_t s) {
+  k_finish<<<1, 1024, 0, s>>>(ctl, its, nsig, handle, set_condition ? 1 : 0,
+                              cond_lo, cond_hi);
 }
 
 bool ControlKernelsLaunchable() {

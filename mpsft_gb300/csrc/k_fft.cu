@@ -7,6 +7,8 @@
 // One CTA per (row, trial, signal). FP32 path: the convolution runs in FP32
 // (M <= 16384 points, 128 KB of shared memory); FP64 path: in FP64
 // (M <= 8192).
+#include <algorithm>
+
 #include "fft.cuh"
 #include "launch.h"
 
@@ -21,80 +23,154 @@ __device__ inline const double2 *ChatOf(const SigIter &it, double2 *) { return i
 
 // cond: only signals whose iteration is redone in FP64 take part. Also
 // records the largest |U| of each row (used by the FP32 near-tie bound).
+//
+// Rows per block: small transforms share a block, RowsPerBlock(M) rows side by
+// side (M/8 threads each for the radix-8 passes), so that late iterations
+// with few bins do not launch a block per tiny row.
+constexpr int kRowFftThreads = 512;
+constexpr int kRowsMax = 64;
+__device__ __forceinline__ int RowsPerBlock(int M) {
+  const int r = kRowFftThreads * 8 / M;
+  return r < 1 ? 1 : (r > kRowsMax ? kRowsMax : r);
+}
+
 template <typename V>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(kRowFftThreads)
     k_row_fft(const SigIter *__restrict__ its, int max_trials,
-              const V *__restrict__ tw, int cond) {
+              const V *__restrict__ tw, int cond, int rpb_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ float red[16];
-  V *a = reinterpret_cast<V *>(smem_raw);
+  __shared__ unsigned row_max_bits[kRowsMax];
   const SigIter &it = its[blockIdx.z];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
-  const int row = blockIdx.x;
   const int tr = blockIdx.y;
-  if (row >= it.rows || tr >= it.trials) return;
   const int B = it.bins, M = it.fft_m;
+  const int rpb = min(RowsPerBlock(M), rpb_cap);
+  const int row0 = blockIdx.x * rpb;
+  if (row0 >= it.rows || tr >= it.trials) return;
+  const int nth = kRowFftThreads / rpb;  // threads per row
+  const int lr = threadIdx.x / nth, tid = threadIdx.x % nth;
+  const int row = row0 + lr;
+  const bool live = lr < rpb && row < it.rows;
+  V *a = reinterpret_cast<V *>(smem_raw) + size_t(lr) * PadLen(M);
   const V *__restrict__ chirp = ChirpOf(it, (V *)nullptr);
   const V *__restrict__ chat = ChatOf(it, (V *)nullptr);
-  const V *__restrict__ src = reinterpret_cast<const V *>(it.fold) +
-                              (size_t(tr) * it.rows + row) * it.bins_cap;
-  for (int j = threadIdx.x; j < M; j += blockDim.x) {
-    a[Pad(j)] = j < B ? vmul(src[j], __ldg(&chirp[j]))
-                      : vmake2(0.0, 0.0, (V *)nullptr);
+  if (threadIdx.x < kRowsMax) row_max_bits[threadIdx.x] = 0u;
+  // element loops: up to 8 elements per thread with their loads issued
+  // together (a thread covers M / nth elements)
+  if (live) {
+    const V *__restrict__ src = reinterpret_cast<const V *>(it.fold) +
+                                (size_t(tr) * it.rows + row) * it.bins_cap;
+    for (int j0 = tid; j0 < M; j0 += 8 * nth) {
+      V v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u * nth;
+        if (j < M) {
+          v[u] = j < B ? vmul(src[j], __ldg(&chirp[j]))
+                       : vmake2(0.0, 0.0, (V *)nullptr);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u * nth;
+        if (j < M) a[Pad(j)] = v[u];
+      }
+    }
   }
   __syncthreads();
   // forward DIF (bit-reversed out), product with chat (stored bit-reversed),
-  // inverse DIT (natural out)
-  BlockFFTDif(a, M, it.fft_log2m, tw, false);
-  for (int j = threadIdx.x; j < M; j += blockDim.x) {
-    a[Pad(j)] = vmul(a[Pad(j)], __ldg(&chat[j]));
+  // inverse DIT (natural out); rows past the last run the barriers only
+  BlockFFTDif(a, live ? M : 0, it.fft_log2m, tw, false, tid, nth);
+  if (live) {
+    for (int j0 = tid; j0 < M; j0 += 8 * nth) {
+      V w[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u * nth;
+        if (j < M) w[u] = __ldg(&chat[j]);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u * nth;
+        if (j < M) a[Pad(j)] = vmul(a[Pad(j)], w[u]);
+      }
+    }
   }
   __syncthreads();
-  BlockFFTDit(a, M, it.fft_log2m, tw, true);
-  const double inv_m = 1.0 / double(M);
-  const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
-  double2 *dst = it.ubuf + (size_t(tr) * it.rows + row) * it.bins_cap;
-  float mx = 0.f;
-  for (int k = threadIdx.x; k < B; k += blockDim.x) {
-    const double2 y = cscale(to_d2(vmul(a[Pad(k)], __ldg(&chirp[k]))), inv_m);
-    dst[k] = cmul(bq, y);
-    mx = fmaxf(mx, float(sqrt(y.x * y.x + y.y * y.y)));
+  BlockFFTDit(a, live ? M : 0, it.fft_log2m, tw, true, tid, nth);
+  if (live) {
+    const double inv_m = 1.0 / double(M);
+    const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
+    double2 *dst = it.ubuf + (size_t(tr) * it.rows + row) * it.bins_cap;
+    float mx = 0.f;
+    for (int k0 = tid; k0 < B; k0 += 8 * nth) {
+      V w[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u * nth;
+        if (k < B) w[u] = __ldg(&chirp[k]);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u * nth;
+        if (k < B) {
+          const double2 y = cscale(to_d2(vmul(a[Pad(k)], w[u])), inv_m);
+          dst[k] = cmul(bq, y);
+          mx = fmaxf(mx, float(sqrt(y.x * y.x + y.y * y.y)));
+        }
+      }
+    }
+    // non-negative floats order like their bit patterns
+    atomicMax(&row_max_bits[lr], __float_as_uint(mx));
   }
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-  __syncthreads();
-  if (threadIdx.x == 0 && it.row_max != nullptr) {
-    for (int w = 1; w < int(blockDim.x >> 5); ++w) mx = fmaxf(mx, red[w]);
-    it.row_max[tr * it.rows + row] = mx;
+  __syncthreads();  // (rows past the last only reach the barriers)
+  if (live && tid == 0 && it.row_max != nullptr) {
+    it.row_max[tr * it.rows + row] = __uint_as_float(row_max_bits[lr]);
   }
 }
 
 }  // namespace
 
+// Shared memory of a block: one padded row of the largest transform, or the
+// rows of smaller ones side by side (at most 4096 + 512 + 64 slots).
+inline size_t RowFftSlots(int max_m) {
+  const size_t one = size_t(PadLen(max_m));
+  const size_t packed = size_t(kRowFftThreads) * 8 + kRowFftThreads + kRowsMax;
+  return one > packed ? one : packed;
+}
+
 void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
                   int max_trials, int max_m, bool fp64, const float2 *tw32,
                   const double2 *tw64, cudaStream_t s, bool cond) {
-  dim3 grid(max_rows, max_trials, nsig);
+  // rows per block: as many as the transform size allows, but no fewer
+  // blocks than about two per SM (so that a single signal, or the FP64
+  // pipes, still spread over the GPU); every transform of the launch has at
+  // most max_m points, so at least rpb rows per block
+  const int rpb_cap =
+      std::max(1, int(int64_t(max_rows) * max_trials * nsig / (2 * 152)));
+  const int rpb = std::max(
+      1, std::min({kRowsMax, kRowFftThreads * 8 / std::max(1, max_m), rpb_cap}));
+  dim3 grid((max_rows + rpb - 1) / rpb, max_trials, nsig);
   if (fp64) {
-    const size_t sm = size_t(PadLen(max_m)) * sizeof(double2);
+    const size_t sm = RowFftSlots(max_m) * sizeof(double2);
     cudaFuncSetAttribute(k_row_fft<double2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_row_fft<double2><<<grid, 512, sm, s>>>(d_its, max_trials, tw64,
-                                             cond ? 1 : 0);
+    k_row_fft<double2><<<grid, kRowFftThreads, sm, s>>>(d_its, max_trials, tw64,
+                                                        cond ? 1 : 0, rpb_cap);
   } else {
-    const size_t sm = size_t(PadLen(max_m)) * sizeof(float2);
+    const size_t sm = RowFftSlots(max_m) * sizeof(float2);
     cudaFuncSetAttribute(k_row_fft<float2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_row_fft<float2><<<grid, 512, sm, s>>>(d_its, max_trials, tw32,
-                                            cond ? 1 : 0);
+    k_row_fft<float2><<<grid, kRowFftThreads, sm, s>>>(d_its, max_trials, tw32,
+                                                       cond ? 1 : 0, rpb_cap);
   }
 }
 
 bool FftKernelsLaunchable() {
   int n1 = 0, n2 = 0;
-  const size_t sm32 = size_t(PadLen(kMaxFFT)) * sizeof(float2);
-  const size_t sm64 = size_t(PadLen(kMaxFFT64)) * sizeof(double2);
+  const size_t sm32 = RowFftSlots(kMaxFFT) * sizeof(float2);
+  const size_t sm64 = RowFftSlots(kMaxFFT64) * sizeof(double2);
   cudaFuncSetAttribute(k_row_fft<float2>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm32));
   cudaFuncSetAttribute(k_row_fft<double2>,

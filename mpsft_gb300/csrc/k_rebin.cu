@@ -17,7 +17,8 @@
 // from exact integer phases; each block sum then enters an FP64 total through
 // A_blk. The window comes from a float-float table of the FP64 window.
 //
-// Work item = (signal, listed bin, trial, listed row, chunk of the support),
+// Work item = (signal, listed bin, trial, listed row, chunk of the support;
+// RebinChunks(p) chunks),
 // one warp each; the 32 lanes split the chunk into consecutive runs; lane sums
 // are combined by a fixed shuffle tree and the chunk partials are added in
 // chunk order by whichever warp finishes a row's last chunk (so the result
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(256, 2)
     int64_t items = 0;
     if (q.active && !q.force_fp64) {
       const int nf = *(volatile int32_t *)&q.flags[2];
-      if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * kRebinChunks;
+      if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * RebinChunks(q.p);
     }
     items_end[s] = items;
   }
@@ -157,8 +158,9 @@ __global__ void __launch_bounds__(256, 2)
     while (w >= items_end[sig]) ++sig;
     int64_t local = w - (sig > 0 ? items_end[sig - 1] : 0);
     const SigIter &it = its[sig];
-    const int c = int(local % kRebinChunks);
-    local /= kRebinChunks;
+    const int nch = RebinChunks(it.p);
+    const int c = int(local % nch);
+    local /= nch;
     const int r = int(local % it.rows);
     local /= it.rows;
     const int t = int(local % it.trials);
@@ -177,7 +179,7 @@ __global__ void __launch_bounds__(256, 2)
       off = (r & 1) ? (B << s) : -(B << s);
     }
     const int64_t tau = int64_t(it.q[t]) + off;
-    const int64_t chunk = (int64_t(it.p) + kRebinChunks - 1) / kRebinChunks;
+    const int64_t chunk = (int64_t(it.p) + nch - 1) / nch;
     const int64_t c0 = -int64_t(it.p2) + c * chunk;
     const int64_t c1 = min(c0 + chunk, int64_t(it.p2) + 1);
     const int64_t per = (chunk + 31) / 32;
@@ -252,12 +254,12 @@ __global__ void __launch_bounds__(256, 2)
     if (lane == 0) {
       it.esc_part[etr * kRebinChunks + c] = make_double2(tr, ti);
       __threadfence();
-      last = atomicAdd(&it.esc_cnt[etr], 1) == kRebinChunks - 1;
+      last = atomicAdd(&it.esc_cnt[etr], 1) == nch - 1;
     }
     if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
       __threadfence();
       double2 s = __ldcg(&it.esc_part[etr * kRebinChunks]);
-      for (int cc = 1; cc < kRebinChunks; ++cc) {
+      for (int cc = 1; cc < nch; ++cc) {
         const double2 p = __ldcg(&it.esc_part[etr * kRebinChunks + cc]);
         s.x += p.x;
         s.y += p.y;

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(512)
   }
   __syncthreads();
   // chat in bit-reversed order (the row transforms' forward output order)
-  BlockFFTDif(a, M, it.fft_log2m, tw, false);
+  BlockFFTDif(a, M, it.fft_log2m, tw, false, int(threadIdx.x), int(blockDim.x));
   for (int j = threadIdx.x; j < M; j += blockDim.x) chat[j] = a[Pad(j)];
 }
 

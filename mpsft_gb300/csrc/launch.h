@@ -94,10 +94,13 @@ void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,
 
 // Device-side control of a solve: iteration planning and the stop rule
 // (sets the while condition of the solve graph when set_condition).
-void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, cudaStream_t s);
+// k_plan runs signals needing at most max_bins bins; k_finish continues the
+// loop while a signal with work needs bins in (cond_lo, cond_hi].
+void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, int32_t max_bins,
+                cudaStream_t s);
 void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
                   cudaGraphConditionalHandle handle, bool set_condition,
-                  cudaStream_t s);
+                  int32_t cond_lo, int32_t cond_hi, cudaStream_t s);
 
 // Batched 2x2 pencils.
 void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
