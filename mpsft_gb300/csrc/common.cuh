@@ -326,6 +326,19 @@ __device__ inline double WindowInFreq(const SigIter &it, double xi) {
   return 0.5 * (erf((xi + c) * it.erf_d) - erf((xi - c) * it.erf_d));
 }
 
+// FP64 row-0 terms wf c e^{2 pi i (q_t k1 + c k0)/n} of the mode in table
+// slot s (k1 and its bin given) into mode_base (BinInFreqV1::Run,
+// src/binner.cc:565-591).
+__device__ inline void ModeTerms64(const SigIter &it, int s, int64_t k1, int bin) {
+  const double xi = (double(bin) + 0.5) / double(it.bins) - double(k1) / double(it.n);
+  const double2 wc = cscale(it.tab_coef[s], WindowInFreq(it, xi));
+  const int32_t key = it.tab_key[s];
+  for (int t = 0; t < it.trials; ++t) {
+    const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
+    it.mode_base[size_t(s) * it.trials + t] = cmul(wc, Phase64(it, ph));
+  }
+}
+
 // 2x2 matrix pencil [[u0, u2], [u1, u0]] (src/freqid.cc:27-48).
 // sigma0 = sqrt(largest eigenvalue of A^H A), sigma1 = |det A| / sigma0 (no
 // cancellation). With m01 = conj(u0) u2 + conj(u1) u0, the off-diagonal of

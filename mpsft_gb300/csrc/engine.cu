@@ -528,11 +528,19 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   // the window and the gather/fold run on the main one
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+  // FP32 path: the FP64 window tables (for the near-tie re-binning and the
+  // FP64 kernels) are built on the side stream; the binning uses an FP32
+  // evaluation
+  if (!fp64) LaunchWindow64(d_its, nsig, mx.p2, ctx->side);
   LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
   LaunchModePrep(d_its, nsig, mx.cap, ctx->side);
   LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
-  LaunchWindow(d_its, nsig, mx.p2, s);
+  if (fp64) {
+    LaunchWindow(d_its, nsig, mx.p2, s);
+  } else {
+    LaunchWindow32(d_its, nsig, mx.p2, s);
+  }
   if (timer) {
     int rc = timer->Begin();
     if (rc) return rc;
@@ -546,8 +554,8 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
   LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s);
-  // Bluestein setup, mode preparation, bucketing, window, fold, FFT, decide
-  if (launched) *launched += 7;
+  // Bluestein setup, mode preparation, bucketing, window(s), fold, FFT, decide
+  if (launched) *launched += fp64 ? 7 : 8;
   if (!fp64) {
     // near ties of the FP32 pass: listed bins re-binned and re-decided in
     // FP64; signals that the precision policy sends to FP64 (and signals
@@ -557,13 +565,14 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
     if (launched) *launched += 3;  // power tables, re-binning, decisions
     if (redo) {
+      LaunchModePrep(d_its, nsig, mx.cap, s, true);
       LaunchBluesteinSetup(d_its, nsig, mx.m, true, ctx->tw32, ctx->tw64, s, true);
       LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, true, s,
                     true);
       LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, true, ctx->tw32,
                    ctx->tw64, s, true);
       LaunchDecide(d_its, nsig, mx.bins, mx.trials, false, false, s, true);
-      if (launched) *launched += 4;
+      if (launched) *launched += 5;
     }
   }
   LaunchMerge(d_its, nsig, mx.bins, s);
@@ -1572,7 +1581,12 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   }
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   ctx->stream));
-  LaunchWindow(d_it, 1, it.p2, st);
+  // the window the solves use: FP64 for the FP64 path, FP32-evaluated for FP32
+  if (fp64) {
+    LaunchWindow(d_it, 1, it.p2, st);
+  } else {
+    LaunchWindow32(d_it, 1, it.p2, st);
+  }
   LaunchBluesteinSetup(d_it, 1, it.fft_m, fp64, ctx->tw32, ctx->tw64, st);
   BinTimer timer{ctx};
   rc = timer.Begin();

@@ -46,9 +46,10 @@ __device__ inline float WindowInFreq32(const SigIter &it, int64_t k1, int bin) {
   return 0.5f * (erff(float(np) * it.wf_scale) - erff(float(nm) * it.wf_scale));
 }
 
-__global__ void k_mode_prep(const SigIter *__restrict__ its) {
+__global__ void k_mode_prep(const SigIter *__restrict__ its, int cond) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
+  if (cond && !RedoFP64(it)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *it.tab_count) return;
   const int s = it.occ_list[i];
@@ -60,7 +61,8 @@ __global__ void k_mode_prep(const SigIter *__restrict__ its) {
   const int bin = int(mod.quot(k1 * B));
   it.mode_k1[s] = int32_t(k1);
   it.mode_bin[s] = bin;
-  if (it.eps_rel > 0.f) {
+  const bool fp32 = it.eps_rel > 0.f && !it.force_fp64 && !cond;
+  if (fp32) {
     const float wf = WindowInFreq32(it, k1, bin);
     const double2 cd = it.tab_coef[s];
     const float2 wc = make_float2(float(cd.x) * wf, float(cd.y) * wf);
@@ -70,14 +72,8 @@ __global__ void k_mode_prep(const SigIter *__restrict__ its) {
     }
     it.mode_errw[s] = float(it.tab_err[s]) * fabsf(wf) +
                       8.f * it.eps_rel * sqrtf(wc.x * wc.x + wc.y * wc.y);
-  }
-  // FP64 terms: the FP64 path's subtraction, and on the FP32 path the
-  // near-tie bins' (this kernel runs beside the binning, off the critical path)
-  const double xi = (double(bin) + 0.5) / double(B) - double(k1) / double(n);
-  const double2 wc = cscale(it.tab_coef[s], WindowInFreq(it, xi));
-  for (int t = 0; t < it.trials; ++t) {
-    const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;
-    it.mode_base[size_t(s) * it.trials + t] = cmul(wc, Phase64(it, ph));
+  } else {
+    ModeTerms64(it, s, k1, bin);
   }
 }
 
@@ -846,11 +842,12 @@ void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
                                          max_cap);
 }
 
-void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s) {
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,
+                    bool cond) {
   // the occupied count is only known on the device: cover the whole table,
   // blocks past the count exit at once
   dim3 grid((max_cap + 255) / 256, nsig);
-  k_mode_prep<<<grid, 256, 0, s>>>(d_its);
+  k_mode_prep<<<grid, 256, 0, s>>>(d_its, cond ? 1 : 0);
 }
 
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,

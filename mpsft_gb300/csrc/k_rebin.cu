@@ -105,7 +105,7 @@ __device__ inline double2 PowerOfStep(int64_t k, int64_t b, int64_t g,
 
 // One warp per listed bin: s^k (k < 64) as float-float complex
 // {re.hi, im.hi, re.lo, im.lo} and s^64 in FP64 (esc_pow / esc_step hold
-// esc_cap bins).
+// esc_cap bins), and the FP64 terms of the bin's found modes.
 __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ its) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.force_fp64) return;
@@ -128,6 +128,17 @@ __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ 
     pw[k] = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
   }
   if (lane == 0) it.esc_step[e] = PowerOfStep(kPowLen, b, g, n, twoB);
+  // FP64 row-0 terms of the bin's found modes, for its FP64 decision (the FP32
+  // path's mode preparation only made FP32 ones); near-tie lists of a solve
+  // carry a row mask, the direct evaluation of every bin has neither modes
+  // nor a mask
+  if (it.esc_mask == nullptr) return;
+  const int beta = it.esc_list[e];
+  const int nm = it.bkt_count[beta], st = it.bkt_start[beta];
+  for (int i = lane; i < nm; i += 32) {
+    const int sl = it.bkt_list[st + i];
+    ModeTerms64(it, sl, it.mode_k1[sl], it.mode_bin[sl]);
+  }
 }
 
 template <typename TX>

@@ -42,7 +42,9 @@ __device__ double SincPi(double x) {
   return r;
 }
 
-__global__ void k_window(const SigIter *__restrict__ its) {
+// FP64 window (the reference's evaluation order) into wt64 and, when
+// present, the float-float copy wtff; with_fp32 also rounds it into wt32.
+__global__ void k_window64(const SigIter *__restrict__ its, int with_fp32) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.tables_valid) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -58,11 +60,29 @@ __global__ void k_window(const SigIter *__restrict__ its) {
                   exp(__dmul_rn(__dmul_rn(-2.0, u), u)));
   }
   it.wt64[i] = v;
-  it.wt32[i] = float(v);
+  if (with_fp32) it.wt32[i] = float(v);
   if (it.wtff != nullptr) {
     const float h = __double2float_rn(v);
     it.wtff[i] = make_float2(h, __double2float_rn(v - double(h)));
   }
+}
+
+// The same window evaluated in FP32 for the FP32 binning (a few ulp; the
+// FP64 tables are built beside it, off the binning's critical path).
+__global__ void k_window32(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active || it.tables_valid || it.force_fp64) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > it.p2) return;
+  const float w = float(it.width);
+  float v = w;
+  if (i > 0) {
+    const float t = float(i);
+    const float y = t * w;  // sinc argument in units of pi
+    const float u = t * float(M_PI * it.sigma_f);
+    v = w * (sinpif(y) / (float(M_PI) * y)) * expf(-2.f * u * u);
+  }
+  it.wt32[i] = v;
 }
 
 // ph_lo[l] = e^{2 pi i l / n} for l < 2^ph_k and ph_hi[h] = e^{2 pi i h 2^ph_k / n}
@@ -136,7 +156,17 @@ void LaunchPhaseTables(const SigIter *d_its, int nsig, int64_t entries,
 
 void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
   dim3 grid((max_p2 + 1 + 255) / 256, nsig);
-  k_window<<<grid, 256, 0, s>>>(d_its);
+  k_window64<<<grid, 256, 0, s>>>(d_its, 1);
+}
+
+void LaunchWindow64(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
+  dim3 grid((max_p2 + 1 + 255) / 256, nsig);
+  k_window64<<<grid, 256, 0, s>>>(d_its, 0);
+}
+
+void LaunchWindow32(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
+  dim3 grid((max_p2 + 1 + 255) / 256, nsig);
+  k_window32<<<grid, 256, 0, s>>>(d_its);
 }
 
 void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,

@@ -20,8 +20,13 @@ inline int64_t PhaseTableEntries(int64_t n) {
   return lo > hi ? lo : hi;
 }
 
-// Window tables wt32 / wt64 at |t| in [0, p2] of every active signal.
+// Window tables at |t| in [0, p2] of every active signal: LaunchWindow
+// evaluates in FP64 and fills wt64, wtff and wt32 (rounded); the FP32 path
+// splits this into LaunchWindow32 (wt32 evaluated in FP32, for the binning)
+// and LaunchWindow64 (wt64 and wtff, on a side stream).
 void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s);
+void LaunchWindow32(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s);
+void LaunchWindow64(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s);
 
 // Bluestein chirp and FFT(conjugate chirp) of every active signal.
 // fp64 selects double tables.
@@ -42,8 +47,11 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
                   int max_trials, int max_m, bool fp64, const float2 *tw32,
                   const double2 *tw64, cudaStream_t s, bool cond = false);
 
-// Per found mode: k1, bin, window response and the per-trial row-0 term.
-void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s);
+// Per found mode: k1, bin, window response and the per-trial row-0 term
+// (FP32 terms on the FP32 path, FP64 terms on the FP64 path and for signals
+// the FP32 path runs on its FP64 kernels; cond: only those redone in FP64).
+void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,
+                    bool cond = false);
 
 // Empty mode tables and control words of every signal.
 void LaunchClearTables(const SigIter *d_its, int nsig, int max_cap,

@@ -165,7 +165,11 @@ extern "C" int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n,
   }
   const float2 *tw32 = reinterpret_cast<const float2 *>(base + kOffTw32);
   const double2 *tw64 = reinterpret_cast<const double2 *>(base + kOffTw64);
-  LaunchWindow(d_it, 1, it.p2, st);
+  if (fp64) {
+    LaunchWindow(d_it, 1, it.p2, st);
+  } else {
+    LaunchWindow32(d_it, 1, it.p2, st);
+  }
   LaunchBluesteinSetup(d_it, 1, it.fft_m, fp64, tw32, tw64, st);
   LaunchBinFold(d_it, 1, bins, bits, 1, dtype == MPSFT_C128, fp64, st);
   LaunchRowFFT(d_it, 1, it.rows, 1, it.fft_m, fp64, tw32, tw64, st);
