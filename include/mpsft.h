@@ -137,6 +137,36 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
                       const int32_t *k0, const double *coef, int64_t m,
                       double *inout);
 
+/* ---- coefficient estimation for a fixed frequency set, and its adjoint ---
+ * No entry point of the reference corresponds: these expose, as a linear map
+ * of x, the coefficient estimate of Iterate (src/iterate.cc:146-171) with the
+ * identified frequencies held fixed (no identification, no subtraction of
+ * other modes), and its adjoint (for gradients through the estimate). For
+ * each given k0 (k1 = (a k0 + b) mod n, beta = floor(k1 bins / n),
+ * xi0 = k1/n - (beta + 1/2)/bins, rows tau = q_t, q_t +- bins 2^s):
+ *   c(k0) = e^{-2 pi i c k0/n} / (wf(xi0) trials (1 + 2 bits))
+ *           * sum_t sum_rows U_{t,row}[beta] e^{-2 pi i tau k1 / n}
+ * with U the FP64 bins of mpsft_bin_in_time. FP64 throughout. */
+typedef struct {
+  int32_t bins;            /* odd                                          */
+  int32_t bits;            /* rows = 1 + 2 bits                           */
+  int32_t trials;          /* 1 .. 15                                      */
+  double window_delta;
+  int32_t a, b, c;         /* the transform of the estimate               */
+  int32_t q[15];           /* q of each trial                              */
+} mpsft_estimate_setup;
+
+/* c = A x: writes coef[2i], coef[2i+1] (host) for the m given k0. */
+int mpsft_estimate(mpsft_ctx *ctx, const mpsft_signal *sig,
+                   const mpsft_estimate_setup *setup, const int32_t *k0,
+                   int64_t m, double *coef);
+
+/* dx = A^H g for a signal of length n: g[2i], g[2i+1] (host, m entries) is
+ * the gradient with respect to c(k0[i]) in the conjugate-Wirtinger
+ * convention (torch's); writes dx[2j], dx[2j+1] (host, n entries). */
+int mpsft_adjoint(mpsft_ctx *ctx, int32_t n, const mpsft_estimate_setup *setup,
+                  const int32_t *k0, int64_t m, const double *g, double *dx);
+
 /* ---- MatPencil (batched) -------------------------------------------------- */
 /* For each i < count: the 2x2 pencil [[u0, u2], [u1, u0]] with
  * u = (u0, u1, u2) = u3[6i .. 6i+6) (interleaved complex); writes

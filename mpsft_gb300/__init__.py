@@ -59,6 +59,14 @@ class SolveOptions(ctypes.Structure):
                 ("near_tie_margin", ctypes.c_double)]
 
 
+class EstimateSetup(ctypes.Structure):
+    """The transform and shape of a fixed-set coefficient estimate."""
+    _fields_ = [("bins", ctypes.c_int32), ("bits", ctypes.c_int32),
+                ("trials", ctypes.c_int32), ("window_delta", ctypes.c_double),
+                ("a", ctypes.c_int32), ("b", ctypes.c_int32), ("c", ctypes.c_int32),
+                ("q", ctypes.c_int32 * 15)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("found", ctypes.c_int32),
                 ("gathers", ctypes.c_int64), ("bin_bytes", ctypes.c_int64),
@@ -109,6 +117,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_bin_in_freq": (I, [P, I32, I32, I32, D, I32, I32, I32, I32, P, P,
                                   I64, P]),
         "mpsft_mat_pencil": (I, [P, P, I64, P, P]),
+        "mpsft_estimate": (I, [P, P, ctypes.POINTER(EstimateSetup), P, I64, P]),
+        "mpsft_adjoint": (I, [P, I32, ctypes.POINTER(EstimateSetup), P, I64, P, P]),
         "mpsft_iterate": (I, [P, P, ctypes.POINTER(IterateOptions), P, P, P, P,
                               I32, P]),
         "mpsft_solve_options_default": (None, [ctypes.POINTER(SolveOptions)]),
@@ -123,6 +133,11 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def num_bits(n: int, bins: int) -> int:
+    """NumBits (src/iterate.cc:30-42): halvings of n while n >= bins."""
+    return int(load_library().mpsft_num_bits(int(n), int(bins)))
 
 
 def exported_symbols() -> list[str]:
@@ -242,6 +257,37 @@ class Context:
         _check(self, self._lib.mpsft_bin_in_freq(
             self._h, n, bins, bits, delta, a, b, c, q, _ptr(k0), _ptr(coef),
             k0.size, _ptr(out)))
+        return out
+
+    @staticmethod
+    def estimate_setup(bins: int, bits: int, delta: float, a: int, b: int, c: int,
+                       q) -> EstimateSetup:
+        s = EstimateSetup()
+        s.bins, s.bits, s.window_delta = bins, bits, delta
+        s.a, s.b, s.c = a, b, c
+        q = list(q)
+        s.trials = len(q)
+        for i, v in enumerate(q):
+            s.q[i] = int(v)
+        return s
+
+    def estimate(self, sig: "Signal", setup: EstimateSetup,
+                 k0: np.ndarray) -> np.ndarray:
+        """Coefficient estimate of the fixed set k0 (a linear map of x)."""
+        k0 = np.ascontiguousarray(k0, np.int32)
+        out = np.zeros(k0.size, np.complex128)
+        _check(self, self._lib.mpsft_estimate(self._h, sig._h, ctypes.byref(setup),
+                                              _ptr(k0), k0.size, _ptr(out)))
+        return out
+
+    def adjoint(self, n: int, setup: EstimateSetup, k0: np.ndarray,
+                g: np.ndarray) -> np.ndarray:
+        """A^H g for the estimate of k0 (complex128, n entries)."""
+        k0 = np.ascontiguousarray(k0, np.int32)
+        g = np.ascontiguousarray(g, np.complex128)
+        out = np.zeros(n, np.complex128)
+        _check(self, self._lib.mpsft_adjoint(self._h, n, ctypes.byref(setup),
+                                             _ptr(k0), k0.size, _ptr(g), _ptr(out)))
         return out
 
     def mat_pencil(self, u: np.ndarray):

@@ -1684,6 +1684,145 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   return MPSFT_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Shared setup of mpsft_estimate / mpsft_adjoint: validates, carves one
+// signal's buffers plus `extra` bytes, fills and uploads the descriptor, and
+// builds the FP64 window, Bluestein and unit-phase tables.
+int EstimateSetup(mpsft_ctx *ctx, int32_t n, const void *x,
+                  const mpsft_estimate_setup *su, size_t extra, Carve *cv,
+                  SigIter *it, SigIter **d_it) {
+  if (!su) return Fail(ctx, MPSFT_ERR_INVALID, "null setup");
+  int rc = CheckN(ctx, n);
+  if (rc) return rc;
+  rc = CheckWindow(ctx, su->bins, su->window_delta, true);
+  if (rc) return rc;
+  if (su->bits < 0 || su->bits > kMaxBits || su->trials < 1 ||
+      su->trials > kMaxTrials) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bad bits or trials");
+  }
+  if (int64_t(su->bins) << (su->bits > 0 ? su->bits - 1 : 0) > INT32_MAX) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bins * 2^(bits-1) overflows int32");
+  }
+  Shape s;
+  s.n = n;
+  s.bins_cap = su->bins;
+  s.rows_cap = 1 + 2 * su->bits;
+  s.trials = su->trials;
+  s.p2_cap = MakeWindow(su->bins, su->window_delta).p2;
+  s.m_cap = 1 << FFTLog2(su->bins);
+  s.tab_cap = 64;
+  s.fp64 = true;
+  Carve probe{nullptr};
+  SigIter tmp{};
+  int32_t *ctl;
+  CarveSignal(probe, s, &tmp, &ctl);
+  rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + extra + 4096);
+  if (rc) return rc;
+  *cv = Carve{ctx->arena};
+  *d_it = cv->take<SigIter>(1);
+  std::memset(it, 0, sizeof(*it));
+  CarveSignal(*cv, s, it, &ctl);
+  mpsft_signal fake{};
+  fake.n = n;
+  fake.d_x = const_cast<void *>(x);
+  const Transform tf{su->a, su->b, su->c, 0};
+  FillIter(it, &fake, su->bins, su->bits, su->window_delta, tf, su->q, su->trials);
+  cudaStream_t st = ctx->stream;
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(*d_it, it, sizeof(SigIter),
+                                  cudaMemcpyHostToDevice, st));
+  LaunchPhaseTables(*d_it, 1, PhaseTableEntries(n), st);
+  LaunchWindow(*d_it, 1, it->p2, st);
+  LaunchBluesteinSetup(*d_it, 1, it->fft_m, true, ctx->tw32, ctx->tw64, st);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  return MPSFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpsft_estimate(mpsft_ctx *ctx, const mpsft_signal *sig,
+                   const mpsft_estimate_setup *setup, const int32_t *k0,
+                   int64_t m, double *coef) {
+  if (!ctx || (m > 0 && (!k0 || !coef)) || m < 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  int rc = CheckSignal(ctx, sig);
+  if (rc) return rc;
+  Carve cv{nullptr};
+  SigIter it;
+  SigIter *d_it = nullptr;
+  const size_t extra = size_t(m) * (sizeof(int32_t) + sizeof(double2)) + 1024;
+  rc = EstimateSetup(ctx, int32_t(sig->n), sig->d_x, setup, extra, &cv, &it, &d_it);
+  if (rc) return rc;
+  int32_t *d_k0 = cv.take<int32_t>(size_t(m));
+  double2 *d_coef = cv.take<double2>(size_t(m));
+  cudaStream_t st = ctx->stream;
+  LaunchBinFold(d_it, 1, it.bins, it.bits, it.trials, sig->dtype == MPSFT_C128,
+                true, st);
+  LaunchRowFFT(d_it, 1, it.rows, it.trials, it.fft_m, true, ctx->tw32, ctx->tw64,
+               st);
+  if (m > 0) {
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_k0, k0, sizeof(int32_t) * m,
+                                    cudaMemcpyHostToDevice, st));
+    LaunchEstimate(d_it, d_k0, m, d_coef, st);
+  }
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  if (m > 0) {
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(coef, d_coef, sizeof(double2) * m,
+                                    cudaMemcpyDeviceToHost, st));
+  }
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  return MPSFT_OK;
+}
+
+int mpsft_adjoint(mpsft_ctx *ctx, int32_t n, const mpsft_estimate_setup *setup,
+                  const int32_t *k0, int64_t m, const double *g, double *dx) {
+  if (!ctx || !dx || (m > 0 && (!k0 || !g)) || m < 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  Carve cv{nullptr};
+  SigIter it;
+  SigIter *d_it = nullptr;
+  const size_t extra = size_t(m) * (sizeof(int32_t) + sizeof(double2)) +
+                       sizeof(double2) * size_t(n) + 1024;
+  int rc = EstimateSetup(ctx, n, nullptr, setup, extra, &cv, &it, &d_it);
+  if (rc) return rc;
+  int32_t *d_k0 = cv.take<int32_t>(size_t(m));
+  double2 *d_g = cv.take<double2>(size_t(m));
+  double2 *d_dx = cv.take<double2>(size_t(n));
+  cudaStream_t st = ctx->stream;
+  const int64_t cells = int64_t(it.trials) * it.rows * it.bins_cap;
+  MPSFT_CUDA(ctx, cudaMemsetAsync(it.fold, 0, sizeof(double2) * cells, st));
+  MPSFT_CUDA(ctx, cudaMemsetAsync(d_dx, 0, sizeof(double2) * size_t(n), st));
+  if (m > 0) {
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_k0, k0, sizeof(int32_t) * m,
+                                    cudaMemcpyHostToDevice, st));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_g, g, sizeof(double2) * m,
+                                    cudaMemcpyHostToDevice, st));
+  }
+  LaunchAdjointSpread(d_it, d_k0, d_g, m, st);
+  // inverse DFT of every row as conj(DFT(conj(G))): the row transform with
+  // unit row factors
+  for (int t = 0; t < it.trials; ++t) {
+    it.bq_re[t] = 1.0;
+    it.bq_im[t] = 0.0;
+  }
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(SigIter),
+                                  cudaMemcpyHostToDevice, st));
+  LaunchRowFFT(d_it, 1, it.rows, it.trials, it.fft_m, true, ctx->tw32, ctx->tw64,
+               st);
+  LaunchAdjointScatter(d_it, int64_t(it.trials) * it.rows * it.p, d_dx, st);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(dx, d_dx, sizeof(double2) * size_t(n),
+                                  cudaMemcpyDeviceToHost, st));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  return MPSFT_OK;
+}
+
 int mpsft_mat_pencil(mpsft_ctx *ctx, const double *u3, int64_t count,
                      double *sigma, int32_t *vote) {
   if (!ctx || count < 0 || (count > 0 && (!u3 || !sigma || !vote))) {

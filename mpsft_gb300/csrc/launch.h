@@ -114,6 +114,17 @@ void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
 void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
                   int32_t *vote, cudaStream_t s);
 
+// Coefficient estimate of a fixed frequency set from the bins in ubuf
+// (c = A x), and the pieces of its adjoint: spread g, conjugated, over the
+// rows of the fold buffer (zeroed by the caller), then, after a row FFT with
+// unit row factors into ubuf, scatter-add into dx (zeroed, n entries).
+void LaunchEstimate(const SigIter *d_it, const int32_t *k0, int64_t m,
+                    double2 *coef, cudaStream_t s);
+void LaunchAdjointSpread(const SigIter *d_it, const int32_t *k0, const double2 *g,
+                         int64_t m, cudaStream_t s);
+void LaunchAdjointScatter(const SigIter *d_it, int64_t items, double2 *dx,
+                          cudaStream_t s);
+
 // Whether the kernels with large blocks or shared memory can be launched on
 // the current device in their largest configuration (checked when a context
 // is created, so that a resource limit fails loudly instead of silently

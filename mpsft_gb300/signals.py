@@ -100,3 +100,20 @@ def config2(seed: int = 7) -> SparseSignal:
     """N = 2^22 complex64, S = 1000, |c| log-uniform in [1e-2, 1], 60 dB SNR."""
     return make_signal(1 << 22, 1000, seed, magnitude="loguniform",
                        mag_range=(1e-2, 1.0), snr_db=60.0)
+
+
+def config3(index: int, base_seed: int = 300) -> SparseSignal:
+    """Signal `index` of the uneven batch: N = 2^e with e uniform in
+    {16, ..., 24}, S uniform in [10, 2000], config-1 modes and noise
+    (unit magnitudes, sigma = 1e-6), complex64; seed-indexed."""
+    rng = np.random.default_rng(base_seed + index)
+    e = int(rng.integers(16, 25))
+    s = int(rng.integers(10, 2001))
+    return make_signal(1 << e, s, base_seed * 1000 + index, sigma=1e-6)
+
+
+def config5(seed: int = 5) -> SparseSignal:
+    """N = 2^26 complex64 (512 MiB), S = 4000 with 25% of the modes in close
+    pairs 1-3 apart, |c| log-uniform in [1e-3, 1], 40 dB SNR."""
+    return make_signal(1 << 26, 4000, seed, magnitude="loguniform",
+                       mag_range=(1e-3, 1.0), snr_db=40.0, pair_frac=0.25)
