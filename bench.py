@@ -54,7 +54,11 @@ def parse_args():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--batch", type=int, default=8, help="signals per step per GPU")
+    p.add_argument("--batch", type=int, default=64, help="signals per step per GPU")
+    p.add_argument("--workload", choices=["config2", "config3"], default="config2",
+                   help="config3: one step = the 256-signal uneven batch "
+                        "(N in 2^16..2^24, S in [10, 2000]); reported on its own "
+                        "line, not the headline")
     p.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="bounded CPU-baseline sample length")
@@ -227,6 +231,61 @@ def profile_traffic() -> float | None:
             except ValueError:
                 return None
     return None
+
+
+def run_config3(args) -> None:
+    """The uneven batch of config 3 as one batched solve per step (device-
+    resident signals; a parity workload measured for information)."""
+    import torch
+    import mpsft_gb300 as m
+    from mpsft_gb300.signals import config3
+
+    torch.cuda.set_device(0)
+    sigs_host = [config3(i) for i in range(256)]
+    ctx = m.Context(0)
+    stream = torch.cuda.Stream(device=0)
+    ctx.set_stream(stream.cuda_stream)
+    sigs = [ctx.upload(sg.x) for sg in sigs_host]
+    opts = [ctx.solve_options(sg.k.size, sg.sigma, trials=1, min_bins=51,
+                              window_delta=1e-5, window_threshold=0.1,
+                              max_stale_iter=5, precision=m.FP32)
+            for sg in sigs_host]
+    total_n = sum(sg.n for sg in sigs_host)
+    del sigs_host
+
+    def step():
+        rngs = [m.Rng(SEED_RNG + i) for i in range(len(sigs))]
+        return ctx.solve_batched(sigs, rngs, opts)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    steps = max(1, min(args.steps, 10))
+    ev0.record(stream)
+    iters, fp64_its = [], 0
+    for _ in range(steps):
+        out, stats = step()
+        iters += [s["iterations"] for s in stats]
+        fp64_its += sum(s["fp64_iterations"] for s in stats)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / steps
+    print(json.dumps({
+        "metric": "solves/s, config 3 uneven batch (256 signals, N 2^16..2^24, "
+                  "S 10..2000)",
+        "value": 256 / (ms / 1e3), "unit": "solves/s", "n_gpus": 1,
+        "steps": steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "config3", "signals": 256, "samples": total_n,
+                   "iterations_mean": float(np.mean(iters)),
+                   "fp64_iterations_per_step": fp64_its / steps},
+        "clocks": clk}), flush=True)
 
 
 def run_gpu(args) -> None:
@@ -436,6 +495,9 @@ def run_gpu(args) -> None:
 
 def main():
     args = parse_args()
+    if args.impl == "gpu" and args.workload == "config3":
+        run_config3(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
