@@ -561,9 +561,9 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     // FP64; signals that the precision policy sends to FP64 (and signals
     // whose near-tie list overflowed) run the FP64 kernels
     const bool redo = any_forced && mx.m <= kMaxFFT64;
-    LaunchRebin(d_its, nsig, kMaxListed, x_c128, s);
+    LaunchRebin(d_its, nsig, kMaxListed, x_c128, false, s);
     LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
-    if (launched) *launched += 3;  // power tables, re-binning, decisions
+    if (launched) *launched += 2;  // re-binning, FP64 decisions
     if (redo) {
       LaunchModePrep(d_its, nsig, mx.cap, s, true);
       LaunchBluesteinSetup(d_its, nsig, mx.m, true, ctx->tw32, ctx->tw64, s, true);
@@ -1527,10 +1527,10 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   const size_t direct_cells = direct ? size_t(bins) * s.rows_cap * kRebinChunks : 0;
   rc = EnsureArena(ctx, probe.off + sizeof(SigIter) + 1024 +
                             direct_cells * sizeof(double2) +
-                            (direct ? (sizeof(int32_t) + sizeof(double2) +
+                            (direct ? (2 * sizeof(int32_t) + sizeof(double2) +
                                        64 * sizeof(float4)) * size_t(bins) +
                                           (sizeof(double2) + sizeof(int32_t)) *
-                                              (direct_cells / kRebinChunks) + 2048
+                                              (direct_cells / kRebinChunks) + 2304
                                     : 0));
   if (rc) return rc;
   Carve cv{ctx->arena};
@@ -1561,7 +1561,7 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                     st));
     LaunchWindow(d_it, 1, it.p2, st);
-    LaunchRebin(d_it, 1, bins, sig->dtype == MPSFT_C128, st);
+    LaunchRebin(d_it, 1, bins, sig->dtype == MPSFT_C128, true, st);
     MPSFT_CUDA(ctx, cudaGetLastError());
     std::vector<double2> sum(direct_cells / kRebinChunks);
     MPSFT_CUDA(ctx, cudaMemcpyAsync(sum.data(), it.esc_sum,

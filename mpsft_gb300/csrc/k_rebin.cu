@@ -25,19 +25,11 @@
 // does not depend on the scheduling).
 #include "common.cuh"
 #include "launch.h"
+#include "rebin.cuh"
 
 namespace mpsft {
 
 namespace {
-
-struct FF {
-  float hi, lo;
-};
-
-__device__ __forceinline__ FF FFOf(double v) {
-  const float h = __double2float_rn(v);
-  return {h, __double2float_rn(v - double(h))};
-}
 
 // x*y + u*v in float-float: exact products of the high parts (FMA), two-sum
 // of those, the cross terms in the low word, then renormalisation.
@@ -90,22 +82,9 @@ __device__ __forceinline__ void SampleTimesWindow(double2 v, float2 w, FF *re,
   *im = FFOf(v.y * wd);
 }
 
-constexpr int kPowLen = 64;  // s^k table length = block of samples
-
-// Phase e^{2 pi i k Delta} from exact integer reductions:
-// k Delta = (k b mod n)/n - (k (2 beta + 1) mod 2B)/(2B) (mod 1).
-__device__ inline double2 PowerOfStep(int64_t k, int64_t b, int64_t g,
-                                      int64_t n, int64_t twoB) {
-  const int64_t m = PosMod(k * b, n);
-  const int64_t r = PosMod(k * g, twoB);
-  double s, c;
-  sincospi(2.0 * (double(m) / double(n) - double(r) / double(twoB)), &s, &c);
-  return make_double2(c, s);
-}
-
-// One warp per listed bin: s^k (k < 64) as float-float complex
-// {re.hi, im.hi, re.lo, im.lo} and s^64 in FP64 (esc_pow / esc_step hold
-// esc_cap bins), and the FP64 terms of the bin's found modes.
+// The preparation of the direct evaluation of every bin (mpsft_bin_in_time,
+// FP64_DIRECT): one warp per listed bin. A solve's FP32 decide kernel
+// prepares its listed bins itself when it lists them.
 __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ its) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.force_fp64) return;
@@ -113,32 +92,7 @@ __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ 
   if (nf > it.esc_cap) return;
   const int e = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (e >= nf) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t n = it.n, twoB = 2 * int64_t(it.bins);
-  const int64_t b = PosMod(it.b, n);
-  const int64_t g = 2 * int64_t(it.esc_list[e]) + 1;
-  // arrival counters of this bin's (trial, row) sums
-  for (int i = lane; i < it.trials * it.rows; i += 32) {
-    it.esc_cnt[size_t(e) * it.trials * it.rows + i] = 0;
-  }
-  float4 *pw = it.esc_pow + size_t(e) * kPowLen;
-  for (int k = lane; k < kPowLen; k += 32) {
-    const double2 z = PowerOfStep(k, b, g, n, twoB);
-    const FF zr = FFOf(z.x), zi = FFOf(z.y);
-    pw[k] = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
-  }
-  if (lane == 0) it.esc_step[e] = PowerOfStep(kPowLen, b, g, n, twoB);
-  // FP64 row-0 terms of the bin's found modes, for its FP64 decision (the FP32
-  // path's mode preparation only made FP32 ones); near-tie lists of a solve
-  // carry a row mask, the direct evaluation of every bin has neither modes
-  // nor a mask
-  if (it.esc_mask == nullptr) return;
-  const int beta = it.esc_list[e];
-  const int nm = it.bkt_count[beta], st = it.bkt_start[beta];
-  for (int i = lane; i < nm; i += 32) {
-    const int sl = it.bkt_list[st + i];
-    ModeTerms64(it, sl, it.mode_k1[sl], it.mode_bin[sl]);
-  }
+  PrepListedBin(it, e, it.esc_list[e], threadIdx.x & 31);
 }
 
 template <typename TX>
@@ -283,12 +237,14 @@ __global__ void __launch_bounds__(256, 2)
 }  // namespace
 
 void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
-                 cudaStream_t s) {
-  // s^k tables of every listed bin, then a persistent grid whose warps stride
-  // over the work items; batches are cut into groups of at most
-  // kRebinMaxSignals signals
-  dim3 pgrid((max_listed + 7) / 8, nsig);
-  k_rebin_prep<<<pgrid, 256, 0, s>>>(d_its);
+                 bool prepare, cudaStream_t s) {
+  // optionally the listed bins' preparation (a solve's decide kernel does it
+  // when it lists them), then a persistent grid whose warps stride over the
+  // work items; batches are cut into groups of at most kRebinMaxSignals
+  if (prepare) {
+    dim3 pgrid((max_listed + 7) / 8, nsig);
+    k_rebin_prep<<<pgrid, 256, 0, s>>>(d_its);
+  }
   const int blocks = 152 * 2;  // two resident blocks per SM (124 registers)
   for (int s0 = 0; s0 < nsig; s0 += kRebinMaxSignals) {
     const int cnt = nsig - s0 < kRebinMaxSignals ? nsig - s0 : kRebinMaxSignals;

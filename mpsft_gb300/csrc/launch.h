@@ -83,13 +83,14 @@ void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
                   bool cond = false);
 
 // Re-binning of the near-tie bins listed by the FP32 decide pass (direct sums
-// over the window support in float-float arithmetic with FP64 block totals)
-// and their FP64 decisions.
-// max_listed: the largest esc_cap of the signals.
+// over the window support in float-float arithmetic with FP64 block totals).
+// prepare: run the listed bins' preparation first (a solve's decide kernel
+// prepares the bins it lists itself). max_listed: the largest esc_cap.
 void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
-                 cudaStream_t s);
-// redo: the conditional FP64 kernels follow (signals whose list overflowed are
-// redone whole); without them such signals are reported unresolved.
+                 bool prepare, cudaStream_t s);
+// FP64 decisions of the listed bins on their re-binned rows. redo: the
+// conditional FP64 kernels follow (signals whose list overflowed are redone
+// whole); without them such signals are reported unresolved.
 void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
                         bool redo, cudaStream_t s);
 
