@@ -1,8 +1,7 @@
 // The per-bin decision of an iteration (the bin loop of Iterate,
 // src/iterate.cc:113-175, with IdentifyFreq, src/iterate.cc:44-76, MatPencil,
 // src/freqid.cc:27-48, and BinInFreqV1's subtraction, src/binner.cc:565-591),
-// shared by the decide kernels and the near-tie re-binning kernel, which
-// decides each listed bin as soon as its rows are re-binned.
+// used by the FP32, FP64 and near-tie (listed bin) decide kernels.
 #pragma once
 
 #include "common.cuh"
@@ -116,11 +115,13 @@ struct FromRebin {
   }
 };
 
+template <typename V> __device__ inline float Abs32(V a) {
+  const float x = float(a.x), y = float(a.y);
+  return sqrtf(x * x + y * y);
+}
+
 enum DecideMode { kDecide = 0, kSubtractOnly = 1, kDecideExact = 2 };
 
-// The bin loop body of Iterate for one bin (warp-wide). T = float: the FP32
-// path with near-tie detection; T = double: FP64 decisions (the FP64 path, and
-// the near-tie bins after their FP64 re-binning).
 // k1 = round(n (beta + xi1) / B) with xi1 = (2 xs + 1) / 2^{L+1}, exactly in
 // integers: num = n (beta 2^{L+1} + 2 xs + 1) < 2^64, den = B 2^{L+1} < 2^33
 // (B 2^{L-1} <= n by the definition of L). The reference evaluates this in
@@ -174,9 +175,11 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
   const int npre = min(nm, 32);
   V pre_base[TMAX];
   float mode_err = 0.f;  // FP32 error carried into this bin by the found modes
+  int pre_k1 = 0;  // k1 of the lane's mode (row factors below)
   if (lane < npre) {
     const int sl = it.bkt_list[st + lane];
     O::template terms<TMAX>(it, sl, pre_base);
+    pre_k1 = it.mode_k1[sl];
     if (fp32) mode_err = it.mode_errw[sl];
   }
   for (int i = 0; i < nm; ++i) {
@@ -272,30 +275,44 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
     }
   }
   const int64_t off = has_bit ? (int64_t(B) << lane) : 0;
-  for (int i = 0; i < nm; ++i) {
-    V bs[TMAX];
-    if (i < 32) {
+  // four modes at a time: their row factors e^{2 pi i (B 2^s k1 mod n)/n}
+  // (src/binner.cc:584-589) are evaluated side by side, then subtracted in
+  // the bin's mode order
+  for (int i0 = 0; i0 < nm; i0 += 4) {
+    V fac[4];
 #pragma unroll
-      for (int t = 0; t < TMAX; ++t) {
-        if (t < TR) {
-          bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
-          bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
-        }
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i < nm) {
+        const int64_t k1 = i < 32 ? __shfl_sync(0xffffffffu, pre_k1, i)
+                                  : it.mode_k1[it.bkt_list[st + i]];
+        if (has_bit) fac[u] = O::phase(it, off * k1);
       }
-    } else {
-      const int sl = it.bkt_list[st + i];
-      O::template terms<TMAX>(it, sl, bs);
     }
-    if (has_bit) {
-      // row factor e^{2 pi i (B 2^s k1 mod n)/n} of this lane's bit
-      // (src/binner.cc:584-589)
-      const int sl = it.bkt_list[st + i];
-      const V fac = O::phase(it, off * int64_t(it.mode_k1[sl]));
 #pragma unroll
-      for (int t = 0; t < TMAX; ++t) {
-        if (t < TR) {
-          up[t] = vsub2(up[t], vmul2(bs[t], fac));
-          um[t] = vsub2(um[t], vmul2(bs[t], vconj2(fac)));
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i < nm) {
+        V bs[TMAX];
+        if (i < 32) {
+#pragma unroll
+          for (int t = 0; t < TMAX; ++t) {
+            if (t < TR) {
+              bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
+              bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
+            }
+          }
+        } else {
+          O::template terms<TMAX>(it, it.bkt_list[st + i], bs);
+        }
+        if (has_bit) {
+#pragma unroll
+          for (int t = 0; t < TMAX; ++t) {
+            if (t < TR) {
+              up[t] = vsub2(up[t], vmul2(bs[t], fac[u]));
+              um[t] = vsub2(um[t], vmul2(bs[t], vconj2(fac[u])));
+            }
+          }
         }
       }
     }
@@ -474,10 +491,11 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
       if (t < TR) {
         const float *r = it.row_max + size_t(t) * rows;
         rm = fmaxf(rm, r[0]);
-        am = fmaxf(am, float(vabs2<T, V>(u0[t])));
+        // magnitudes in FP32 (an error bound needs no more)
+        am = fmaxf(am, Abs32(u0[t]));
         if (has_bit) {
           rm = fmaxf(rm, fmaxf(r[2 * lane + 1], r[2 * lane + 2]));
-          am = fmaxf(am, float(max(vabs2<T, V>(up[t]), vabs2<T, V>(um[t]))));
+          am = fmaxf(am, fmaxf(Abs32(up[t]), Abs32(um[t])));
         }
       }
     }
