@@ -1060,8 +1060,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   if (!host_loop) {
     std::vector<SolveCtl> h_ctl(nsig);
-    MPSFT_CUDA(ctx, cudaMemcpy(h_ctl.data(), ctx->d_solve_ctl,
-                               sizeof(SolveCtl) * nsig, cudaMemcpyDeviceToHost));
+    // on the context's stream (a legacy-stream copy would also wait for
+    // unrelated work, such as a caller's uploads on another stream)
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(h_ctl.data(), ctx->d_solve_ctl,
+                                    sizeof(SolveCtl) * nsig,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < nsig; ++i) {
       Run &r = run[i];
       const SolveCtl &c = h_ctl[i];
