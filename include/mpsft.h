@@ -101,6 +101,16 @@ int mpsft_signal_free(mpsft_signal *sig);
  * respect to the host until the next solve call. */
 int mpsft_signal_write(mpsft_ctx *ctx, mpsft_signal *sig, const void *x_host);
 
+/* mpsft_signal_write for count signals in one call, enqueued on stream (a
+ * cudaStream_t; NULL = the context's stream). The call touches no context
+ * state (errors are returned, not recorded as the context's last error), so
+ * a second host thread may issue the next batch's copies on its own stream
+ * while a solve of the same context runs; the caller orders the solve after
+ * the copies (an event recorded on stream). */
+int mpsft_signal_write_many(mpsft_ctx *ctx, mpsft_signal *const *sigs,
+                            const void *const *x_host, int32_t count,
+                            void *stream);
+
 /* ---- BinInTime::Run ------------------------------------------------------- */
 /* Overwrites out with the (1 + 2*bits) x bins bin matrix of signal sig for the
  * transform (a, b, c) and offset q: row 0 is tau = q, row 2s+1 is

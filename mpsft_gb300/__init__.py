@@ -113,6 +113,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_signal_wrap_device": (I, [P, P, I64, I, PP]),
         "mpsft_signal_free": (I, [P]),
         "mpsft_signal_write": (I, [P, P, P]),
+        "mpsft_signal_write_many": (I, [P, P, P, I32, P]),
         "mpsft_bin_in_time": (I, [P, P, I32, I32, D, I32, I32, I32, I32, I, P, I]),
         "mpsft_bin_in_freq": (I, [P, I32, I32, I32, D, I32, I32, I32, I32, P, P,
                                   I64, P]),
@@ -195,6 +196,9 @@ class Context:
             raise MpsftError(rc, "mpsft_ctx_create failed (is a GPU present?)")
         self._h = h
         self._lib = lib
+        # grow-only host buffers that batched solves write their modes into
+        self._out_k = np.empty(0, np.int32)
+        self._out_c = np.empty(0, np.complex128)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -230,6 +234,24 @@ class Context:
         _check(self, self._lib.mpsft_signal_wrap_device(
             self._h, ctypes.c_void_p(ptr), int(n), int(dtype), ctypes.byref(h)))
         return Signal(self, h, n, dtype)
+
+    def write_many(self, sigs: list, xs: list, stream_handle: int | None = None) -> None:
+        """Refills many signals from host arrays (pinned memory for an
+        asynchronous copy) on the given CUDA stream (None = the context's).
+        Safe to call from a second thread while a solve of this context runs,
+        when it names its own stream; order the solve after it with an event."""
+        if len(sigs) != len(xs):
+            raise ValueError("one host array per signal")
+        for sg, x in zip(sigs, xs):
+            want = np.complex64 if sg.dtype == C64 else np.complex128
+            if sg.ctx is not self or x.dtype != want or x.size != sg.n or \
+                    not x.flags.c_contiguous:
+                raise ValueError("x must match its signal's context, n and dtype")
+        nsig = len(sigs)
+        sig_arr = (ctypes.c_void_p * nsig)(*[s._h.value for s in sigs])
+        x_arr = (ctypes.c_void_p * nsig)(*[x.ctypes.data for x in xs])
+        _check(None, self._lib.mpsft_signal_write_many(
+            self._h, sig_arr, x_arr, nsig, ctypes.c_void_p(stream_handle or 0)))
 
     # ---- operators -------------------------------------------------------
     def window_table(self, n: int, bins: int, delta: float) -> np.ndarray:
@@ -365,21 +387,27 @@ class Context:
         (list of (k, coef) arrays, list of Stats dicts)."""
         nsig = len(sigs)
         caps = np.array([cap or (4 * o.k + 4096) for o in opts], np.int32)
-        ks = [np.zeros(int(cp), np.int32) for cp in caps]
-        cs = [np.zeros(int(cp), np.complex128) for cp in caps]
+        offs = np.zeros(nsig + 1, np.int64)
+        np.cumsum(caps, out=offs[1:])
+        total = int(offs[-1])
+        if self._out_k.size < total:
+            self._out_k = np.empty(total, np.int32)
+            self._out_c = np.empty(total, np.complex128)
         count = np.zeros(nsig, np.int32)
         stats = (Stats * nsig)()
         opt_arr = (SolveOptions * nsig)(*opts)
         sig_arr = (ctypes.c_void_p * nsig)(*[s._h.value for s in sigs])
         rng_arr = (ctypes.c_void_p * nsig)(*[r._h.value for r in rngs])
-        k_arr = (ctypes.c_void_p * nsig)(*[a.ctypes.data for a in ks])
-        c_arr = (ctypes.c_void_p * nsig)(*[a.ctypes.data for a in cs])
+        kb, cb = self._out_k.ctypes.data, self._out_c.ctypes.data
+        k_arr = (ctypes.c_void_p * nsig)(*(kb + 4 * offs[:-1]).tolist())
+        c_arr = (ctypes.c_void_p * nsig)(*(cb + 16 * offs[:-1]).tolist())
         rc = self._lib.mpsft_solve_batched(
             self._h, sig_arr, opt_arr, nsig, rng_arr, k_arr, c_arr, _ptr(caps),
             _ptr(count), stats)
         if raise_on_error:
             _check(self, rc)
-        out = [(ks[i][:count[i]], cs[i][:count[i]]) for i in range(nsig)]
+        out = [(self._out_k[o:o + c].copy(), self._out_c[o:o + c].copy())
+               for o, c in zip(offs[:-1].tolist(), count.tolist())]
         return out, [stats[i].as_dict() for i in range(nsig)]
 
 

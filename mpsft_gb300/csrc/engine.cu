@@ -662,6 +662,57 @@ void FillDraws(mpsft_rng *rng, int32_t n, int32_t trials, int stride,
   }
 }
 
+// Host side of the solve graph's draw tables: the first kDrawChunk
+// iterations' draws of every signal, its initial device state (SolveCtl) and
+// the RNG states to rewind to. Filled while the GPU computes the signal
+// energies (nothing here depends on them; force_fp64 is set afterwards).
+struct DrawTables {
+  int tmax = 1, stride = 5;
+  size_t bq_per = 0;
+  std::vector<SolveCtl> hc;
+  std::vector<int32_t> hd;
+  std::vector<double> hb;
+  std::vector<mpsft_rng> saved;
+};
+
+void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                  const mpsft_solve_options *opts, int nsig,
+                  mpsft_rng *const *rngs, bool fp64, DrawTables *dt) {
+  dt->tmax = 1;
+  for (int i = 0; i < nsig; ++i) dt->tmax = std::max(dt->tmax, opts[i].trials);
+  const int stride = dt->stride = 4 + dt->tmax;
+  dt->bq_per = size_t(kDrawChunk) * dt->tmax * 2;
+  dt->hc.assign(nsig, SolveCtl{});
+  dt->hd.assign(size_t(nsig) * kDrawChunk * stride, 0);
+  dt->hb.assign(nsig * dt->bq_per, 0.0);
+  dt->saved.resize(nsig);
+  for (int i = 0; i < nsig; ++i) {
+    const mpsft_solve_options &o = opts[i];
+    SolveCtl &c = dt->hc[i];
+    std::memset(&c, 0, sizeof(c));
+    c.k = o.k;
+    c.min_bins = o.min_bins;
+    c.trials = o.trials;
+    c.draw_stride = stride;
+    c.max_stale = o.max_stale_iter;
+    c.max_iter = o.max_iter > 0 ? o.max_iter : 64 + 8 * o.k;
+    c.fp64_path = fp64 ? 1 : 0;
+    c.sigma = o.sigma;
+    c.sqrt_c_delta = std::sqrt(-std::log(o.window_delta));
+    c.win_thr = o.window_threshold;
+    c.margin = o.near_tie_margin > 0 ? o.near_tie_margin : kDefaultNearTieMargin;
+    c.draws = ctx->d_draws + size_t(i) * kDrawChunk * stride;
+    c.draw_bq = ctx->d_draw_bq + i * dt->bq_per;
+    c.draw_base = 0;
+    c.draws_avail = kDrawChunk;
+    c.last_bins = -1;
+    dt->saved[i] = *rngs[i];
+    FillDraws(rngs[i], int32_t(sigs[i]->n), o.trials, stride,
+              dt->hd.data() + size_t(i) * kDrawChunk * stride,
+              dt->hb.data() + i * dt->bq_per);
+  }
+}
+
 // The solve as a CUDA graph: a while node whose body is one iteration of
 // every signal (k_plan, the iteration kernels, k_finish). The host only
 // refills draw tables; the loop ends when every signal has stopped. The RNGs
@@ -669,13 +720,12 @@ void FillDraws(mpsft_rng *rng, int32_t n, int32_t trials, int stride,
 int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
               const mpsft_solve_options *opts, int nsig,
               mpsft_rng *const *rngs, const std::vector<Shape> &shapes,
-              SigIter *d_its, std::vector<SigIter> *its,
+              SigIter *d_its, std::vector<SigIter> *its, DrawTables *dt,
               const std::vector<int32_t> &force, bool any_forced, bool fp64,
               bool x_c128, int64_t *launches) {
-  int tmax = 1;
+  const int tmax = dt->tmax;
   Maxima mx;
   for (int i = 0; i < nsig; ++i) {
-    tmax = std::max(tmax, opts[i].trials);
     const Shape &s = shapes[i];
     mx.bins = std::max(mx.bins, s.bins_cap);
     mx.bits = std::max(mx.bits, (s.rows_cap - 1) / 2);
@@ -685,7 +735,7 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     mx.cap = std::max(mx.cap, s.tab_cap);
   }
   mx.trials = tmax;
-  const int stride = 4 + tmax;
+  const int stride = dt->stride;
   // static fields of the iteration descriptors (k_plan fills the rest)
   for (int i = 0; i < nsig; ++i) {
     SigIter &it = (*its)[i];
@@ -702,36 +752,12 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its->data(), sizeof(SigIter) * nsig,
                                   cudaMemcpyHostToDevice, ctx->stream));
-  std::vector<SolveCtl> hc(nsig);
-  std::vector<int32_t> hd(size_t(nsig) * kDrawChunk * stride, 0);
-  const size_t bq_per = size_t(kDrawChunk) * tmax * 2;
-  std::vector<double> hb(nsig * bq_per, 0.0);
-  std::vector<mpsft_rng> saved(nsig);
-  for (int i = 0; i < nsig; ++i) {
-    const mpsft_solve_options &o = opts[i];
-    SolveCtl &c = hc[i];
-    std::memset(&c, 0, sizeof(c));
-    c.k = o.k;
-    c.min_bins = o.min_bins;
-    c.trials = o.trials;
-    c.draw_stride = stride;
-    c.max_stale = o.max_stale_iter;
-    c.max_iter = o.max_iter > 0 ? o.max_iter : 64 + 8 * o.k;
-    c.fp64_path = fp64 ? 1 : 0;
-    c.force_fp64 = force[i];
-    c.sigma = o.sigma;
-    c.sqrt_c_delta = std::sqrt(-std::log(o.window_delta));
-    c.win_thr = o.window_threshold;
-    c.margin = o.near_tie_margin > 0 ? o.near_tie_margin : kDefaultNearTieMargin;
-    c.draws = ctx->d_draws + size_t(i) * kDrawChunk * stride;
-    c.draw_bq = ctx->d_draw_bq + i * bq_per;
-    c.draw_base = 0;
-    c.draws_avail = kDrawChunk;
-    c.last_bins = -1;
-    saved[i] = *rngs[i];
-    FillDraws(rngs[i], int32_t(sigs[i]->n), o.trials, stride,
-              hd.data() + size_t(i) * kDrawChunk * stride, hb.data() + i * bq_per);
-  }
+  std::vector<SolveCtl> &hc = dt->hc;
+  std::vector<int32_t> &hd = dt->hd;
+  std::vector<double> &hb = dt->hb;
+  const std::vector<mpsft_rng> &saved = dt->saved;
+  const size_t bq_per = dt->bq_per;
+  for (int i = 0; i < nsig; ++i) hc[i].force_fp64 = force[i];
   MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draws, hd.data(), sizeof(int32_t) * hd.size(),
                                   cudaMemcpyHostToDevice, ctx->stream));
   MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draw_bq, hb.data(), sizeof(double) * hb.size(),
@@ -1007,7 +1033,9 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                   cudaMemcpyHostToDevice, ctx->stream));
   LaunchClearTables(d_its, nsig, max_cap, ctx->stream);
   LaunchPhaseTables(d_its, nsig, phase_entries, ctx->stream);
+  bool host_loop = ctx->profiling || ctx->graph_unavailable;
   std::vector<double> energy(nsig, 0.0);
+  DrawTables draws;
   if (!fp64) {
     // mean |x|^2 of every signal scales the FP32 near-tie margin
     std::vector<const void *> h_xs(nsig);
@@ -1021,8 +1049,15 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_ns, h_ns.data(), sizeof(int64_t) * nsig,
                                     cudaMemcpyHostToDevice, ctx->stream));
     LaunchEnergy(d_xs, d_ns, nsig, x_c128, d_energy, ctx->stream);
+    // the host's share of the solve graph runs while the GPU reads x
+    if (!host_loop) PrepareDraws(ctx, sigs, opts, nsig, rngs, fp64, &draws);
     rc = ReadEnergy(ctx, d_energy, nsig, &energy);
-    if (rc) return rc;
+    if (rc) {
+      for (int i = 0; i < int(draws.saved.size()); ++i) *rngs[i] = draws.saved[i];
+      return rc;
+    }
+  } else if (!host_loop) {
+    PrepareDraws(ctx, sigs, opts, nsig, rngs, fp64, &draws);
   }
   // precision policy, once per solve (FP32 calls)
   std::vector<int32_t> force(nsig, 0);
@@ -1045,11 +1080,10 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   std::vector<Run> run(nsig);
   BinTimer timer{ctx};
   int64_t launches = 0;
-  bool host_loop = ctx->profiling || ctx->graph_unavailable;
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
   if (!host_loop) {
-    rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, &its, force,
-                   any_forced, fp64, x_c128, &launches);
+    rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, &its, &draws,
+                   force, any_forced, fp64, x_c128, &launches);
     if (rc == kGraphUnavailable) {
       // no iteration ran and the tables are untouched; the RNGs are back
       // where they were
@@ -1445,6 +1479,33 @@ int mpsft_signal_write(mpsft_ctx *ctx, mpsft_signal *sig, const void *x_host) {
   const size_t bytes = size_t(sig->n) * (sig->dtype == MPSFT_C64 ? 8 : 16);
   MPSFT_CUDA(ctx, cudaMemcpyAsync(sig->d_x, x_host, bytes, cudaMemcpyHostToDevice,
                                   ctx->stream));
+  return MPSFT_OK;
+}
+
+int mpsft_signal_write_many(mpsft_ctx *ctx, mpsft_signal *const *sigs,
+                            const void *const *x_host, int32_t count,
+                            void *stream) {
+  if (!ctx || count < 0 || (count > 0 && (!sigs || !x_host))) {
+    return MPSFT_ERR_INVALID;
+  }
+  for (int32_t i = 0; i < count; ++i) {
+    if (!sigs[i] || !x_host[i] || sigs[i]->ctx != ctx) return MPSFT_ERR_INVALID;
+  }
+  // the calling thread may not have selected the context's device
+  if (cudaSetDevice(ctx->device) != cudaSuccess) {
+    cudaGetLastError();
+    return MPSFT_ERR_CUDA;
+  }
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  for (int32_t i = 0; i < count; ++i) {
+    const mpsft_signal *sig = sigs[i];
+    const size_t bytes = size_t(sig->n) * (sig->dtype == MPSFT_C64 ? 8 : 16);
+    if (cudaMemcpyAsync(sig->d_x, x_host[i], bytes, cudaMemcpyHostToDevice, st) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return MPSFT_ERR_CUDA;
+    }
+  }
   return MPSFT_OK;
 }
 

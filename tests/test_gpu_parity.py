@@ -209,6 +209,68 @@ def test_batched_equals_single(ctx):
         assert st["status"] == 0
 
 
+def test_write_many_pipelined(ctx):
+    """Two signal sets alternating as a serving loop runs them: a second host
+    thread refills one set from pinned memory on a copy stream (one
+    mpsft_signal_write_many call) while the context solves the other; every
+    step returns exactly what a solve of freshly uploaded signals returns."""
+    import threading
+
+    import torch
+    from mpsft_gb300.signals import make_signal
+
+    n, S = 1 << 16, 40
+    steps = [[make_signal(n, S, 900 + 4 * s + i, sigma=1e-5) for i in range(4)]
+             for s in range(4)]
+    opts = [ctx.solve_options(S, sg.sigma, min_bins=51, window_delta=1e-5,
+                              max_stale_iter=5) for sg in steps[0]]
+    want = []
+    for batch in steps:
+        up = [ctx.upload(sg.x) for sg in batch]
+        want.append(ctx.solve_batched(up, [m.Rng(60 + i) for i in range(4)], opts)[0])
+        for sg in up:
+            sg.free()
+    pinned = []
+    for batch in steps:
+        row = []
+        for sg in batch:
+            t = torch.empty(n, dtype=torch.complex64, pin_memory=True)
+            t.numpy()[:] = sg.x
+            row.append(t.numpy())
+        pinned.append(row)
+    sets = [[ctx.upload(np.zeros(n, np.complex64)) for _ in range(4)] for _ in range(2)]
+    copy_stream = torch.cuda.Stream()
+    ready = [torch.cuda.Event(), torch.cuda.Event()]
+
+    def write_set(j, s):
+        ctx.write_many(sets[j], pinned[s], copy_stream.cuda_stream)
+        ready[j].record(copy_stream)
+
+    solve_stream = torch.cuda.Stream()
+    ctx.set_stream(solve_stream.cuda_stream)
+    try:
+        write_set(0, 0)
+        for s in range(len(steps)):
+            cur = s % 2
+            solve_stream.wait_event(ready[cur])
+            th = None
+            if s + 1 < len(steps):
+                th = threading.Thread(target=write_set, args=(1 - cur, s + 1))
+                th.start()
+            got, stats = ctx.solve_batched(sets[cur], [m.Rng(60 + i) for i in range(4)],
+                                           opts)
+            if th is not None:
+                th.join()
+            for (k, c), (k0, c0), st in zip(got, want[s], stats):
+                assert st["status"] == 0
+                assert np.array_equal(k, k0)
+                assert np.array_equal(c.view(np.uint64), c0.view(np.uint64))
+    finally:
+        ctx.set_stream(None)
+    with pytest.raises(ValueError):
+        ctx.write_many(sets[0][:1], [np.zeros(n, np.complex128)])
+
+
 @pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
 def test_deterministic(ctx, prec):
     from mpsft_gb300.signals import make_signal
