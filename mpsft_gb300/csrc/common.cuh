@@ -92,7 +92,10 @@ struct SigIter {
   float2 *wtff;         // wt64 as float-float (hi, lo); may be null
   void *fold;           // FP32: float2, FP64: double2
   double2 *ubuf;
-  int32_t bins_cap;     // row stride of fold / ubuf
+  // solves and iterations on the FP32 path: the FP32 pass's bins (the row
+  // FFT writes here instead of ubuf, which then holds only FP64 bins)
+  float2 *ubuf32;
+  int32_t bins_cap;     // row stride of fold / ubuf / ubuf32
   // Bluestein tables: chirp = e^{-pi i k^2 / bins} (bins entries) and
   // chat = FFT of the conjugate chirp sequence (fft_m entries), FP32 and FP64
   float2 *chirp32, *chat32;

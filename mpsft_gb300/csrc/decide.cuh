@@ -16,6 +16,7 @@ template <typename T> struct Ops;
 template <> struct Ops<float> {
   using V = float2;
   __device__ static V from(double2 d) { return make_float2(float(d.x), float(d.y)); }
+  __device__ static V from(float2 f) { return f; }
   __device__ static V phase(const SigIter &it, int64_t m) { return Phase32(it, m); }
   // row-0 terms of a found mode, from k_mode_prep's FP32 copies
   template <int TMAX>
@@ -101,6 +102,19 @@ struct FromBins {
   }
 };
 
+// Bin values of the FP32 pass at bin beta: complex64 from ubuf32 in solves
+// and iterations, else the complex128 bins.
+struct FromBins32 {
+  const SigIter &it;
+  int beta;
+  __device__ float2 get(int t, int r) const {
+    const size_t i = (size_t(t) * it.rows + r) * it.bins_cap + beta;
+    if (it.ubuf32 != nullptr) return it.ubuf32[i];
+    const double2 d = it.ubuf[i];
+    return make_float2(float(d.x), float(d.y));
+  }
+};
+
 // Bin values of listed bin e: rows re-binned in FP64 (the chunk partial sums
 // in their fixed order), the other rows from the FP32 pass.
 struct FromRebin {
@@ -109,7 +123,12 @@ struct FromRebin {
   uint32_t mask;
   __device__ double2 get(int t, int r) const {
     if (!RowListed(mask, r)) {
-      return it.ubuf[(size_t(t) * it.rows + r) * it.bins_cap + beta];
+      const size_t i = (size_t(t) * it.rows + r) * it.bins_cap + beta;
+      if (it.ubuf32 != nullptr) {
+        const float2 f = it.ubuf32[i];
+        return make_double2(f.x, f.y);
+      }
+      return it.ubuf[i];
     }
     return __ldcg(&it.esc_sum[(size_t(e) * it.trials + t) * it.rows + r]);
   }

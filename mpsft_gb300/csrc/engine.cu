@@ -27,10 +27,17 @@ struct mpsft_ctx {
   int device = 0;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
-  // second stream for the kernels of an iteration that do not depend on the
-  // gather/fold (tables, mode preparation and bucketing)
+  // second stream, at the highest priority, for the kernels of an iteration
+  // that do not depend on the gather/fold (tables, mode preparation and
+  // bucketing): their few blocks go ahead of the fold's many, so that the
+  // FFT and the decisions do not wait for them
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // third stream, at the lowest priority, for the FP64 window tables (only
+  // the near-tie re-binning and the FP64 kernels use them): FP64
+  // transcendentals, slow on this part, that fill SMs the fold leaves idle
+  cudaStream_t side64 = nullptr;
+  cudaEvent_t ev_join64 = nullptr;
   cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
   // stream the solve graph is captured on, and the last instantiated graph
   cudaStream_t cap = nullptr;
@@ -287,6 +294,7 @@ struct Shape {
   int32_t n = 0, bins_cap = 0, rows_cap = 0, trials = 1, p2_cap = 0;
   int32_t m_cap = 0, tab_cap = 0;
   bool fp64 = false;
+  bool fp32_bins = false;  // FP32 pass bins in ubuf32 (solves, iterations)
 };
 
 void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
@@ -297,6 +305,7 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   // 16-byte cells: the FP32 path may redo an iteration in FP64
   it->fold = cv.take<double2>(cells);
   it->ubuf = cv.take<double2>(cells);
+  it->ubuf32 = s.fp32_bins ? cv.take<float2>(cells) : nullptr;
   it->row_max = cv.take<float>(size_t(s.trials) * s.rows_cap);
   it->chirp32 = cv.take<float2>(s.bins_cap);
   it->chat32 = cv.take<float2>(s.m_cap);
@@ -528,14 +537,18 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   // the window and the gather/fold run on the main one
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-  // FP32 path: the FP64 window tables (for the near-tie re-binning and the
-  // FP64 kernels) are built on the side stream; the binning uses an FP32
-  // evaluation
-  if (!fp64) LaunchWindow64(d_its, nsig, mx.p2, ctx->side);
   LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
   LaunchModePrep(d_its, nsig, mx.cap, ctx->side);
   LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+  // FP32 path: the FP64 window tables (for the near-tie re-binning and the
+  // FP64 kernels) are built on the low-priority stream and joined only
+  // before the re-binning; the binning uses an FP32 evaluation
+  if (!fp64) {
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side64, ctx->ev_fork, 0));
+    LaunchWindow64(d_its, nsig, mx.p2, ctx->side64);
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join64, ctx->side64));
+  }
   if (fp64) {
     LaunchWindow(d_its, nsig, mx.p2, s);
   } else {
@@ -561,6 +574,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     // FP64; signals that the precision policy sends to FP64 (and signals
     // whose near-tie list overflowed) run the FP64 kernels
     const bool redo = any_forced && mx.m <= kMaxFFT64;
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join64, 0));
     LaunchRebin(d_its, nsig, kMaxListed, x_c128, false, s);
     LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
     if (launched) *launched += 2;  // re-binning, FP64 decisions
@@ -850,7 +864,10 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
     cudaGraphExec_t exec = nullptr;
     cudaError_t ie = cudaErrorUnknown;
-    if (rc == MPSFT_OK && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, g, 0);
+    // the side stream's priority was captured into its kernel nodes
+    if (rc == MPSFT_OK && ce == cudaSuccess) {
+      ie = cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
+    }
     if (rc != MPSFT_OK || ce != cudaSuccess || ie != cudaSuccess) {
       // no graph on this device / driver: the host loop takes over
       cudaGetLastError();
@@ -982,6 +999,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       return Fail(ctx, MPSFT_ERR_INVALID, "mode table larger than 32768 slots");
     }
     s.fp64 = fp64;
+    s.fp32_bins = !fp64;
     Carve probe{nullptr};
     SigIter dummy{};
     int32_t *ctl = nullptr;
@@ -1300,12 +1318,24 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   ctx->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking);
+  int prio_least = 0, prio_greatest = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  if (e == cudaSuccess) {
+    e = cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, prio_greatest);
+  }
+  if (e == cudaSuccess) {
+    e = cudaStreamCreateWithPriority(&ctx->side64, cudaStreamNonBlocking, prio_least);
+  }
+  // the solve graph's main chain sits between the two side streams
+  if (e == cudaSuccess) {
+    e = cudaStreamCreateWithPriority(&ctx->cap, cudaStreamNonBlocking,
+                                     (prio_least + prio_greatest) / 2);
+  }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop1);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join64, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
   if (e != cudaSuccess) {
@@ -1341,6 +1371,10 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->tw32) cudaFree(ctx->tw32);
   if (ctx->tw64) cudaFree(ctx->tw64);
+  if (ctx->side64) {
+    cudaStreamSynchronize(ctx->side64);
+    cudaStreamDestroy(ctx->side64);
+  }
   if (ctx->side) {
     cudaStreamSynchronize(ctx->side);
     cudaStreamDestroy(ctx->side);
@@ -1352,6 +1386,7 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->ev_loop0) cudaEventDestroy(ctx->ev_loop0);
   if (ctx->ev_loop1) cudaEventDestroy(ctx->ev_loop1);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->ev_join64) cudaEventDestroy(ctx->ev_join64);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return MPSFT_OK;
@@ -1951,6 +1986,7 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
     return Fail(ctx, MPSFT_ERR_CAPACITY, "mode map larger than the table");
   }
   s.fp64 = fp64;
+  s.fp32_bins = !fp64;
   Carve probe{nullptr};
   SigIter it{};
   int32_t *ctl;

@@ -160,17 +160,27 @@ __global__ void __launch_bounds__(256)
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
   const int beta = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (beta >= it.bins) return;
-  const int e = DecideBin<T, TMAX>(it, beta, FromBins{it, beta}, mode);
+  int e;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    e = DecideBin<T, TMAX>(it, beta, FromBins32{it, beta}, mode);
+  } else {
+    e = DecideBin<T, TMAX>(it, beta, FromBins{it, beta}, mode);
+  }
   // a listed near tie: its re-binning's tables (after the decision, when few
   // registers are live)
   if (e >= 0) PrepListedBin(it, e, beta, threadIdx.x & 31);
 }
 
-// One warp per listed near-tie bin: FP64 decision on the re-binned values.
-// Signals whose list overflowed are redone whole instead (redo), or marked
-// unresolved.
+// FP64 decisions on the re-binned values of the listed near-tie bins.
+// Single-warp blocks, kListedWarps per signal, each taking every
+// kListedWarps-th listed bin: a decision is a long chain of FP64 operations,
+// and GB300's few FP64 pipes per SM are best shared by few such warps, so the
+// listed bins spread over the SMs. Signals whose list overflowed are redone
+// whole instead (redo), or marked unresolved.
+constexpr int kListedWarps = 8;
+
 template <int TMAX>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32)
     k_decide_listed(const SigIter *__restrict__ its, int redo) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
@@ -182,11 +192,11 @@ __global__ void __launch_bounds__(256)
     }
     return;
   }
-  const int e = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (e >= nf) return;
-  const int beta = it.esc_list[e];
-  DecideBin<double, TMAX>(it, beta, FromRebin{it, e, beta, it.esc_mask[e]},
-                          kDecideExact);
+  for (int e = blockIdx.x; e < nf; e += kListedWarps) {
+    const int beta = it.esc_list[e];
+    DecideBin<double, TMAX>(it, beta, FromRebin{it, e, beta, it.esc_mask[e]},
+                            kDecideExact);
+  }
 }
 
 // ---------------------------------------------------------------- merge
@@ -392,14 +402,14 @@ void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
 
 void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
                         bool redo, cudaStream_t s) {
-  dim3 grid((kMaxListed + 7) / 8, nsig);
+  dim3 grid(kListedWarps, nsig);
   const int r = redo ? 1 : 0;
   if (max_trials <= 1) {
-    k_decide_listed<1><<<grid, 256, 0, s>>>(d_its, r);
+    k_decide_listed<1><<<grid, 32, 0, s>>>(d_its, r);
   } else if (max_trials <= 5) {
-    k_decide_listed<5><<<grid, 256, 0, s>>>(d_its, r);
+    k_decide_listed<5><<<grid, 32, 0, s>>>(d_its, r);
   } else {
-    k_decide_listed<kMaxTrials><<<grid, 256, 0, s>>>(d_its, r);
+    k_decide_listed<kMaxTrials><<<grid, 32, 0, s>>>(d_its, r);
   }
 }
 
@@ -436,7 +446,7 @@ bool DecideKernelsLaunchable() {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_decide<double, kMaxTrials>, 256, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_decide<float, kMaxTrials>, 256, 0);
   int l = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, k_decide_listed<kMaxTrials>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, k_decide_listed<kMaxTrials>, 32, 0);
   return a > 0 && b > 0 && c > 0 && l > 0;
 }
 

@@ -6,7 +6,11 @@
 //
 // One CTA per (row, trial, signal). FP32 path: the convolution runs in FP32
 // (M <= 16384 points, 128 KB of shared memory); FP64 path: in FP64
-// (M <= 8192).
+// (M <= 8192). In solves and iterations the FP32 path writes complex64 bins
+// (ubuf32) and keeps the FP64 pipes out of the epilogue (GB300 issues FP64
+// at a small fraction of its FP32 rate, with long latencies): the row factor
+// is applied as a float-float value, and each product is formed with exact
+// FMA products and a two-sum, then rounded once to FP32.
 #include <algorithm>
 
 #include "fft.cuh"
@@ -20,6 +24,26 @@ __device__ inline const float2 *ChirpOf(const SigIter &it, float2 *) { return it
 __device__ inline const double2 *ChirpOf(const SigIter &it, double2 *) { return it.chirp64; }
 __device__ inline const float2 *ChatOf(const SigIter &it, float2 *) { return it.chat32; }
 __device__ inline const double2 *ChatOf(const SigIter &it, double2 *) { return it.chat64; }
+
+// y * (bh + bl) rounded to FP32 (bh + bl: a unit phase as float-float):
+// the high products exactly (FMA residuals), a two-sum of the pair, then the
+// residuals and the low-word products, one final rounding.
+__device__ __forceinline__ float DotRound(float x0, float y0, float x1, float y1,
+                                          float l0, float l1) {
+  // x0 y0 + x1 y1 + (x0 l0 + x1 l1)
+  const float p0 = __fmul_rn(x0, y0), e0 = fmaf(x0, y0, -p0);
+  const float p1 = __fmul_rn(x1, y1), e1 = fmaf(x1, y1, -p1);
+  const float s = __fadd_rn(p0, p1);
+  const float bb = __fsub_rn(s, p0);
+  const float es = __fadd_rn(__fsub_rn(p0, __fsub_rn(s, bb)), __fsub_rn(p1, bb));
+  const float lo = __fadd_rn(__fadd_rn(es, __fadd_rn(e0, e1)),
+                             fmaf(x0, l0, __fmul_rn(x1, l1)));
+  return __fadd_rn(s, lo);
+}
+__device__ __forceinline__ float2 MulPhaseFF(float2 y, float2 bh, float2 bl) {
+  return make_float2(DotRound(y.x, bh.x, -y.y, bh.y, bl.x, bl.y),
+                     DotRound(y.x, bh.y, y.y, bh.x, bl.y, bl.x));
+}
 
 // cond: only signals whose iteration is redone in FP64 take part. Also
 // records the largest |U| of each row (used by the FP32 near-tie bound).
@@ -56,6 +80,17 @@ __global__ void __launch_bounds__(kRowFftThreads)
   const V *__restrict__ chirp = ChirpOf(it, (V *)nullptr);
   const V *__restrict__ chat = ChatOf(it, (V *)nullptr);
   if (threadIdx.x < kRowsMax) row_max_bits[threadIdx.x] = 0u;
+  // the trial's row factor as float-float for the complex64 epilogue (read
+  // after the transforms' barriers)
+  __shared__ float2 bq_ff[2];
+  const bool out32 = sizeof(V) == sizeof(float2) && it.ubuf32 != nullptr;
+  if (out32 && threadIdx.x == 0) {
+    const double br = it.bq_re[tr], bi = it.bq_im[tr];
+    const float hr = __double2float_rn(br), hi = __double2float_rn(bi);
+    bq_ff[0] = make_float2(hr, hi);
+    bq_ff[1] = make_float2(__double2float_rn(br - double(hr)),
+                           __double2float_rn(bi - double(hi)));
+  }
   // element loops: up to 8 elements per thread with their loads issued
   // together (a thread covers M / nth elements)
   if (live) {
@@ -99,7 +134,32 @@ __global__ void __launch_bounds__(kRowFftThreads)
   }
   __syncthreads();
   BlockFFTDit(a, live ? M : 0, it.fft_log2m, tw, true, tid, nth);
-  if (live) {
+  if (live && out32) {
+    // FP32 bins: exact power-of-two scale, float-float row factor
+    const float inv_mf = 1.0f / float(M);
+    const float2 bh = bq_ff[0], bl = bq_ff[1];
+    float2 *dst = it.ubuf32 + (size_t(tr) * it.rows + row) * it.bins_cap;
+    float mx = 0.f;
+    for (int k0 = tid; k0 < B; k0 += 8 * nth) {
+      V w[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u * nth;
+        if (k < B) w[u] = __ldg(&chirp[k]);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u * nth;
+        if (k < B) {
+          const V z = vmul(a[Pad(k)], w[u]);
+          const float2 y = make_float2(float(z.x) * inv_mf, float(z.y) * inv_mf);
+          dst[k] = MulPhaseFF(y, bh, bl);
+          mx = fmaxf(mx, sqrtf(y.x * y.x + y.y * y.y));
+        }
+      }
+    }
+    atomicMax(&row_max_bits[lr], __float_as_uint(mx));
+  } else if (live) {
     const double inv_m = 1.0 / double(M);
     const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
     double2 *dst = it.ubuf + (size_t(tr) * it.rows + row) * it.bins_cap;
