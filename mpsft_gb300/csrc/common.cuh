@@ -151,9 +151,13 @@ struct SigIter {
   // FP32 path only: 1 when this signal's FP32 rounding is not small against
   // its noise thresholds, so this iteration runs on the FP64 kernels
   int32_t force_fp64;
-  // 1 when the window and FP32 Bluestein tables of the previous iteration
-  // (same number of bins) are still valid
+  // 1 when the window and FP32 Bluestein tables for this iteration's bins are
+  // in place (the previous iteration's, the context's table cache, or built
+  // in this iteration by another signal of the batch): the table kernels skip
+  // this signal
   int32_t tables_valid;
+  // table cache slot (bins >> 1) this signal builds in this iteration, or -1
+  int32_t win_slot;
   int32_t *esc_list;    // esc_cap bins
   uint32_t *esc_mask;   // per listed bin: bit s set = rows 2s+1, 2s+2 near
   int32_t esc_cap;
@@ -183,7 +187,30 @@ struct SolveCtl {
   int32_t iter, stale, done, status, last_bins;
   int32_t near_ties, unresolved, fp64_iters;
   int64_t gathers, bin_bytes;
+  // the context's table cache (null: per-signal tables): per odd bins B,
+  // block win_base[B >> 1] of win_pool holds wt32, wt64, wtff (p2 + 1
+  // entries each), chirp32 (B) and chat32 (M), each 16-byte aligned;
+  // win_valid marks built blocks, win_claim elects one builder per block
+  const int64_t *win_base;
+  unsigned char *win_pool;
+  int32_t *win_valid, *win_claim;
 };
+
+// Byte offsets of the tables inside a table-cache block.
+struct WinBlock {
+  int64_t wt64, wtff, chirp32, chat32, bytes;
+};
+__host__ __device__ inline int64_t Align16(int64_t v) { return (v + 15) & ~int64_t(15); }
+__host__ __device__ inline WinBlock WinBlockOf(int32_t p2, int32_t bins, int32_t m) {
+  WinBlock w;
+  const int64_t e = int64_t(p2) + 1;
+  w.wt64 = Align16(4 * e);
+  w.wtff = w.wt64 + Align16(8 * e);
+  w.chirp32 = w.wtff + Align16(8 * e);
+  w.chat32 = w.chirp32 + Align16(8 * int64_t(bins));
+  w.bytes = w.chat32 + Align16(8 * int64_t(m));
+  return w;
+}
 
 // ---------------------------------------------------------------- helpers
 __host__ __device__ inline int64_t PosMod(int64_t v, int64_t n) {

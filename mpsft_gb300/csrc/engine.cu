@@ -64,6 +64,14 @@ struct mpsft_ctx {
   unsigned char *h_stage = nullptr;
   size_t h_stage_n = 0;
   std::vector<cudaEvent_t> events;
+  // table cache of FP32 solves: window tables (FP32, FP64, float-float) and
+  // FP32 Bluestein tables per odd number of bins for one window delta, built
+  // on first use and kept, like FFT plans (win_dev: block offsets, valid and
+  // claim words, then the pool)
+  unsigned char *win_dev = nullptr;
+  size_t win_bytes = 0;
+  double win_delta = 0.0;
+  int32_t win_bmin = 0, win_bmax = 0;
 };
 
 struct mpsft_signal {
@@ -388,6 +396,71 @@ int EnsureHostStage(mpsft_ctx *ctx, size_t bytes) {
   ctx->h_stage_n = 0;
   MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_stage, bytes));
   ctx->h_stage_n = bytes;
+  return MPSFT_OK;
+}
+
+// Table cache for odd bins in [bmin, bmax] and window delta (see mpsft_ctx);
+// *out gets the device pointers, or nulls when the cache would exceed its
+// budget (the solve then builds per-signal tables).
+constexpr size_t kWinCacheBudget = size_t(1) << 30;
+struct WinCacheRefs {
+  const int64_t *base = nullptr;
+  unsigned char *pool = nullptr;
+  int32_t *valid = nullptr, *claim = nullptr;
+};
+
+int EnsureWinCache(mpsft_ctx *ctx, double delta, int32_t bmin, int32_t bmax,
+                   WinCacheRefs *out) {
+  *out = WinCacheRefs{};
+  const bool fits = ctx->win_dev && ctx->win_delta == delta &&
+                    bmin >= ctx->win_bmin && bmax <= ctx->win_bmax;
+  if (!fits) {
+    if (ctx->win_dev && ctx->win_delta == delta) {
+      bmin = std::min(bmin, ctx->win_bmin);
+      bmax = std::max(bmax, ctx->win_bmax);
+    }
+    const int32_t h_n = (bmax >> 1) + 1;
+    std::vector<int64_t> base(h_n, 0);
+    int64_t pool = 0;
+    for (int32_t b = bmin | 1; b <= bmax; b += 2) {
+      const WinParams w = MakeWindow(b, delta);
+      base[b >> 1] = pool;
+      pool += WinBlockOf(w.p2, b, 1 << FFTLog2(b)).bytes;
+    }
+    if (size_t(pool) > kWinCacheBudget) return MPSFT_OK;
+    const size_t head = size_t(Align16(8 * int64_t(h_n)) + 2 * Align16(4 * int64_t(h_n)));
+    const size_t bytes = head + size_t(pool);
+    if (ctx->win_dev) {
+      MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      cudaFree(ctx->win_dev);
+      ctx->win_dev = nullptr;
+      ctx->win_bytes = 0;
+    }
+    if (cudaMalloc(&ctx->win_dev, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->win_dev = nullptr;
+      return MPSFT_OK;  // no cache: per-signal tables
+    }
+    ctx->win_bytes = bytes;
+    ctx->win_delta = delta;
+    ctx->win_bmin = bmin;
+    ctx->win_bmax = bmax;
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->win_dev, base.data(), sizeof(int64_t) * h_n,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    MPSFT_CUDA(ctx, cudaMemsetAsync(ctx->win_dev + Align16(8 * int64_t(h_n)), 0,
+                                    2 * Align16(4 * int64_t(h_n)), ctx->stream));
+    // pageable source: complete before the vector goes away
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  const int32_t h_n = (ctx->win_bmax >> 1) + 1;
+  unsigned char *d = ctx->win_dev;
+  out->base = reinterpret_cast<const int64_t *>(d);
+  out->valid = reinterpret_cast<int32_t *>(d + Align16(8 * int64_t(h_n)));
+  out->claim = reinterpret_cast<int32_t *>(d + Align16(8 * int64_t(h_n)) +
+                                           Align16(4 * int64_t(h_n)));
+  out->pool = d + Align16(8 * int64_t(h_n)) + 2 * Align16(4 * int64_t(h_n));
+  // one builder per block and solve: claims start over
+  MPSFT_CUDA(ctx, cudaMemsetAsync(out->claim, 0, sizeof(int32_t) * h_n, ctx->stream));
   return MPSFT_OK;
 }
 
@@ -1098,6 +1171,31 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   std::vector<Run> run(nsig);
   BinTimer timer{ctx};
   int64_t launches = 0;
+  if (!host_loop && !fp64) {
+    // the FP32 tables from the context's cache when the batch shares one
+    // window delta
+    bool one_delta = true;
+    int32_t bmin = INT32_MAX, bmax = 1;
+    for (int i = 0; i < nsig; ++i) {
+      one_delta = one_delta && opts[i].window_delta == opts[0].window_delta;
+      bmin = std::min(bmin, std::min(shapes[i].bins_cap, opts[i].min_bins));
+      bmax = std::max(bmax, shapes[i].bins_cap);
+    }
+    WinCacheRefs wc;
+    if (one_delta) {
+      rc = EnsureWinCache(ctx, opts[0].window_delta, bmin, bmax, &wc);
+      if (rc) {
+        for (int i = 0; i < nsig; ++i) *rngs[i] = draws.saved[i];
+        return rc;
+      }
+    }
+    for (int i = 0; i < nsig; ++i) {
+      draws.hc[i].win_base = wc.base;
+      draws.hc[i].win_pool = wc.pool;
+      draws.hc[i].win_valid = wc.valid;
+      draws.hc[i].win_claim = wc.claim;
+    }
+  }
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
   if (!host_loop) {
     rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, &its, &draws,
@@ -1371,6 +1469,7 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->tw32) cudaFree(ctx->tw32);
   if (ctx->tw64) cudaFree(ctx->tw64);
+  if (ctx->win_dev) cudaFree(ctx->win_dev);
   if (ctx->side64) {
     cudaStreamSynchronize(ctx->side64);
     cudaStreamDestroy(ctx->side64);

@@ -107,7 +107,24 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     it.eps_rel = 0.f;
     it.eps_scale = 0.0;
   }
-  it.tables_valid = (c.last_bins == bins && !c.force_fp64) ? 1 : 0;
+  it.win_slot = -1;
+  if (c.win_base != nullptr && !c.force_fp64) {
+    // tables from the context's cache: built already, or built now by the
+    // one signal of the batch that claims the block
+    const int h = bins >> 1;
+    const WinBlock wb = WinBlockOf(it.p2, bins, it.fft_m);
+    unsigned char *blk = c.win_pool + c.win_base[h];
+    it.wt32 = reinterpret_cast<float *>(blk);
+    it.wt64 = reinterpret_cast<double *>(blk + wb.wt64);
+    it.wtff = reinterpret_cast<float2 *>(blk + wb.wtff);
+    it.chirp32 = reinterpret_cast<float2 *>(blk + wb.chirp32);
+    it.chat32 = reinterpret_cast<float2 *>(blk + wb.chat32);
+    const bool build = c.win_valid[h] == 0 && atomicCAS(&c.win_claim[h], 0, 1) == 0;
+    it.tables_valid = build ? 0 : 1;
+    if (build) it.win_slot = h;
+  } else {
+    it.tables_valid = (c.last_bins == bins && !c.force_fp64) ? 1 : 0;
+  }
   it.flags[0] = 0;
   it.flags[1] = 0;
   it.flags[2] = 0;
@@ -148,6 +165,9 @@ __global__ void __launch_bounds__(1024)
       }
       if (c.status != 0 || c.stale >= c.max_stale) c.done = 1;
       c.last_bins = it.force_fp64 ? -1 : it.bins;
+      // the tables this signal built are complete (every table kernel of
+      // the iteration has run)
+      if (it.win_slot >= 0) c.win_valid[it.win_slot] = 1;
       it.active = 0;
     }
     if (!c.done && c.iter - c.draw_base < c.draws_avail) {

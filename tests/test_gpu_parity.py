@@ -312,6 +312,31 @@ def test_graph_loop_equals_host_loop(ctx, prec):
     assert s1.escalated == s2.escalated and s1.status == s2.status == 0
 
 
+def test_table_cache_across_solves(ctx):
+    """The solve graph takes its window and Bluestein tables from the
+    context's cache (built on first use per number of bins and window delta):
+    solves that switch delta and bin range, and then repeat, give what the
+    host-driven loop (per-signal tables) gives, bit for bit."""
+    from mpsft_gb300.signals import make_signal
+
+    cases = [(1 << 16, 40, 1e-5, 51), (1 << 17, 90, 1e-6, 31), (1 << 16, 40, 1e-5, 51),
+             (1 << 16, 300, 1e-5, 51)]
+    for n, S, delta, mb in cases:
+        sg = make_signal(n, S, 40 + S, sigma=1e-5)
+        sig = ctx.upload(sg.x)
+        opt = ctx.solve_options(S, sg.sigma, min_bins=mb, window_delta=delta,
+                                max_stale_iter=5)
+        k1, c1, s1 = ctx.solve_arrays(sig, m.Rng(7), opt)
+        ctx.set_profiling(True)
+        try:
+            k2, c2, s2 = ctx.solve_arrays(sig, m.Rng(7), opt)
+        finally:
+            ctx.set_profiling(False)
+        assert s1.status == s2.status == 0
+        assert np.array_equal(k1, k2)
+        assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64))
+
+
 # ------------------------------------------------------------ error paths
 def test_errors_are_statuses(ctx):
     from mpsft_gb300.signals import make_signal
