@@ -161,16 +161,17 @@ __device__ inline int64_t RoundK1(int64_t n, int beta, uint32_t xs, int L, int B
   return int64_t(q) + (2 * r >= den ? 1 : 0);
 }
 
-// The bin loop body of Iterate for one bin (warp-wide). T = float: the FP32
-// path with near-tie detection, FP32 arithmetic only (GB300 runs FP64 at a
-// small fraction of its FP32 rate): a surviving bin leaves a pending
-// candidate (cand_valid = 2: k1 in cand_k0, the unscaled coefficient sum in
-// cand_coef, its error bound in cand_err) that the merge finishes in FP64 on
-// full warps. T = double: FP64 decisions to the end (the FP64 path, and the
-// near-tie bins after their re-binning).
-template <typename T, int TMAX, typename Src>
-__device__ int DecideBin(const SigIter &it, int beta, const Src &src,
-                          int mode) {
+// The decisions of a bin from its mode-subtracted values (the part of
+// DecideBin after the subtraction; also the listed bins' block-wide FP64
+// decision): non-finite check, IdentifyFreq, k1, coefficient. Returns the
+// near-tie list position (FP32) or listed.
+template <typename T, int TMAX>
+__device__ __forceinline__ int DecideTail(const SigIter &it, int beta, int mode,
+                                          const typename Ops<T>::V *u0,
+                                          const typename Ops<T>::V *up,
+                                          const typename Ops<T>::V *um,
+                                          float eps_base, float rml, bool e_near,
+                                          int listed) {
   using O = Ops<T>;
   using V = typename O::V;
   const int lane = threadIdx.x & 31;
@@ -179,178 +180,7 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
   const int B = it.bins;
   const bool has_bit = lane < L;
   const bool fp32 = sizeof(T) == 4;
-  const int nm = it.bkt_count[beta];
-  const int st = it.bkt_start[beta];
-  int listed = -1;  // list position when this bin is listed as a near tie
-
-  // ---- row 0 and its mode subtraction (the bin's modes are in increasing k0).
-  // The first 32 modes are loaded once, one per lane, and shared by shuffles
-  // (the common case); further modes are read directly.
-  V u0[TMAX];
-#pragma unroll
-  for (int t = 0; t < TMAX; ++t) {
-    if (t < TR) u0[t] = O::from(src.get(t, 0));
-  }
-  const int npre = min(nm, 32);
-  V pre_base[TMAX];
-  float mode_err = 0.f;  // FP32 error carried into this bin by the found modes
-  int pre_k1 = 0;  // k1 of the lane's mode (row factors below)
-  if (lane < npre) {
-    const int sl = it.bkt_list[st + lane];
-    O::template terms<TMAX>(it, sl, pre_base);
-    pre_k1 = it.mode_k1[sl];
-    if (fp32) mode_err = it.mode_errw[sl];
-  }
-  for (int i = 0; i < nm; ++i) {
-    V bs[TMAX];
-    if (i < 32) {
-#pragma unroll
-      for (int t = 0; t < TMAX; ++t) {
-        if (t < TR) {
-          bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
-          bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
-        }
-      }
-    } else {
-      const int sl = it.bkt_list[st + i];
-      O::template terms<TMAX>(it, sl, bs);
-      if (fp32 && lane == 0) mode_err += it.mode_errw[sl];
-    }
-#pragma unroll
-    for (int t = 0; t < TMAX; ++t) {
-      if (t < TR) u0[t] = vsub2(u0[t], bs[t]);
-    }
-  }
-  if (fp32) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mode_err += __shfl_xor_sync(0xffffffffu, mode_err, o);
-  }
-  // FP32 error bound of this lane's values (see kEpsRms and friends)
-  float eps_base = 0.f, rm0 = 0.f, rml = 0.f;
-  if (fp32) {
-    eps_base = *it.eps_dev + mode_err;
-#pragma unroll
-    for (int t = 0; t < TMAX; ++t) {
-      if (t < TR) {
-        const float *rm = it.row_max + size_t(t) * rows;
-        rm0 = fmaxf(rm0, rm[0]);
-        if (has_bit) rml = fmaxf(rml, fmaxf(rm[2 * lane + 1], rm[2 * lane + 2]));
-      }
-    }
-    rml = fmaxf(rml, rm0);
-  }
-  bool e_near = false;  // energy decision near its threshold (warp-uniform)
-
-  if (mode != kSubtractOnly) {
-    // ---- energy threshold (src/iterate.cc:114-124) on row 0 only
-    T e = 0;
-    T amax = 0;
-#pragma unroll
-    for (int t = 0; t < TMAX; ++t) {
-      if (t < TR) {
-        e += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
-        amax = max(amax, vabs2<T, V>(u0[t]));
-      }
-    }
-    e /= T(TR);
-    if (!isfinite(e)) {
-      if (lane == 0) {
-        atomicOr(&it.flags[1], kStatusNonFinite);
-        it.cand_valid[beta] = 0;
-      }
-      return listed;
-    }
-    if (fp32 ? it.bin_thr2_f > 0.f : it.bin_thr > 0) {
-      T thr2;
-      if (fp32) {
-        thr2 = it.bin_thr2_f;
-        const T eps0 = T(eps_base + it.eps_rel * (kEpsRowMax * rm0 +
-                                                  kEpsValue * float(amax)));
-        // |d e| <= 2 max|u0| eps + eps^2, plus the threshold's FP32 rounding
-        e_near = fabs(e - thr2) <= T(2) * amax * eps0 + eps0 * eps0 +
-                                       thr2 * T(1.2e-7);
-      } else {
-        thr2 = T(it.bin_thr * it.bin_thr);
-      }
-      if (e < thr2) {
-        if (e_near) listed = FlagBin(it, beta, 0u, lane);
-        NoCandidate(it, beta, lane);
-        return listed;
-      }
-    }
-  }
-
-  // ---- rows 2s+1, 2s+2 of this lane's bit and their mode subtraction
-  V up[TMAX], um[TMAX];
-#pragma unroll
-  for (int t = 0; t < TMAX; ++t) {
-    if (t < TR) {
-      if (has_bit) {
-        up[t] = O::from(src.get(t, 2 * lane + 1));
-        um[t] = O::from(src.get(t, 2 * lane + 2));
-      } else {
-        up[t].x = up[t].y = um[t].x = um[t].y = T(0);
-      }
-    }
-  }
   const int64_t off = has_bit ? (int64_t(B) << lane) : 0;
-  // four modes at a time: their row factors e^{2 pi i (B 2^s k1 mod n)/n}
-  // (src/binner.cc:584-589) are evaluated side by side, then subtracted in
-  // the bin's mode order
-  for (int i0 = 0; i0 < nm; i0 += 4) {
-    V fac[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u;
-      if (i < nm) {
-        const int64_t k1 = i < 32 ? __shfl_sync(0xffffffffu, pre_k1, i)
-                                  : it.mode_k1[it.bkt_list[st + i]];
-        if (has_bit) fac[u] = O::phase(it, off * k1);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u;
-      if (i < nm) {
-        V bs[TMAX];
-        if (i < 32) {
-#pragma unroll
-          for (int t = 0; t < TMAX; ++t) {
-            if (t < TR) {
-              bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
-              bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
-            }
-          }
-        } else {
-          O::template terms<TMAX>(it, it.bkt_list[st + i], bs);
-        }
-        if (has_bit) {
-#pragma unroll
-          for (int t = 0; t < TMAX; ++t) {
-            if (t < TR) {
-              up[t] = vsub2(up[t], vmul2(bs[t], fac[u]));
-              um[t] = vsub2(um[t], vmul2(bs[t], vconj2(fac[u])));
-            }
-          }
-        }
-      }
-    }
-  }
-  if (mode == kSubtractOnly) {
-#pragma unroll
-    for (int t = 0; t < TMAX; ++t) {
-      if (t < TR) {
-        double2 *base = it.ubuf + size_t(t) * rows * it.bins_cap;
-        if (lane == 0) base[beta] = make_double2(u0[t].x, u0[t].y);
-        if (has_bit) {
-          base[(2 * lane + 1) * it.bins_cap + beta] = make_double2(up[t].x, up[t].y);
-          base[(2 * lane + 2) * it.bins_cap + beta] = make_double2(um[t].x, um[t].y);
-        }
-      }
-    }
-    return listed;
-  }
-
   // ---- non-finite input is reported instead of being voted on
   bool finite = true;
 #pragma unroll
@@ -545,6 +375,201 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
     it.flags[0] = 1;
   }
   return listed;
+}
+
+// The bin loop body of Iterate for one bin (warp-wide). T = float: the FP32
+// path with near-tie detection, FP32 arithmetic only (GB300 runs FP64 at a
+// small fraction of its FP32 rate): a surviving bin leaves a pending
+// candidate (cand_valid = 2: k1 in cand_k0, the unscaled coefficient sum in
+// cand_coef, its error bound in cand_err) that the merge finishes in FP64 on
+// full warps. T = double: FP64 decisions to the end (the FP64 path, and the
+// near-tie bins after their re-binning).
+template <typename T, int TMAX, typename Src>
+__device__ int DecideBin(const SigIter &it, int beta, const Src &src,
+                          int mode) {
+  using O = Ops<T>;
+  using V = typename O::V;
+  const int lane = threadIdx.x & 31;
+  const int L = it.bits, TR = it.trials, rows = it.rows;
+  const int64_t n = it.n;
+  const int B = it.bins;
+  const bool has_bit = lane < L;
+  const bool fp32 = sizeof(T) == 4;
+  const int nm = it.bkt_count[beta];
+  const int st = it.bkt_start[beta];
+  int listed = -1;  // list position when this bin is listed as a near tie
+
+  // ---- row 0 and its mode subtraction (the bin's modes are in increasing k0).
+  // The first 32 modes are loaded once, one per lane, and shared by shuffles
+  // (the common case); further modes are read directly.
+  V u0[TMAX];
+#pragma unroll
+  for (int t = 0; t < TMAX; ++t) {
+    if (t < TR) u0[t] = O::from(src.get(t, 0));
+  }
+  const int npre = min(nm, 32);
+  V pre_base[TMAX];
+  float mode_err = 0.f;  // FP32 error carried into this bin by the found modes
+  int pre_k1 = 0;  // k1 of the lane's mode (row factors below)
+  if (lane < npre) {
+    const int sl = it.bkt_list[st + lane];
+    O::template terms<TMAX>(it, sl, pre_base);
+    pre_k1 = it.mode_k1[sl];
+    if (fp32) mode_err = it.mode_errw[sl];
+  }
+  for (int i = 0; i < nm; ++i) {
+    V bs[TMAX];
+    if (i < 32) {
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) {
+          bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
+          bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
+        }
+      }
+    } else {
+      const int sl = it.bkt_list[st + i];
+      O::template terms<TMAX>(it, sl, bs);
+      if (fp32 && lane == 0) mode_err += it.mode_errw[sl];
+    }
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) u0[t] = vsub2(u0[t], bs[t]);
+    }
+  }
+  if (fp32) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mode_err += __shfl_xor_sync(0xffffffffu, mode_err, o);
+  }
+  // FP32 error bound of this lane's values (see kEpsRms and friends)
+  float eps_base = 0.f, rm0 = 0.f, rml = 0.f;
+  if (fp32) {
+    eps_base = *it.eps_dev + mode_err;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        const float *rm = it.row_max + size_t(t) * rows;
+        rm0 = fmaxf(rm0, rm[0]);
+        if (has_bit) rml = fmaxf(rml, fmaxf(rm[2 * lane + 1], rm[2 * lane + 2]));
+      }
+    }
+    rml = fmaxf(rml, rm0);
+  }
+  bool e_near = false;  // energy decision near its threshold (warp-uniform)
+
+  if (mode != kSubtractOnly) {
+    // ---- energy threshold (src/iterate.cc:114-124) on row 0 only
+    T e = 0;
+    T amax = 0;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        e += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
+        amax = max(amax, vabs2<T, V>(u0[t]));
+      }
+    }
+    e /= T(TR);
+    if (!isfinite(e)) {
+      if (lane == 0) {
+        atomicOr(&it.flags[1], kStatusNonFinite);
+        it.cand_valid[beta] = 0;
+      }
+      return listed;
+    }
+    if (fp32 ? it.bin_thr2_f > 0.f : it.bin_thr > 0) {
+      T thr2;
+      if (fp32) {
+        thr2 = it.bin_thr2_f;
+        const T eps0 = T(eps_base + it.eps_rel * (kEpsRowMax * rm0 +
+                                                  kEpsValue * float(amax)));
+        // |d e| <= 2 max|u0| eps + eps^2, plus the threshold's FP32 rounding
+        e_near = fabs(e - thr2) <= T(2) * amax * eps0 + eps0 * eps0 +
+                                       thr2 * T(1.2e-7);
+      } else {
+        thr2 = T(it.bin_thr * it.bin_thr);
+      }
+      if (e < thr2) {
+        if (e_near) listed = FlagBin(it, beta, 0u, lane);
+        NoCandidate(it, beta, lane);
+        return listed;
+      }
+    }
+  }
+
+  // ---- rows 2s+1, 2s+2 of this lane's bit and their mode subtraction
+  V up[TMAX], um[TMAX];
+#pragma unroll
+  for (int t = 0; t < TMAX; ++t) {
+    if (t < TR) {
+      if (has_bit) {
+        up[t] = O::from(src.get(t, 2 * lane + 1));
+        um[t] = O::from(src.get(t, 2 * lane + 2));
+      } else {
+        up[t].x = up[t].y = um[t].x = um[t].y = T(0);
+      }
+    }
+  }
+  const int64_t off = has_bit ? (int64_t(B) << lane) : 0;
+  // four modes at a time: their row factors e^{2 pi i (B 2^s k1 mod n)/n}
+  // (src/binner.cc:584-589) are evaluated side by side, then subtracted in
+  // the bin's mode order
+  for (int i0 = 0; i0 < nm; i0 += 4) {
+    V fac[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i < nm) {
+        const int64_t k1 = i < 32 ? __shfl_sync(0xffffffffu, pre_k1, i)
+                                  : it.mode_k1[it.bkt_list[st + i]];
+        if (has_bit) fac[u] = O::phase(it, off * k1);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i < nm) {
+        V bs[TMAX];
+        if (i < 32) {
+#pragma unroll
+          for (int t = 0; t < TMAX; ++t) {
+            if (t < TR) {
+              bs[t].x = __shfl_sync(0xffffffffu, pre_base[t].x, i);
+              bs[t].y = __shfl_sync(0xffffffffu, pre_base[t].y, i);
+            }
+          }
+        } else {
+          O::template terms<TMAX>(it, it.bkt_list[st + i], bs);
+        }
+        if (has_bit) {
+#pragma unroll
+          for (int t = 0; t < TMAX; ++t) {
+            if (t < TR) {
+              up[t] = vsub2(up[t], vmul2(bs[t], fac[u]));
+              um[t] = vsub2(um[t], vmul2(bs[t], vconj2(fac[u])));
+            }
+          }
+        }
+      }
+    }
+  }
+  if (mode == kSubtractOnly) {
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        double2 *base = it.ubuf + size_t(t) * rows * it.bins_cap;
+        if (lane == 0) base[beta] = make_double2(u0[t].x, u0[t].y);
+        if (has_bit) {
+          base[(2 * lane + 1) * it.bins_cap + beta] = make_double2(up[t].x, up[t].y);
+          base[(2 * lane + 2) * it.bins_cap + beta] = make_double2(um[t].x, um[t].y);
+        }
+      }
+    }
+    return listed;
+  }
+
+  return DecideTail<T, TMAX>(it, beta, mode, u0, up, um, eps_base, rml, e_near,
+                             listed);
+
 }
 
 }  // namespace

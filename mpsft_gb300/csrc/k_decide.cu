@@ -171,17 +171,24 @@ __global__ void __launch_bounds__(256)
   if (e >= 0) PrepListedBin(it, e, beta, threadIdx.x & 31);
 }
 
-// FP64 decisions on the re-binned values of the listed near-tie bins.
-// Single-warp blocks, kListedWarps per signal, each taking every
-// kListedWarps-th listed bin: a decision is a long chain of FP64 operations,
-// and GB300's few FP64 pipes per SM are best shared by few such warps, so the
-// listed bins spread over the SMs. Signals whose list overflowed are redone
-// whole instead (redo), or marked unresolved.
-constexpr int kListedWarps = 8;
+// FP64 decisions on the re-binned values of the listed near-tie bins: one
+// block of W warps per listed bin, kListedBlocks blocks per signal taking
+// every kListedBlocks-th bin. The subtraction of the bin's found modes from
+// row 0 and from each bit's two rows (a long chain of FP64 operations per
+// mode; GB300 has few FP64 pipes, with long latencies) is split over the
+// warps: warp w takes the groups of G consecutive modes w, w + W, ..., loads
+// their terms and row-factor table entries together, and keeps per-lane
+// partial sums; the partials meet in shared memory in warp order, and warp 0
+// decides (energy threshold, then DecideTail). Signals whose list overflowed
+// are redone whole instead (redo), or marked unresolved.
+constexpr int kListedBlocks = 8;
 
-template <int TMAX>
-__global__ void __launch_bounds__(32)
+template <int TMAX, int W, int G>
+__global__ void __launch_bounds__(32 * W)
     k_decide_listed(const SigIter *__restrict__ its, int redo) {
+  __shared__ double2 s_p0[W][TMAX];
+  __shared__ double2 s_pp[W][32][TMAX];
+  __shared__ double2 s_pm[W][32][TMAX];
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   if (it.force_fp64) return;
@@ -192,10 +199,118 @@ __global__ void __launch_bounds__(32)
     }
     return;
   }
-  for (int e = blockIdx.x; e < nf; e += kListedWarps) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int TR = it.trials;
+  const bool has_bit = lane < it.bits;
+  const int64_t off = has_bit ? (int64_t(it.bins) << lane) : 0;
+  const ModN mod{uint32_t(it.n), it.n_inv};
+  const uint32_t lo_mask = (1u << it.ph_k) - 1u;
+  for (int e = blockIdx.x; e < nf; e += kListedBlocks) {
     const int beta = it.esc_list[e];
-    DecideBin<double, TMAX>(it, beta, FromRebin{it, e, beta, it.esc_mask[e]},
-                            kDecideExact);
+    const int nm = it.bkt_count[beta], st = it.bkt_start[beta];
+    double2 p0[TMAX], pp[TMAX], pm[TMAX];
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      p0[t] = pp[t] = pm[t] = make_double2(0.0, 0.0);
+    }
+    for (int i0 = warp * G; i0 < nm; i0 += G * W) {
+      // G modes: slots (past the end: the group's first, not accumulated),
+      // then their terms, k1 and row-factor table entries, all loads issued
+      // before any is used
+      int sl[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u) sl[u] = it.bkt_list[st + min(i0 + u, nm - 1)];
+      int64_t k1[G];
+      double2 bs[G][TMAX];
+#pragma unroll
+      for (int u = 0; u < G; ++u) {
+        k1[u] = it.mode_k1[sl[u]];
+#pragma unroll
+        for (int t = 0; t < TMAX; ++t) {
+          if (t < TR) bs[u][t] = it.mode_base[size_t(sl[u]) * TR + t];
+        }
+      }
+      double2 h[G], l[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u) {
+        const uint32_t r = mod(off * k1[u]);
+        h[u] = it.ph_hi[r >> it.ph_k];
+        l[u] = it.ph_lo[r & lo_mask];
+      }
+#pragma unroll
+      for (int u = 0; u < G; ++u) {
+        if (i0 + u < nm) {
+          const double2 fac = cmul(h[u], l[u]);
+#pragma unroll
+          for (int t = 0; t < TMAX; ++t) {
+            if (t < TR) {
+              p0[t] = cadd(p0[t], bs[u][t]);
+              pp[t] = cadd(pp[t], cmul(bs[u][t], fac));
+              pm[t] = cadd(pm[t], cmul(bs[u][t], cconj(fac)));
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        if (lane == 0) s_p0[warp][t] = p0[t];
+        s_pp[warp][lane][t] = pp[t];
+        s_pm[warp][lane][t] = pm[t];
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const FromRebin src{it, e, beta, it.esc_mask[e]};
+      double2 u0[TMAX], up[TMAX], um[TMAX];
+      double en = 0.0;
+#pragma unroll
+      for (int t = 0; t < TMAX; ++t) {
+        if (t < TR) {
+          double2 sum = s_p0[0][t];
+#pragma unroll
+          for (int w = 1; w < W; ++w) sum = cadd(sum, s_p0[w][t]);
+          u0[t] = csub(src.get(t, 0), sum);
+          en += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
+        }
+      }
+      en /= double(TR);
+      // energy threshold on row 0 (src/iterate.cc:114-124)
+      bool go = true;
+      if (!isfinite(en)) {
+        if (lane == 0) {
+          atomicOr(&it.flags[1], kStatusNonFinite);
+          it.cand_valid[beta] = 0;
+        }
+        go = false;
+      } else if (it.bin_thr > 0 && en < it.bin_thr * it.bin_thr) {
+        NoCandidate(it, beta, lane);
+        go = false;
+      }
+      if (go) {
+#pragma unroll
+        for (int t = 0; t < TMAX; ++t) {
+          if (t < TR) {
+            if (has_bit) {
+              double2 sp = s_pp[0][lane][t], sm = s_pm[0][lane][t];
+#pragma unroll
+              for (int w = 1; w < W; ++w) {
+                sp = cadd(sp, s_pp[w][lane][t]);
+                sm = cadd(sm, s_pm[w][lane][t]);
+              }
+              up[t] = csub(src.get(t, 2 * lane + 1), sp);
+              um[t] = csub(src.get(t, 2 * lane + 2), sm);
+            } else {
+              up[t] = um[t] = make_double2(0.0, 0.0);
+            }
+          }
+        }
+        DecideTail<double, TMAX>(it, beta, kDecideExact, u0, up, um, 0.f, 0.f,
+                                 false, -1);
+      }
+    }
+    __syncthreads();  // the partials are rewritten for the next listed bin
   }
 }
 
@@ -402,14 +517,14 @@ void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
 
 void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
                         bool redo, cudaStream_t s) {
-  dim3 grid(kListedWarps, nsig);
+  dim3 grid(kListedBlocks, nsig);
   const int r = redo ? 1 : 0;
   if (max_trials <= 1) {
-    k_decide_listed<1><<<grid, 32, 0, s>>>(d_its, r);
+    k_decide_listed<1, 8, 4><<<grid, 32 * 8, 0, s>>>(d_its, r);
   } else if (max_trials <= 5) {
-    k_decide_listed<5><<<grid, 32, 0, s>>>(d_its, r);
+    k_decide_listed<5, 4, 2><<<grid, 32 * 4, 0, s>>>(d_its, r);
   } else {
-    k_decide_listed<kMaxTrials><<<grid, 32, 0, s>>>(d_its, r);
+    k_decide_listed<kMaxTrials, 2, 1><<<grid, 32 * 2, 0, s>>>(d_its, r);
   }
 }
 
@@ -446,7 +561,11 @@ bool DecideKernelsLaunchable() {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_decide<double, kMaxTrials>, 256, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_decide<float, kMaxTrials>, 256, 0);
   int l = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, k_decide_listed<kMaxTrials>, 32, 0);
+  int l1 = 0, l5 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, k_decide_listed<kMaxTrials, 2, 1>, 64, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l1, k_decide_listed<1, 8, 4>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l5, k_decide_listed<5, 4, 2>, 128, 0);
+  l = (l1 > 0 && l5 > 0) ? l : 0;
   return a > 0 && b > 0 && c > 0 && l > 0;
 }
 
