@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -199,9 +200,13 @@ class Context:
         # grow-only host buffers that batched solves write their modes into
         self._out_k = np.empty(0, np.int32)
         self._out_c = np.empty(0, np.complex128)
+        # live signals of this context: freed before the context itself
+        self._signals = weakref.WeakSet()
 
     def close(self) -> None:
         if getattr(self, "_h", None):
+            for sg in list(getattr(self, "_signals", ())):
+                sg.free()
             self._lib.mpsft_ctx_destroy(self._h)
             self._h = None
 
@@ -227,13 +232,17 @@ class Context:
         h = ctypes.c_void_p()
         _check(self, self._lib.mpsft_signal_upload(self._h, _ptr(x), x.size, dt,
                                                    ctypes.byref(h)))
-        return Signal(self, h, x.size, dt)
+        sg = Signal(self, h, x.size, dt)
+        self._signals.add(sg)
+        return sg
 
     def wrap_device(self, ptr: int, n: int, dtype: int) -> "Signal":
         h = ctypes.c_void_p()
         _check(self, self._lib.mpsft_signal_wrap_device(
             self._h, ctypes.c_void_p(ptr), int(n), int(dtype), ctypes.byref(h)))
-        return Signal(self, h, n, dtype)
+        sg = Signal(self, h, n, dtype)
+        self._signals.add(sg)
+        return sg
 
     def write_many(self, sigs: list, xs: list, stream_handle: int | None = None) -> None:
         """Refills many signals from host arrays (pinned memory for an
@@ -411,7 +420,7 @@ class Context:
         return out, [stats[i].as_dict() for i in range(nsig)]
 
 
-@dataclass
+@dataclass(eq=False)
 class Signal:
     ctx: Context
     _h: ctypes.c_void_p

@@ -200,7 +200,9 @@ __device__ __forceinline__ int DecideTail(const SigIter &it, int beta, int mode,
 
   // ---- IdentifyFreq: per-bit majority of the pencil votes, sv rejection
   int count = 0;
-  bool sv_fail = false, near = false;
+  // clear_fail: an sv rejection outside its rounding bound, which rejects the
+  // bin whatever the near decisions elsewhere give (no listing needed)
+  bool sv_fail = false, near = false, clear_fail = false;
   if (has_bit) {
     const T sv_thr = fp32 ? T(it.sv_thr_f) : T(it.sv_thr);
 #pragma unroll
@@ -225,15 +227,19 @@ __device__ __forceinline__ int DecideTail(const SigIter &it, int beta, int mode,
           // |d Im(m01)| <= eps (2|u0| + |u1| + |u2|) + 4 eps^2;
           // |d sigma1| <= ||dA||_2 <= 2 eps, plus the threshold's rounding.
           if (fabs(im) <= eps * (T(2) * a0 + a1 + a2) + T(4) * eps * eps) near = true;
-          if (sv_thr > T(0) &&
-              fabs(s1 * T(0.5) - sv_thr) <= eps + sv_thr * T(1.2e-7)) {
-            near = true;
+          if (sv_thr > T(0)) {
+            const bool sv_near = fabs(s1 * T(0.5) - sv_thr) <= eps + sv_thr * T(1.2e-7);
+            if (sv_near) {
+              near = true;
+            } else if (s1 * T(0.5) > sv_thr) {
+              clear_fail = true;
+            }
           }
         }
       }
     }
   }
-  if (fp32) {
+  if (fp32 && !__any_sync(0xffffffffu, clear_fail)) {
     const uint32_t near_bits = __ballot_sync(0xffffffffu, has_bit && near);
     if (near_bits || e_near) listed = FlagBin(it, beta, near_bits, lane);
   }

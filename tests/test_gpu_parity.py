@@ -337,6 +337,17 @@ def test_table_cache_across_solves(ctx):
         assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64))
 
 
+def test_close_frees_live_signals():
+    """Closing a context frees its live signals first; the signals' own free
+    (explicit or at collection) is then a no-op."""
+    c2 = m.Context(0)
+    sigs = [c2.upload(np.ones(1 << 12, np.complex64)) for _ in range(3)]
+    c2.close()
+    assert all(sg._freed for sg in sigs)
+    sigs[0].free()
+    del sigs
+
+
 # ------------------------------------------------------------ error paths
 def test_errors_are_statuses(ctx):
     from mpsft_gb300.signals import make_signal
