@@ -100,6 +100,9 @@ struct SigIter {
   // chat = FFT of the conjugate chirp sequence (fft_m entries), FP32 and FP64
   float2 *chirp32, *chat32;
   double2 *chirp64, *chat64;
+  // FP32 path: e^{-pi i r / bins} for r < 2 bins (FP64), the bins-grid half of
+  // the near-tie phase steps (the n grid comes from ph_lo / ph_hi); may be null
+  double2 *r2b64;
   // mode table
   int32_t *tab_key;
   double2 *tab_coef;
@@ -189,7 +192,8 @@ struct SolveCtl {
   int64_t gathers, bin_bytes;
   // the context's table cache (null: per-signal tables): per odd bins B,
   // block win_base[B >> 1] of win_pool holds wt32, wt64, wtff (p2 + 1
-  // entries each), chirp32 (B) and chat32 (M), each 16-byte aligned;
+  // entries each), chirp32 (B), chat32 (M) and r2b64 (2B), each 16-byte
+  // aligned;
   // win_valid marks built blocks, win_claim elects one builder per block
   const int64_t *win_base;
   unsigned char *win_pool;
@@ -198,7 +202,7 @@ struct SolveCtl {
 
 // Byte offsets of the tables inside a table-cache block.
 struct WinBlock {
-  int64_t wt64, wtff, chirp32, chat32, bytes;
+  int64_t wt64, wtff, chirp32, chat32, r2b64, bytes;
 };
 __host__ __device__ inline int64_t Align16(int64_t v) { return (v + 15) & ~int64_t(15); }
 __host__ __device__ inline WinBlock WinBlockOf(int32_t p2, int32_t bins, int32_t m) {
@@ -208,7 +212,8 @@ __host__ __device__ inline WinBlock WinBlockOf(int32_t p2, int32_t bins, int32_t
   w.wtff = w.wt64 + Align16(8 * e);
   w.chirp32 = w.wtff + Align16(8 * e);
   w.chat32 = w.chirp32 + Align16(8 * int64_t(bins));
-  w.bytes = w.chat32 + Align16(8 * int64_t(m));
+  w.r2b64 = w.chat32 + Align16(8 * int64_t(m));
+  w.bytes = w.r2b64 + Align16(32 * int64_t(bins));
   return w;
 }
 

@@ -38,6 +38,7 @@ struct mpsft_ctx {
   // transcendentals, slow on this part, that fill SMs the fold leaves idle
   cudaStream_t side64 = nullptr;
   cudaEvent_t ev_join64 = nullptr;
+  cudaEvent_t ev_fork_l = nullptr, ev_join_l = nullptr;  // listed-bin terms
   cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
   // stream the solve graph is captured on, and the last instantiated graph
   cudaStream_t cap = nullptr;
@@ -319,6 +320,7 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->chat32 = cv.take<float2>(s.m_cap);
   it->chirp64 = cv.take<double2>(s.bins_cap);
   it->chat64 = cv.take<double2>(s.m_cap);
+  it->r2b64 = s.fp32_bins ? cv.take<double2>(2 * size_t(s.bins_cap)) : nullptr;
   it->esc_part =
       cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap * kRebinChunks);
   it->esc_sum = cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap);
@@ -647,10 +649,17 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     // FP64; signals that the precision policy sends to FP64 (and signals
     // whose near-tie list overflowed) run the FP64 kernels
     const bool redo = any_forced && mx.m <= kMaxFFT64;
+    // the listed bins' FP64 mode terms on the side stream, beside the
+    // re-binning
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_l, s));
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork_l, 0));
+    LaunchListedTerms(d_its, nsig, ctx->side);
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_l, ctx->side));
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join64, 0));
     LaunchRebin(d_its, nsig, kMaxListed, x_c128, false, s);
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join_l, 0));
     LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
-    if (launched) *launched += 2;  // re-binning, FP64 decisions
+    if (launched) *launched += 3;  // mode terms, re-binning, FP64 decisions
     if (redo) {
       LaunchModePrep(d_its, nsig, mx.cap, s, true);
       LaunchBluesteinSetup(d_its, nsig, mx.m, true, ctx->tw32, ctx->tw64, s, true);
@@ -1434,6 +1443,8 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop1);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join64, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork_l, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_l, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
   if (e != cudaSuccess) {
@@ -1486,6 +1497,8 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->ev_loop1) cudaEventDestroy(ctx->ev_loop1);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->ev_join64) cudaEventDestroy(ctx->ev_join64);
+  if (ctx->ev_fork_l) cudaEventDestroy(ctx->ev_fork_l);
+  if (ctx->ev_join_l) cudaEventDestroy(ctx->ev_join_l);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return MPSFT_OK;

@@ -119,6 +119,7 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     it.wtff = reinterpret_cast<float2 *>(blk + wb.wtff);
     it.chirp32 = reinterpret_cast<float2 *>(blk + wb.chirp32);
     it.chat32 = reinterpret_cast<float2 *>(blk + wb.chat32);
+    it.r2b64 = reinterpret_cast<double2 *>(blk + wb.r2b64);
     const bool build = c.win_valid[h] == 0 && atomicCAS(&c.win_claim[h], 0, 1) == 0;
     it.tables_valid = build ? 0 : 1;
     if (build) it.win_slot = h;

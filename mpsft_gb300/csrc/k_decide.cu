@@ -314,6 +314,25 @@ __global__ void __launch_bounds__(32 * W)
   }
 }
 
+// FP64 row-0 terms (ModeTerms64: two FP64 erf, long on this part) of the
+// found modes in the listed bins, for their FP64 decisions: blocks over a
+// signal's listed bins, a thread per mode. Runs on the side stream while the
+// listed bins are re-binned.
+__global__ void __launch_bounds__(128) k_listed_terms(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active || it.force_fp64 || it.esc_mask == nullptr) return;
+  const int nf = *(volatile int32_t *)&it.flags[2];
+  if (nf > it.esc_cap) return;
+  for (int e = blockIdx.x; e < nf; e += gridDim.x) {
+    const int beta = it.esc_list[e];
+    const int nm = it.bkt_count[beta], st = it.bkt_start[beta];
+    for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+      const int sl = it.bkt_list[st + i];
+      ModeTerms64(it, sl, it.mode_k1[sl], it.mode_bin[sl]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- merge
 __device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef,
                            double err) {
@@ -526,6 +545,11 @@ void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
   } else {
     k_decide_listed<kMaxTrials, 2, 1><<<grid, 32 * 2, 0, s>>>(d_its, r);
   }
+}
+
+void LaunchListedTerms(const SigIter *d_its, int nsig, cudaStream_t s) {
+  dim3 grid(kListedBlocks, nsig);
+  k_listed_terms<<<grid, 128, 0, s>>>(d_its);
 }
 
 void LaunchMerge(const SigIter *d_its, int nsig, int max_bins,

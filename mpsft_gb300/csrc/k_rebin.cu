@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(256, 2)
       const uint32_t nn = uint32_t(n);
       const int64_t m0 = PosMod(int64_t(it.b) * u0, n);
       const int64_t r0 = PosMod(g * t0, twoB);
-      double ar, ai;
-      sincospi(2.0 * (double(m0) / double(n) - double(r0) / double(twoB)), &ai, &ar);
+      const double2 a0 = StepPhase(it, m0, r0);
+      double ar = a0.x, ai = a0.y;
       const double2 S = it.esc_step[e];
       const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
       const float2 *__restrict__ wff = it.wtff;

@@ -135,6 +135,14 @@ __global__ void __launch_bounds__(512)
     a[Pad(j)] = cc;
     if (j > 0) a[Pad(M - j)] = cc;
   }
+  // FP32 tables: the bins-grid unit roots of the near-tie phase steps
+  if (!cond && sizeof(V) == sizeof(float2) && it.r2b64 != nullptr) {
+    for (int r = threadIdx.x; r < twoB; r += blockDim.x) {
+      double s, c;
+      sincospi(-double(r) / double(B), &s, &c);
+      it.r2b64[r] = make_double2(c, s);
+    }
+  }
   __syncthreads();
   // chat in bit-reversed order (the row transforms' forward output order)
   BlockFFTDif(a, M, it.fft_log2m, tw, false, int(threadIdx.x), int(blockDim.x));
