@@ -26,10 +26,11 @@ constexpr int kMaxFFT = 16384;     // largest Bluestein transform (FP32)
 constexpr int kMaxFFT64 = 8192;    // largest Bluestein transform (FP64)
 constexpr int32_t kEmptyKey = -1;
 constexpr int kRebinChunks = 16;   // re-binning: at most this many chunks of the support
-// chunks of a window support of p samples: runs of at least 64 samples per
-// lane (32 lanes per chunk), at most kRebinChunks
+// chunks of a window support of p samples: runs of at least 16 samples per
+// lane (32 lanes per chunk; a short support spreads over several warps, so
+// that each lane waits for few rounds of gathers), at most kRebinChunks
 __host__ __device__ inline int RebinChunks(int p) {
-  const int c = (p + 2047) / 2048;
+  const int c = (p + 511) / 512;
   return c < 1 ? 1 : (c > kRebinChunks ? kRebinChunks : c);
 }
 constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
@@ -68,6 +69,7 @@ struct SigIter {
   uint64_t n_fix;
   // erf_d / (4 n bins) in FP32: the FP32 window response's argument scale
   float wf_scale;
+  double xi_scale;  // 1 / (2 n bins): xi = (2 bins k1 - (2 beta + 1) n) xi_scale
   // FP64 unit phases e^{2 pi i r / n} = ph_hi[r >> ph_k] * ph_lo[r & (2^ph_k - 1)]
   // (built once per call, see PhaseTableK)
   double2 *ph_lo, *ph_hi;
@@ -234,6 +236,7 @@ __host__ __device__ inline void SetFixedPoint(SigIter *it) {
   it->psi = uint64_t((((unsigned __int128)1 << 64) + twoB / 2) / twoB);
   it->n_fix = n > 1 ? uint64_t((((unsigned __int128)1 << 64) + n / 2) / n) : 0;
   it->wf_scale = float(it->erf_d / (4.0 * double(n) * double(it->bins)));
+  it->xi_scale = 1.0 / (2.0 * double(n) * double(it->bins));
 }
 
 // FP32 copies of an iteration's thresholds (bin_thr, sv_thr set).

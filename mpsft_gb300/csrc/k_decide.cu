@@ -372,19 +372,22 @@ __global__ void k_merge(const SigIter *__restrict__ its) {
   if (v == 2) {
     const int64_t n = it.n, k1 = k0;
     const int B = it.bins;
-    const double xi0 = double(k1) / double(n) - (double(beta) + 0.5) / double(B);
-    const double wf = WindowInFreq(it, xi0);
+    // xi0 = k1/n - (beta + 1/2)/B from its exact integer numerator
+    // (|num| < 2^53) and 1/(2nB); one FP64 division per candidate (each is a
+    // long sequence on this part's FP64 pipes)
+    const int64_t num = 2 * int64_t(B) * k1 - (2 * int64_t(beta) + 1) * n;
+    const double wf = WindowInFreq(it, double(num) * it.xi_scale);
     if (fabs(wf) < it.win_thr) {
       it.cand_valid[beta] = 0;
       return;
     }
     const double m = double(it.trials * (1 + 2 * it.bits));
-    coef = make_double2(coef.x / m, coef.y / m);
+    const double scale = 1.0 / (m * wf);  // the average and the window
     const ModN mod{uint32_t(n), it.n_inv};
     k0 = int32_t(mod(int64_t(it.a_inv) * mod(k1 - it.b)));
     coef = cmul(coef, Phase64(it, -int64_t(it.c) * k0));
-    coef = make_double2(coef.x / wf, coef.y / wf);
-    err = err / fabs(wf);
+    coef = make_double2(coef.x * scale, coef.y * scale);
+    err = err * fabs(m * scale);
     it.cand_k0[beta] = k0;
     it.cand_coef[beta] = coef;
     it.cand_err[beta] = err;
