@@ -37,6 +37,9 @@ constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
 constexpr int kRebinMaxSignals = 256;  // signals per FP64 re-binning launch
 
 constexpr int kCtlWords = 4;  // found flag, status bits, near ties, mode count
+// cand_valid of a listed near-tie bin held back from the merge until its FP64
+// decision (added to the FP32 pass's 0 or 2)
+constexpr int32_t kCandListed = 3;
 
 // Per-signal status bits written by the device.
 enum : int32_t {

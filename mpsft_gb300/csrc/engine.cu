@@ -39,6 +39,7 @@ struct mpsft_ctx {
   cudaStream_t side64 = nullptr;
   cudaEvent_t ev_join64 = nullptr;
   cudaEvent_t ev_fork_l = nullptr, ev_join_l = nullptr;  // listed-bin terms
+  cudaEvent_t ev_join_m = nullptr;  // merge of the bins not listed
   cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
   // stream the solve graph is captured on, and the last instantiated graph
   cudaStream_t cap = nullptr;
@@ -641,24 +642,32 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));  // join
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
-  LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s);
+  // near ties of the FP32 pass: listed bins re-binned and re-decided in
+  // FP64; signals that the precision policy sends to FP64 (and signals whose
+  // near-tie list overflowed) run the FP64 kernels (redo). Without redo the
+  // other bins' merge runs beside the re-binning: the FP32 decide holds the
+  // listed bins back and their FP64 decision merges them.
+  const bool redo = !fp64 && any_forced && mx.m <= kMaxFFT64;
+  const bool side_merge = !fp64 && !redo;
+  LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s, false, side_merge);
   // Bluestein setup, mode preparation, bucketing, window(s), fold, FFT, decide
   if (launched) *launched += fp64 ? 7 : 8;
   if (!fp64) {
-    // near ties of the FP32 pass: listed bins re-binned and re-decided in
-    // FP64; signals that the precision policy sends to FP64 (and signals
-    // whose near-tie list overflowed) run the FP64 kernels
-    const bool redo = any_forced && mx.m <= kMaxFFT64;
-    // the listed bins' FP64 mode terms on the side stream, beside the
+    // side stream: the listed bins' FP64 mode terms (before any merge
+    // changes a coefficient), then the merge of the other bins, beside the
     // re-binning
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_l, s));
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork_l, 0));
     LaunchListedTerms(d_its, nsig, ctx->side);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_l, ctx->side));
+    if (side_merge) {
+      LaunchMerge(d_its, nsig, mx.bins, ctx->side);
+      MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_m, ctx->side));
+    }
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join64, 0));
     LaunchRebin(d_its, nsig, kMaxListed, x_c128, false, s);
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join_l, 0));
-    LaunchDecideListed(d_its, nsig, mx.trials, redo, s);
+    LaunchDecideListed(d_its, nsig, mx.trials, redo, side_merge, s);
     if (launched) *launched += 3;  // mode terms, re-binning, FP64 decisions
     if (redo) {
       LaunchModePrep(d_its, nsig, mx.cap, s, true);
@@ -671,7 +680,11 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
       if (launched) *launched += 5;
     }
   }
-  LaunchMerge(d_its, nsig, mx.bins, s);
+  if (side_merge) {
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join_m, 0));
+  } else {
+    LaunchMerge(d_its, nsig, mx.bins, s);
+  }
   if (launched) *launched += 1;
   MPSFT_CUDA(ctx, cudaGetLastError());
   return MPSFT_OK;
@@ -1445,6 +1458,7 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join64, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork_l, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_l, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_m, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
   if (e != cudaSuccess) {
@@ -1499,6 +1513,7 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->ev_join64) cudaEventDestroy(ctx->ev_join64);
   if (ctx->ev_fork_l) cudaEventDestroy(ctx->ev_fork_l);
   if (ctx->ev_join_l) cudaEventDestroy(ctx->ev_join_l);
+  if (ctx->ev_join_m) cudaEventDestroy(ctx->ev_join_m);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return MPSFT_OK;

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
 // (more near-tie bins than their list holds) take part.
 template <typename T, int TMAX>
 __global__ void __launch_bounds__(256)
-    k_decide(const SigIter *__restrict__ its, int mode, int cond) {
+    k_decide(const SigIter *__restrict__ its, int mode, int cond, int mark) {
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
@@ -167,8 +167,12 @@ __global__ void __launch_bounds__(256)
     e = DecideBin<T, TMAX>(it, beta, FromBins{it, beta}, mode);
   }
   // a listed near tie: its re-binning's tables (after the decision, when few
-  // registers are live)
-  if (e >= 0) PrepListedBin(it, e, beta, threadIdx.x & 31);
+  // registers are live); with mark, the bin's candidate is held back from
+  // the merge (cand_valid + kCandListed) until its FP64 decision
+  if (e >= 0) {
+    if (mark && (threadIdx.x & 31) == 0) it.cand_valid[beta] += kCandListed;
+    PrepListedBin(it, e, beta, threadIdx.x & 31);
+  }
 }
 
 // FP64 decisions on the re-binned values of the listed near-tie bins: one
@@ -183,9 +187,11 @@ __global__ void __launch_bounds__(256)
 // are redone whole instead (redo), or marked unresolved.
 constexpr int kListedBlocks = 8;
 
+__device__ void MergeBin(const SigIter &it, int beta);
+
 template <int TMAX, int W, int G>
 __global__ void __launch_bounds__(32 * W)
-    k_decide_listed(const SigIter *__restrict__ its, int redo) {
+    k_decide_listed(const SigIter *__restrict__ its, int redo, int merge) {
   __shared__ double2 s_p0[W][TMAX];
   __shared__ double2 s_pp[W][32][TMAX];
   __shared__ double2 s_pm[W][32][TMAX];
@@ -196,6 +202,14 @@ __global__ void __launch_bounds__(32 * W)
   if (nf > it.esc_cap) {
     if (!redo && blockIdx.x == 0 && threadIdx.x == 0) {
       atomicOr(&it.flags[1], kStatusUnresolved);
+    }
+    // unresolved: the held-back bins keep their FP32 candidates
+    if (merge && threadIdx.x == 0) {
+      for (int e = blockIdx.x; e < it.esc_cap; e += kListedBlocks) {
+        const int beta = it.esc_list[e];
+        it.cand_valid[beta] -= kCandListed;
+        MergeBin(it, beta);
+      }
     }
     return;
   }
@@ -309,6 +323,8 @@ __global__ void __launch_bounds__(32 * W)
         DecideTail<double, TMAX>(it, beta, kDecideExact, u0, up, um, 0.f, 0.f,
                                  false, -1);
       }
+      // the bin's candidate (written by lane 0 above) into the table
+      if (merge && lane == 0) MergeBin(it, beta);
     }
     __syncthreads();  // the partials are rewritten for the next listed bin
   }
@@ -354,16 +370,12 @@ __device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef,
   atomicOr(&it.flags[1], kStatusCapacity);
 }
 
-// Candidates -> table. Pending FP32 candidates are finished here in FP64 on
-// full warps (src/iterate.cc:139-171): the window response at
+// Candidate of bin beta -> table. A pending FP32 candidate is finished here
+// in FP64 (src/iterate.cc:139-171): the window response at
 // xi0 = k1/n - (beta + 1/2)/B and its threshold, the average over the
 // T (1 + 2L) values, k0 = a^-1 (k1 - b) mod n, the factor e^{-2 pi i c k0/n}
 // and the division by the window response.
-__global__ void k_merge(const SigIter *__restrict__ its) {
-  const SigIter &it = its[blockIdx.y];
-  if (!it.active) return;
-  const int beta = blockIdx.x * blockDim.x + threadIdx.x;
-  if (beta >= it.bins) return;
+__device__ void MergeBin(const SigIter &it, int beta) {
   const int v = it.cand_valid[beta];
   if (!v) return;
   int32_t k0 = it.cand_k0[beta];
@@ -395,6 +407,17 @@ __global__ void k_merge(const SigIter *__restrict__ its) {
   }
   it.flags[0] = 1;
   InsertMode(it, k0, coef, err);
+}
+
+// Candidates -> table, one thread per bin; bins held back for their FP64
+// near-tie decision (cand_valid >= kCandListed) are merged by that decision.
+__global__ void k_merge(const SigIter *__restrict__ its) {
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active) return;
+  const int beta = blockIdx.x * blockDim.x + threadIdx.x;
+  if (beta >= it.bins) return;
+  if (it.cand_valid[beta] >= kCandListed) return;
+  MergeBin(it, beta);
 }
 
 __global__ void k_table_insert(const SigIter *__restrict__ it,
@@ -474,20 +497,20 @@ __global__ void __launch_bounds__(1024)
 
 template <typename T, int TMAX>
 void LaunchDecideT(const SigIter *d_its, int nsig, int max_bins, int mode,
-                   int cond, cudaStream_t s) {
+                   int cond, int mark, cudaStream_t s) {
   dim3 grid((max_bins + 7) / 8, nsig);
-  k_decide<T, TMAX><<<grid, 256, 0, s>>>(d_its, mode, cond);
+  k_decide<T, TMAX><<<grid, 256, 0, s>>>(d_its, mode, cond, mark);
 }
 
 template <typename T>
 void LaunchDecideP(const SigIter *d_its, int nsig, int max_bins, int max_trials,
-                   int mode, int cond, cudaStream_t s) {
+                   int mode, int cond, int mark, cudaStream_t s) {
   if (max_trials <= 1) {
-    LaunchDecideT<T, 1>(d_its, nsig, max_bins, mode, cond, s);
+    LaunchDecideT<T, 1>(d_its, nsig, max_bins, mode, cond, mark, s);
   } else if (max_trials <= 5) {
-    LaunchDecideT<T, 5>(d_its, nsig, max_bins, mode, cond, s);
+    LaunchDecideT<T, 5>(d_its, nsig, max_bins, mode, cond, mark, s);
   } else {
-    LaunchDecideT<T, kMaxTrials>(d_its, nsig, max_bins, mode, cond, s);
+    LaunchDecideT<T, kMaxTrials>(d_its, nsig, max_bins, mode, cond, mark, s);
   }
 }
 
@@ -527,26 +550,28 @@ void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
 }
 
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
-                  bool fp32, bool subtract_only, cudaStream_t s, bool cond) {
+                  bool fp32, bool subtract_only, cudaStream_t s, bool cond,
+                  bool mark_listed) {
   const int mode = subtract_only ? kSubtractOnly : kDecide;
   if (fp32) {
-    LaunchDecideP<float>(d_its, nsig, max_bins, max_trials, mode, 0, s);
+    LaunchDecideP<float>(d_its, nsig, max_bins, max_trials, mode, 0,
+                         mark_listed ? 1 : 0, s);
   } else {
     LaunchDecideP<double>(d_its, nsig, max_bins, max_trials, mode, cond ? 1 : 0,
-                          s);
+                          0, s);
   }
 }
 
 void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
-                        bool redo, cudaStream_t s) {
+                        bool redo, bool merge, cudaStream_t s) {
   dim3 grid(kListedBlocks, nsig);
-  const int r = redo ? 1 : 0;
+  const int r = redo ? 1 : 0, mg = merge ? 1 : 0;
   if (max_trials <= 1) {
-    k_decide_listed<1, 8, 4><<<grid, 32 * 8, 0, s>>>(d_its, r);
+    k_decide_listed<1, 8, 4><<<grid, 32 * 8, 0, s>>>(d_its, r, mg);
   } else if (max_trials <= 5) {
-    k_decide_listed<5, 4, 2><<<grid, 32 * 4, 0, s>>>(d_its, r);
+    k_decide_listed<5, 4, 2><<<grid, 32 * 4, 0, s>>>(d_its, r, mg);
   } else {
-    k_decide_listed<kMaxTrials, 2, 1><<<grid, 32 * 2, 0, s>>>(d_its, r);
+    k_decide_listed<kMaxTrials, 2, 1><<<grid, 32 * 2, 0, s>>>(d_its, r, mg);
   }
 }
 

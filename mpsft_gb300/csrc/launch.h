@@ -78,9 +78,11 @@ void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
 // estimation (the bin loop of Iterate); writes the candidates. With
 // subtract_only, only the mode subtraction of BinInFreq::Run is applied to
 // ubuf in place.
+// mark_listed: the FP32 pass holds its listed bins back from the merge
+// (cand_valid + kCandListed); their FP64 decision merges them.
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
                   bool fp32, bool subtract_only, cudaStream_t s,
-                  bool cond = false);
+                  bool cond = false, bool mark_listed = false);
 
 // Re-binning of the near-tie bins listed by the FP32 decide pass (direct sums
 // over the window support in float-float arithmetic with FP64 block totals).
@@ -91,8 +93,10 @@ void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
 // FP64 decisions of the listed bins on their re-binned rows. redo: the
 // conditional FP64 kernels follow (signals whose list overflowed are redone
 // whole); without them such signals are reported unresolved.
+// merge: each decided bin goes into the table right away (the other bins'
+// merge runs beside the re-binning).
 void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
-                        bool redo, cudaStream_t s);
+                        bool redo, bool merge, cudaStream_t s);
 
 // Candidates -> mode table (mm[k0] += coef).
 void LaunchMerge(const SigIter *d_its, int nsig, int max_bins, cudaStream_t s);
