@@ -228,18 +228,40 @@ __host__ __device__ inline int64_t PosMod(int64_t v, int64_t n) {
   return v < 0 ? v + n : v;
 }
 
-// The fixed-point constants of an iteration (n, b and bins set).
-__host__ __device__ inline void SetFixedPoint(SigIter *it) {
+// The fixed-point constants that depend on n and the bins only (n, bins and
+// erf_d set).
+__host__ __device__ inline void SetBinsFixedPoint(SigIter *it) {
   const uint64_t n = uint64_t(it->n);
   const bool pow2 = (n & (n - 1)) == 0;
   it->n_inv = pow2 ? 0 : uint64_t(((unsigned __int128)1 << 64) / n);
-  const uint64_t bm = uint64_t(PosMod(it->b, int64_t(n)));
-  it->phi_b = uint64_t((((unsigned __int128)bm << 64) + n / 2) / n);
   const uint64_t twoB = 2 * uint64_t(it->bins);
   it->psi = uint64_t((((unsigned __int128)1 << 64) + twoB / 2) / twoB);
   it->n_fix = n > 1 ? uint64_t((((unsigned __int128)1 << 64) + n / 2) / n) : 0;
   it->wf_scale = float(it->erf_d / (4.0 * double(n) * double(it->bins)));
   it->xi_scale = 1.0 / (2.0 * double(n) * double(it->bins));
+}
+
+// phi_b = round(2^64 (b mod n) / n) (n and b set); for n = 2^k it is exactly
+// (b mod n) 2^(64 - k), without the 128-bit division.
+__host__ __device__ inline void SetPhiB(SigIter *it) {
+  const uint64_t n = uint64_t(it->n);
+  const uint64_t bm = uint64_t(PosMod(it->b, int64_t(n)));
+  if ((n & (n - 1)) == 0) {
+#ifdef __CUDA_ARCH__
+    const int k = 63 - __clzll(static_cast<long long>(n));
+#else
+    const int k = __builtin_ctzll(n);
+#endif
+    it->phi_b = bm << (64 - k);
+  } else {
+    it->phi_b = uint64_t((((unsigned __int128)bm << 64) + n / 2) / n);
+  }
+}
+
+// The fixed-point constants of an iteration (n, b, bins and erf_d set).
+__host__ __device__ inline void SetFixedPoint(SigIter *it) {
+  SetBinsFixedPoint(it);
+  SetPhiB(it);
 }
 
 // FP32 copies of an iteration's thresholds (bin_thr, sv_thr set).

@@ -56,27 +56,52 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     it.active = 0;
     return;
   }
-  const int32_t bits = NumBitsDev(it.n, bins);
+  // Everything that depends on the bins only (and on the signal's constants)
+  // stays from the previous iteration when the bins repeat (most late
+  // iterations): the window scalars, fixed-point constants and thresholds
+  // are a chain of FP64 divisions, square roots and 128-bit divisions, each a
+  // long sequence on this part.
+  const bool same_bins = it.bins == bins;
   const double B = double(bins);
-  // Window scalars in the reference's operation order, no contraction.
-  const double width = __ddiv_rn(1.0, __dmul_rn(2.0, B));
-  const double sq = c.sqrt_c_delta;
-  const double sigma_f =
-      __ddiv_rn(0.5, __dmul_rn(__dmul_rn(__dmul_rn(B, 2.0), M_SQRT2), sq));
-  const double sigma_t = __ddiv_rn(1.0, __dmul_rn(2.0 * M_PI, sigma_f));
-  const double tmp =
-      __dadd_rn(__dmul_rn(__dmul_rn(2.0 * M_SQRT2, sigma_t), sq), 1.0);
-  int32_t f = int32_t(ceil(__ddiv_rn(tmp, B)));
-  if (f % 2 == 0) ++f;
-  it.bins = bins;
-  it.bits = bits;
-  it.rows = 1 + 2 * bits;
-  it.folds = f;
-  it.p = f * bins;
-  it.p2 = (it.p - 1) / 2;
-  it.width = width;
-  it.sigma_f = sigma_f;
-  it.erf_d = __dmul_rn(M_SQRT2 * M_PI, sigma_t);
+  if (!same_bins) {
+    // Window scalars in the reference's operation order, no contraction.
+    const double width = __ddiv_rn(1.0, __dmul_rn(2.0, B));
+    const double sq = c.sqrt_c_delta;
+    const double sigma_f =
+        __ddiv_rn(0.5, __dmul_rn(__dmul_rn(__dmul_rn(B, 2.0), M_SQRT2), sq));
+    const double sigma_t = __ddiv_rn(1.0, __dmul_rn(2.0 * M_PI, sigma_f));
+    const double tmp =
+        __dadd_rn(__dmul_rn(__dmul_rn(2.0 * M_SQRT2, sigma_t), sq), 1.0);
+    int32_t f = int32_t(ceil(__ddiv_rn(tmp, B)));
+    if (f % 2 == 0) ++f;
+    const int32_t bits = NumBitsDev(it.n, bins);
+    it.bins = bins;
+    it.bits = bits;
+    it.rows = 1 + 2 * bits;
+    it.folds = f;
+    it.p = f * bins;
+    it.p2 = (it.p - 1) / 2;
+    it.width = width;
+    it.sigma_f = sigma_f;
+    it.erf_d = __dmul_rn(M_SQRT2 * M_PI, sigma_t);
+    SetBinsFixedPoint(&it);
+    const double rb = __dsqrt_rn(B);
+    it.bin_thr = __ddiv_rn(__dmul_rn(3.0, c.sigma), rb);
+    it.sv_thr = __ddiv_rn(c.sigma, rb);
+    SetThresholdCopies(&it);
+    int l = 0;
+    while ((1 << l) < 2 * bins - 1) ++l;
+    it.fft_log2m = l;
+    it.fft_m = 1 << l;
+    if (!c.fp64_path) {
+      it.eps_rel = float(c.margin * 5.9604644775390625e-08);  // margin * 2^-24
+      it.eps_scale =
+          c.margin * double(kEpsRms) * 5.9604644775390625e-08 / sqrt(2.0 * B);
+    } else {
+      it.eps_rel = 0.f;
+      it.eps_scale = 0.0;
+    }
+  }
   const int32_t *d = c.draws + size_t(local) * c.draw_stride;
   const double *bq = c.draw_bq + size_t(local) * (c.draw_stride - 4) * 2;
   it.a = d[0];
@@ -84,29 +109,14 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
   it.c = d[2];
   it.a_inv = d[3];
   it.trials = c.trials;
-  SetFixedPoint(&it);
+  SetPhiB(&it);
   for (int t = 0; t < c.trials; ++t) {
     it.q[t] = d[4 + t];
     it.bq_re[t] = bq[2 * t];
     it.bq_im[t] = bq[2 * t + 1];
   }
-  const double rb = __dsqrt_rn(B);
-  it.bin_thr = __ddiv_rn(__dmul_rn(3.0, c.sigma), rb);
-  it.sv_thr = __ddiv_rn(c.sigma, rb);
-  SetThresholdCopies(&it);
   it.win_thr = c.win_thr;
-  int l = 0;
-  while ((1 << l) < 2 * bins - 1) ++l;
-  it.fft_log2m = l;
-  it.fft_m = 1 << l;
   it.force_fp64 = c.force_fp64;
-  if (!c.fp64_path) {
-    it.eps_rel = float(c.margin * 5.9604644775390625e-08);  // margin * 2^-24
-    it.eps_scale = c.margin * double(kEpsRms) * 5.9604644775390625e-08 / sqrt(2.0 * B);
-  } else {
-    it.eps_rel = 0.f;
-    it.eps_scale = 0.0;
-  }
   it.win_slot = -1;
   if (c.win_base != nullptr && !c.force_fp64) {
     // tables from the context's cache: built already, or built now by the
