@@ -397,7 +397,6 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
   using V = typename O::V;
   const int lane = threadIdx.x & 31;
   const int L = it.bits, TR = it.trials, rows = it.rows;
-  const int64_t n = it.n;
   const int B = it.bins;
   const bool has_bit = lane < L;
   const bool fp32 = sizeof(T) == 4;

@@ -746,9 +746,9 @@ int CheckSignal(mpsft_ctx *ctx, const mpsft_signal *sig) {
 
 constexpr int kDrawChunk = 32;  // iterations of draws uploaded at a time
 constexpr int kGraphUnavailable = -100;
-static_assert(kSolveCapacity == MPSFT_ERR_CAPACITY &&
-                  kSolveIterCap == MPSFT_ERR_ITER_CAP &&
-                  kSolveNonFinite == MPSFT_ERR_NONFINITE,
+static_assert(int(kSolveCapacity) == int(MPSFT_ERR_CAPACITY) &&
+                  int(kSolveIterCap) == int(MPSFT_ERR_ITER_CAP) &&
+                  int(kSolveNonFinite) == int(MPSFT_ERR_NONFINITE),
               "device stop codes are the ABI's status codes");
 
 // Fills draws for iterations [base, base + kDrawChunk) of one signal from its
