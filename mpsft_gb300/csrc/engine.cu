@@ -630,6 +630,14 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   } else {
     LaunchWindow32(d_its, nsig, mx.p2, s);
   }
+  if (timer && ctx->profiling) {
+    // profiling: the binning alone on the GPU (the side streams' kernels
+    // first), and its launch enqueued while a short delay kernel holds the
+    // stream, so that its events time the kernel, not a host launch gap
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    if (!fp64) MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join64, 0));
+    LaunchDelay(20000, s);
+  }
   if (timer) {
     int rc = timer->Begin();
     if (rc) return rc;

@@ -192,7 +192,23 @@ __global__ void __launch_bounds__(1024)
   }
 }
 
+// Holds the stream for `ns` nanoseconds of the global timer (one thread;
+// the wait always ends): in profiling runs, the host enqueues the timed
+// binning launch and its events meanwhile, so that no host launch gap falls
+// between the events.
+__global__ void k_delay(unsigned long long ns) {
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  do {
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  } while (t - t0 < ns);
+}
+
 }  // namespace
+
+void LaunchDelay(unsigned long long ns, cudaStream_t s) {
+  k_delay<<<1, 1, 0, s>>>(ns);
+}
 
 void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, int32_t max_bins,
                 cudaStream_t s) {

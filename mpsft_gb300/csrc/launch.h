@@ -9,6 +9,8 @@ namespace mpsft {
 
 // e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2, for the FFT twiddles.
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s);
+// A one-thread kernel that holds the stream for ns nanoseconds.
+void LaunchDelay(unsigned long long ns, cudaStream_t s);
 
 // FP64 unit-phase tables ph_lo / ph_hi of every signal (n and the table
 // pointers set); entries = the largest table length of the signals.
