@@ -64,6 +64,11 @@ struct mpsft_ctx {
   size_t h_ctl_n = 0;
   // pinned staging of exported mode tables
   unsigned char *h_stage = nullptr;
+  // pinned, device-mapped staging of a solve's small uploads (copied by a
+  // kernel, see Upload), its device address and the bump offset
+  unsigned char *h_up = nullptr, *d_up = nullptr;
+  size_t h_up_n = 0, up_off = 0;
+  int64_t up_launches = 0;  // copy kernels Upload launched in this call
   size_t h_stage_n = 0;
   std::vector<cudaEvent_t> events;
   // table cache of FP32 solves: window tables (FP32, FP64, float-float) and
@@ -399,6 +404,53 @@ int EnsureHostStage(mpsft_ctx *ctx, size_t bytes) {
   ctx->h_stage_n = 0;
   MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_stage, bytes));
   ctx->h_stage_n = bytes;
+  return MPSFT_OK;
+}
+
+// A solve's small host -> device transfers (iteration descriptors, draw
+// tables, solve state) go through pinned, device-mapped staging and a copy
+// kernel rather than the copy engines: a caller streaming the next batch's
+// signals in on another stream keeps the engines busy with gigabytes, and a
+// DMA copy queued behind those would hold the solve's start back. The
+// staging is a bump allocator, reset at the start of a call and after each
+// stream synchronisation that retires the uploads before it.
+int EnsureUploadStage(mpsft_ctx *ctx, size_t bytes) {
+  if (ctx->h_up_n >= bytes) return MPSFT_OK;
+  if (ctx->h_up) {
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFreeHost(ctx->h_up);
+  }
+  ctx->h_up = nullptr;
+  ctx->d_up = nullptr;
+  ctx->h_up_n = 0;
+  ctx->up_off = 0;
+  const size_t want = bytes + (bytes >> 2) + 4096;
+  MPSFT_CUDA(ctx, cudaHostAlloc(&ctx->h_up, want, cudaHostAllocMapped));
+  void *dp = nullptr;
+  MPSFT_CUDA(ctx, cudaHostGetDevicePointer(&dp, ctx->h_up, 0));
+  ctx->d_up = static_cast<unsigned char *>(dp);
+  ctx->h_up_n = want;
+  return MPSFT_OK;
+}
+
+int Upload(mpsft_ctx *ctx, void *dst, const void *src, size_t bytes,
+           cudaStream_t s) {
+  if (bytes == 0) return MPSFT_OK;
+  const size_t off = (ctx->up_off + 255) & ~size_t(255);
+  if (off + bytes > ctx->h_up_n) {
+    // (only when the caller did not reserve enough: retire the pending
+    // uploads and start over in a larger stage)
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->up_off = 0;
+    int rc = EnsureUploadStage(ctx, bytes);
+    if (rc) return rc;
+    return Upload(ctx, dst, src, bytes, s);
+  }
+  std::memcpy(ctx->h_up + off, src, bytes);
+  ctx->up_off = off + bytes;
+  LaunchCopyMapped(ctx->d_up + off, dst, bytes, s);
+  ++ctx->up_launches;
+  MPSFT_CUDA(ctx, cudaGetLastError());
   return MPSFT_OK;
 }
 
@@ -867,21 +919,26 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     it.trials = opts[i].trials;
     it.active = 0;
   }
-  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its->data(), sizeof(SigIter) * nsig,
-                                  cudaMemcpyHostToDevice, ctx->stream));
+  {
+    const int rc = Upload(ctx, d_its, its->data(), sizeof(SigIter) * nsig, ctx->stream);
+    if (rc) return rc;
+  }
   std::vector<SolveCtl> &hc = dt->hc;
   std::vector<int32_t> &hd = dt->hd;
   std::vector<double> &hb = dt->hb;
   const std::vector<mpsft_rng> &saved = dt->saved;
   const size_t bq_per = dt->bq_per;
   for (int i = 0; i < nsig; ++i) hc[i].force_fp64 = force[i];
-  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draws, hd.data(), sizeof(int32_t) * hd.size(),
-                                  cudaMemcpyHostToDevice, ctx->stream));
-  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draw_bq, hb.data(), sizeof(double) * hb.size(),
-                                  cudaMemcpyHostToDevice, ctx->stream));
-  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_solve_ctl, hc.data(),
-                                  sizeof(SolveCtl) * nsig, cudaMemcpyHostToDevice,
-                                  ctx->stream));
+  {
+    int rc = Upload(ctx, ctx->d_draws, hd.data(), sizeof(int32_t) * hd.size(), ctx->stream);
+    if (rc == MPSFT_OK) {
+      rc = Upload(ctx, ctx->d_draw_bq, hb.data(), sizeof(double) * hb.size(), ctx->stream);
+    }
+    if (rc == MPSFT_OK) {
+      rc = Upload(ctx, ctx->d_solve_ctl, hc.data(), sizeof(SolveCtl) * nsig, ctx->stream);
+    }
+    if (rc) return rc;
+  }
   // late-iteration phase: bins up to small_bins (a few times min_bins)
   int32_t min_bins_max = 1;
   int32_t min_bins_min = INT32_MAX;
@@ -997,6 +1054,7 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                     sizeof(SolveCtl) * nsig,
                                     cudaMemcpyDeviceToHost, ctx->stream));
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->up_off = 0;  // every upload so far has been consumed
     int32_t most = 0;
     bool all_done = true, refilled = false;
     for (int i = 0; i < nsig; ++i) {
@@ -1009,19 +1067,19 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
         FillDraws(rngs[i], int32_t(sigs[i]->n), opts[i].trials, stride,
                   hd.data() + size_t(i) * kDrawChunk * stride,
                   hb.data() + i * bq_per);
-        MPSFT_CUDA(ctx, cudaMemcpyAsync(
-                            ctx->d_draws + size_t(i) * kDrawChunk * stride,
-                            hd.data() + size_t(i) * kDrawChunk * stride,
-                            sizeof(int32_t) * kDrawChunk * stride,
-                            cudaMemcpyHostToDevice, ctx->stream));
-        MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->d_draw_bq + i * bq_per,
-                                        hb.data() + i * bq_per,
-                                        sizeof(double) * bq_per,
-                                        cudaMemcpyHostToDevice, ctx->stream));
         const int32_t window[2] = {hc[i].iter, kDrawChunk};
-        MPSFT_CUDA(ctx, cudaMemcpyAsync(&ctx->d_solve_ctl[i].draw_base, window,
-                                        sizeof(window), cudaMemcpyHostToDevice,
-                                        ctx->stream));
+        int rc = Upload(ctx, ctx->d_draws + size_t(i) * kDrawChunk * stride,
+                        hd.data() + size_t(i) * kDrawChunk * stride,
+                        sizeof(int32_t) * kDrawChunk * stride, ctx->stream);
+        if (rc == MPSFT_OK) {
+          rc = Upload(ctx, ctx->d_draw_bq + i * bq_per, hb.data() + i * bq_per,
+                      sizeof(double) * bq_per, ctx->stream);
+        }
+        if (rc == MPSFT_OK) {
+          rc = Upload(ctx, &ctx->d_solve_ctl[i].draw_base, window, sizeof(window),
+                      ctx->stream);
+        }
+        if (rc) return rc;
         refilled = true;
       }
     }
@@ -1148,10 +1206,20 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     its[i].n = int32_t(sigs[i]->n);
     phase_entries = std::max(phase_entries, PhaseTableEntries(sigs[i]->n));
   }
+  // the call's small uploads (descriptors twice, signal pointers and lengths,
+  // draw tables, solve state) fit the staging without a wait
+  rc = EnsureUploadStage(
+      ctx, 2 * sizeof(SigIter) * nsig + 16 * size_t(nsig) +
+               size_t(nsig) * kDrawChunk * (4 + max_trials_all) * sizeof(int32_t) +
+               size_t(nsig) * kDrawChunk * max_trials_all * 2 * sizeof(double) +
+               sizeof(SolveCtl) * nsig + 16 * 256);
+  if (rc) return rc;
+  ctx->up_off = 0;
+  ctx->up_launches = 0;
   // empty tables and the FP64 unit-phase tables (per signal length, for the
   // whole call)
-  MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
-                                  cudaMemcpyHostToDevice, ctx->stream));
+  rc = Upload(ctx, d_its, its.data(), sizeof(SigIter) * nsig, ctx->stream);
+  if (rc) return rc;
   LaunchClearTables(d_its, nsig, max_cap, ctx->stream);
   LaunchPhaseTables(d_its, nsig, phase_entries, ctx->stream);
   bool host_loop = ctx->profiling || ctx->graph_unavailable;
@@ -1165,10 +1233,10 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       h_xs[i] = sigs[i]->d_x;
       h_ns[i] = sigs[i]->n;
     }
-    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_xs, h_xs.data(), sizeof(void *) * nsig,
-                                    cudaMemcpyHostToDevice, ctx->stream));
-    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_ns, h_ns.data(), sizeof(int64_t) * nsig,
-                                    cudaMemcpyHostToDevice, ctx->stream));
+    rc = Upload(ctx, d_xs, h_xs.data(), sizeof(void *) * nsig, ctx->stream);
+    if (rc) return rc;
+    rc = Upload(ctx, d_ns, h_ns.data(), sizeof(int64_t) * nsig, ctx->stream);
+    if (rc) return rc;
     LaunchEnergy(d_xs, d_ns, nsig, x_c128, d_energy, ctx->stream);
     // the host's share of the solve graph runs while the GPU reads x
     if (!host_loop) PrepareDraws(ctx, sigs, opts, nsig, rngs, fp64, &draws);
@@ -1336,6 +1404,9 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
   int first_err = MPSFT_OK;
   const double bin_ms = timer.TotalMs();
+  // the call's own kernels outside the loop: table clearing, phase tables,
+  // the energy pair (FP32), the export and the upload copies
+  launches += 2 + (fp64 ? 0 : 2) + 1 + ctx->up_launches;
   // every table's entries in two copies: counts first, then the
   // (signals x largest count) block of keys and coefficients
   LaunchExportTables(d_its, nsig, max_cap, d_exp_keys, d_exp_coefs,
@@ -1500,6 +1571,7 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->h_up) cudaFreeHost(ctx->h_up);
   if (ctx->tw32) cudaFree(ctx->tw32);
   if (ctx->tw64) cudaFree(ctx->tw64);
   if (ctx->win_dev) cudaFree(ctx->win_dev);

@@ -14,6 +14,8 @@
 // stale one when nothing was found, stop after max_stale_iter stale ones (never
 // reset), on a status, or at max_iter; then it sets the while condition to
 // "some signal still has work and draws".
+#include <algorithm>
+
 #include "common.cuh"
 #include "launch.h"
 
@@ -204,7 +206,38 @@ __global__ void k_delay(unsigned long long ns) {
   } while (t - t0 < ns);
 }
 
+// dst[0..bytes) = src[0..bytes) with src in device-mapped pinned host memory:
+// 16-byte words when both are 16-byte aligned, 4-byte words when 4-byte
+// aligned, else bytes; the remainder bytewise.
+__global__ void __launch_bounds__(256)
+    k_copy_mapped(const unsigned char *__restrict__ src, unsigned char *__restrict__ dst,
+                  size_t bytes) {
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  const size_t t0 = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uintptr_t al = reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst);
+  const int w = (al & 15u) == 0 ? 16 : ((al & 3u) == 0 ? 4 : 1);
+  const size_t nw = bytes / w;
+  if (w == 16) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (size_t i = t0; i < nw; i += stride) d4[i] = s4[i];
+  } else if (w == 4) {
+    const uint32_t *s1 = reinterpret_cast<const uint32_t *>(src);
+    uint32_t *d1 = reinterpret_cast<uint32_t *>(dst);
+    for (size_t i = t0; i < nw; i += stride) d1[i] = s1[i];
+  }
+  for (size_t i = nw * w + t0; i < bytes; i += stride) dst[i] = src[i];
+}
+
 }  // namespace
+
+void LaunchCopyMapped(const void *src_dev, void *dst, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return;
+  const size_t words = bytes / 16 + 1;
+  const unsigned blocks = unsigned(std::min<size_t>(152, (words + 255) / 256));
+  k_copy_mapped<<<blocks, 256, 0, s>>>(static_cast<const unsigned char *>(src_dev),
+                                       static_cast<unsigned char *>(dst), bytes);
+}
 
 void LaunchDelay(unsigned long long ns, cudaStream_t s) {
   k_delay<<<1, 1, 0, s>>>(ns);

@@ -9,6 +9,9 @@ namespace mpsft {
 
 // e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2, for the FFT twiddles.
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s);
+// dst (device) = src_dev (device address of pinned, mapped host memory), any
+// alignment and size.
+void LaunchCopyMapped(const void *src_dev, void *dst, size_t bytes, cudaStream_t s);
 // A one-thread kernel that holds the stream for ns nanoseconds.
 void LaunchDelay(unsigned long long ns, cudaStream_t s);
 

@@ -271,6 +271,36 @@ def test_write_many_pipelined(ctx):
         ctx.write_many(sets[0][:1], [np.zeros(n, np.complex128)])
 
 
+@pytest.mark.parametrize("n", [65537, 1 << 16])
+def test_write_many_copies(ctx, n):
+    """mpsft_signal_write_many from pinned memory (copied by a kernel through
+    the buffer's device mapping; an odd n leaves an 8-byte tail) and from
+    pageable memory (DMA copy) leaves the same samples as an upload: the bins
+    agree bit for bit."""
+    import torch
+
+    rng = np.random.default_rng(n)
+    xs = [(rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+          for _ in range(3)]
+    pinned = []
+    for x in xs[:2]:
+        t = torch.empty(n, dtype=torch.complex64, pin_memory=True)
+        t.numpy()[:] = x
+        pinned.append(t.numpy())
+    hosts = pinned + [xs[2].copy()]          # two pinned, one pageable
+    sigs = [ctx.upload(np.zeros(n, np.complex64)) for _ in range(3)]
+    ctx.write_many(sigs, hosts)
+    ref = [ctx.upload(x) for x in xs]
+    bins, delta = 51, 1e-5
+    bits = m.num_bits(n, bins)
+    for got, want in zip(sigs, ref):
+        ug = ctx.bin_in_time(got, bins, bits, delta, 3, 5, 7, 11, precision=m.FP32)
+        uw = ctx.bin_in_time(want, bins, bits, delta, 3, 5, 7, 11, precision=m.FP32)
+        assert np.array_equal(ug.view(np.uint64), uw.view(np.uint64))
+    for sg in sigs + ref:
+        sg.free()
+
+
 @pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
 def test_deterministic(ctx, prec):
     from mpsft_gb300.signals import make_signal
