@@ -52,6 +52,7 @@ SOLVES = [
     ("pow2_s200_t3", 1 << 18, 200, 1e-3, 3, 51, 1e-5, 23, 123537, "unit"),
     ("config1", 1 << 20, 50, 1e-6, 1, 51, 1e-5, 1, 123537, "unit"),
     ("pow2_s300_logu", 1 << 20, 300, None, 1, 51, 1e-5, 24, 123537, "loguniform"),
+    ("prime_s120_t5", 65537, 120, 1e-4, 5, 51, 1e-5, 25, 123537, "unit"),
 ]
 
 
