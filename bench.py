@@ -131,41 +131,93 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline
-def _cpu_worker_init(seed):
-    global _W_SIG
+# The oracle port in two builds: "port" (-O2, no FP contraction: the checker's
+# build) and "port_fast" (the reference's optimised flags, -O3 -ffast-math).
+# The CPU baseline reports the faster of the two.
+_BUILDS = {"port": "-O2 strict FP", "port_fast": "-O3 -ffast-math"}
+
+
+def _oracle_lib(kind: str):
+    from oracle import oracle
+    if not oracle.available(kind):
+        (oracle.build_port if kind == "port" else oracle.build_port_fast)()
+    return oracle.Oracle(kind)
+
+
+def host_cpu() -> str:
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE,
+                             stderr=subprocess.DEVNULL, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def _cpu_worker_init(seed, kind="port"):
+    global _W_SIG, _W_KIND
     from mpsft_gb300.signals import config2
     _W_SIG = config2(seed)
+    _W_KIND = kind
 
 
 def _cpu_worker_solve(rseed):
-    from oracle import oracle
-    port = oracle.Oracle("port")
+    port = _oracle_lib(_W_KIND)
     t0 = time.perf_counter()
     modes, _ = port.demo1_run(_W_SIG.x.astype(np.complex128), S, _W_SIG.sigma, rseed,
                               min_bins=51, window_delta=1e-5, max_stale_iter=5)
     return time.perf_counter() - t0, len(modes)
 
 
+def _time_build(kind: str, x, sigma, seconds: float, min_runs: int = 1):
+    port = _oracle_lib(kind)
+    done, t_total, sets = 0, 0.0, []
+    while t_total < seconds or done < min_runs:
+        t0 = time.perf_counter()
+        modes, _ = port.demo1_run(x, S, sigma, SEED_RNG + done, min_bins=51,
+                                  window_delta=1e-5, max_stale_iter=5)
+        t_total += time.perf_counter() - t0
+        sets.append(sorted(modes))
+        done += 1
+    return done, t_total, sets
+
+
+def faster_build(x, sigma) -> str:
+    """The faster oracle build on this host (two solves each, after one warm-up)."""
+    best, best_t = "port", None
+    for kind in _BUILDS:
+        _time_build(kind, x, sigma, 0.0)
+        _, t, _ = _time_build(kind, x, sigma, 0.0, min_runs=2)
+        if best_t is None or t < best_t:
+            best, best_t = kind, t
+    return best
+
+
 def cpu_baseline_single(seconds: float) -> dict:
-    """The oracle port on one host core, a bounded sample of whole solves."""
+    """The oracle port on one host core, a bounded sample of whole solves in
+    each build; the value is the faster build's."""
     from mpsft_gb300.signals import config2
-    from oracle import oracle
-    if not oracle.available("port"):
-        oracle.build_port()
-    port = oracle.Oracle("port")
     sg = config2(1001)
     x = sg.x.astype(np.complex128)
-    done, t_total = 0, 0.0
-    while t_total < seconds or done == 0:
-        t0 = time.perf_counter()
-        port.demo1_run(x, S, sg.sigma, SEED_RNG + done, min_bins=51,
-                       window_delta=1e-5, max_stale_iter=5)
-        t_total += time.perf_counter() - t0
-        done += 1
-    return {"value": done / t_total, "unit": "solves/s", "cores": 1,
+    res = {}
+    for kind in _BUILDS:
+        _time_build(kind, x, sg.sigma, 0.0)  # warm-up
+        res[kind] = _time_build(kind, x, sg.sigma, seconds / 2)
+    rates = {kind: d / t for kind, (d, t, _) in res.items()}
+    best = max(rates, key=rates.get)
+    d, t, _ = res[best]
+    n_same = min(len(v[2]) for v in res.values())
+    same = all(res["port"][2][i] == res["port_fast"][2][i] for i in range(n_same))
+    return {"value": rates[best], "unit": "solves/s", "cores": 1,
             "kind": "port",
-            "sample": f"{done} full config-2 recoveries on 1 core "
-                      f"({t_total:.1f} s, oracle/mpsft_oracle.cc, -O2 FP64)"}
+            "sample": f"{d} full config-2 recoveries on 1 core ({t:.1f} s, "
+                      f"oracle/mpsft_oracle.cc, {_BUILDS[best]}, FP64)",
+            "host": host_cpu(),
+            "builds": {_BUILDS[k]: v for k, v in rates.items()},
+            "builds_same_frequency_sets": same}
 
 
 def run_reference(args) -> None:
@@ -173,14 +225,14 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     import multiprocessing as mp
-    from oracle import oracle
-    if not oracle.available("port"):
-        oracle.build_port()
+    from mpsft_gb300.signals import config2
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") \
         else (os.cpu_count() or 1)
+    sg = config2(2024)
+    kind = faster_build(sg.x.astype(np.complex128), sg.sigma)
     ctxm = mp.get_context("spawn")
     step_times = []
-    with ctxm.Pool(cores, initializer=_cpu_worker_init, initargs=(2024,)) as pool:
+    with ctxm.Pool(cores, initializer=_cpu_worker_init, initargs=(2024, kind)) as pool:
         # warm-up: every worker builds its signal and runs once
         for w in range(args.warmup):
             pool.map(_cpu_worker_solve, [SEED_RNG + 1000 * w + i for i in range(cores)])
@@ -197,12 +249,14 @@ def run_reference(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "batch": cores,
-                   "implementation": "oracle port of the reference algorithm, "
+                   "implementation": "oracle port of the reference algorithm "
+                                     f"({_BUILDS[kind]}, the faster build here), "
                                      "one process per host core"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores,
                          "kind": "port",
                          "sample": f"{args.steps} steps x {cores} recoveries, one "
-                                   f"per core"},
+                                   f"per core",
+                         "host": host_cpu()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -210,6 +264,69 @@ def run_reference(args) -> None:
 
 
 # ----------------------------------------------------------------- GPU arm
+def dense_fft(torch, sigs_host, device, reps: int = 5) -> dict:
+    """Dense full-N FFTs of the same signals, the comparators of a sparse
+    recovery: scipy's FP64 FFT (pocketfft) on the host cores, one worker and
+    all of them, and cuFFT (through torch.fft) over the resident batch in
+    complex64 and complex128. Rates are transforms per second."""
+    import scipy.fft
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") \
+        else (os.cpu_count() or 1)
+    out = {"unit": "full-N transforms/s", "n": N}
+    x = sigs_host[0].x.astype(np.complex128)
+    for w in (1, cores):
+        scipy.fft.fft(x, workers=w)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            scipy.fft.fft(x, workers=w)
+        out[f"scipy_fft_f64_{w}_cores"] = reps / (time.perf_counter() - t0)
+    G = len(sigs_host)
+    xb = torch.empty((G, N), dtype=torch.complex64, device=device)
+    for i, sg in enumerate(sigs_host):
+        xb[i].copy_(torch.from_numpy(sg.x))
+    for name, dt in (("cufft_c64", torch.complex64), ("cufft_c128", torch.complex128)):
+        xt = xb if dt == torch.complex64 else xb.to(dt)
+        y = torch.fft.fft(xt)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            y = torch.fft.fft(xt)
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = G * reps / (e0.elapsed_time(e1) / 1e3)
+        del y, xt
+    out["cufft_batch"] = G
+    del xb
+    torch.cuda.empty_cache()
+    return out
+
+
+def accuracy(sg, k32, c32, k64, c64) -> dict:
+    """Errors of one recovery against an FP64 dense FFT x^ = fft(x)/N, as
+    Demo1::PostAnalyze (src/demo1.cc:61-112) reports them: found modes that
+    are true modes (hits) and the others (misses), the coefficient error of
+    the hits, and the precision error of the FP32 path against the FP64 path."""
+    x = sg.x.astype(np.complex128)
+    xf = np.fft.fft(x) / sg.n
+    true = set(int(v) for v in sg.k)
+
+    def errs(kk, cc):
+        hit = np.array([int(v) in true for v in kk], bool)
+        kh = np.asarray(kk)[hit].astype(np.int64)
+        d = np.asarray(cc)[hit] - xf[kh]
+        return {"hits": int(hit.sum()), "misses": int((~hit).sum()),
+                "algorithm_err": float(np.linalg.norm(d) / np.linalg.norm(xf[kh])),
+                "hit_l1_err": float(np.abs(d).mean())}
+
+    out = {"fp32_path": errs(k32, c32), "fp64_path": errs(k64, c64),
+           "true_modes": len(true)}
+    if np.array_equal(k32, k64):
+        out["precision_err"] = float(np.linalg.norm(c32 - c64) / np.linalg.norm(c64))
+    return out
+
+
 def load_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -465,7 +582,9 @@ def run_gpu(args) -> None:
                                     "ms_per_solve": 1e3 * t64,
                                     "iterations": st64.iterations},
                  "fp32_vs_fp64": {"same_frequency_set": same,
-                                  "coef_precision_err": perr}}
+                                  "coef_precision_err": perr},
+                 "accuracy": accuracy(sg0, k32, c32, k64, c64),
+                 "dense_fft": dense_fft(torch, sigs_host, torch.device("cuda", local))}
 
     if rank == 0:
         peaks = load_peaks()

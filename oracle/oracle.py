@@ -7,6 +7,9 @@ product path (``mpsft_gb300``) never does.
 * ``Oracle("port")`` loads ``oracle/liboracle.so``, this project's restatement
   of the reference algorithm (``oracle/mpsft_oracle.cc``). It is built from
   this directory on any host (``make liboracle``).
+* ``Oracle("port_fast")`` loads ``oracle/liboracle_fast.so``, the same
+  restatement built with the reference's optimised flags (-O3 -ffast-math,
+  ``make liboracle_fast``): for timing the CPU baseline only.
 * ``Oracle("ref")`` / ``Oracle("ref_pow2")`` load ``oracle/_ref/libref*.so``,
   the reference's own sources compiled here against stand-in headers
   (``make ref``); they exist only where the reference tree was present at
@@ -26,6 +29,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 _LIBS = {
     "port": os.path.join(HERE, "liboracle.so"),
+    "port_fast": os.path.join(HERE, "liboracle_fast.so"),
     "ref": os.path.join(HERE, "_ref", "libref.so"),
     "ref_pow2": os.path.join(HERE, "_ref", "libref_pow2.so"),
 }
@@ -40,6 +44,12 @@ def build_port() -> str:
     """Compile oracle/liboracle.so (g++ only)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle"], check=True)
     return _LIBS["port"]
+
+
+def build_port_fast() -> str:
+    """Compile oracle/liboracle_fast.so (g++ only; CPU-baseline timing)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle_fast"], check=True)
+    return _LIBS["port_fast"]
 
 
 def available(kind: str) -> bool:
