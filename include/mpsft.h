@@ -100,6 +100,9 @@ int mpsft_signal_free(mpsft_signal *sig);
  * an existing signal; pinned host memory makes the copy asynchronous with
  * respect to the host until the next solve call. */
 int mpsft_signal_write(mpsft_ctx *ctx, mpsft_signal *sig, const void *x_host);
+/* Copies the signal's n samples (its dtype) to host memory; returns when
+ * they are there. */
+int mpsft_signal_read(mpsft_ctx *ctx, const mpsft_signal *sig, void *x_host);
 
 /* mpsft_signal_write for count signals in one call, enqueued on stream (a
  * cudaStream_t; NULL = the context's stream). The call touches no context
@@ -264,6 +267,59 @@ int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                         mpsft_rng *const *rngs, int32_t *const *out_k,
                         double *const *out_c, const int32_t *cap,
                         int32_t *count, mpsft_stats *stats);
+
+/* ---- test data and result analysis (Demo1's constructor and PostAnalyze) -- */
+/* GenerateModeMap (src/gen.cc:27-39) on rng: count distinct positions
+ * k = RandomInt32() mod n, each with coefficient (RandomNormal(),
+ * RandomNormal()) / |.|, drawn in the reference's order from rng's one
+ * engine. Writes out_k[count] (in draw order) and out_c[2 count]
+ * (interleaved). Host only. */
+int mpsft_generate_mode_map(mpsft_rng *rng, int32_t n, int32_t count,
+                            int32_t *out_k, double *out_c);
+
+/* A signal generated on the device: x_t = sum_j coef_j e^{2 pi i k_j t / n}
+ * + noise_t, the unnormalised backward FFT of the spectrum that
+ * GenerateXhatAlt builds (src/gen.cc:77-89, src/demo1.cc:27-34). The mode
+ * part is an FP64 inverse FFT (cuFFT Z2Z, loaded at first use) of the
+ * sparse spectrum; noise_t is complex Gaussian with E|noise_t|^2 = sigma^2
+ * (real and imaginary parts N(0, sigma^2 / 2)), the time-domain form of
+ * GenerateXhatAlt's per-frequency variance sigma^2 / n, from a
+ * counter-based generator keyed by seed: sample t takes outputs 2t and 2t+1
+ * of the SplitMix64 sequence started at seed (u = ((z >> 11) + 1) 2^-53) through
+ * the Box-Muller transform. The values differ from the reference's
+ * sequential mt19937 draws; the distribution is the same. k must be distinct
+ * positions in [0, n); coef is interleaved (re, im); dtype MPSFT_C64 or
+ * MPSFT_C128 (the sum is formed in FP64, then rounded). */
+int mpsft_signal_generate(mpsft_ctx *ctx, int64_t n, const int32_t *k,
+                          const double *coef, int64_t count, double sigma,
+                          uint64_t seed, int dtype, mpsft_signal **out);
+
+/* xhat = FFT(x) / n of a resident signal in FP64 (cuFFT Z2Z forward):
+ * out receives n complex128 values, interleaved, in host or device memory
+ * (any pointer the CUDA runtime can address). */
+int mpsft_signal_spectrum(mpsft_ctx *ctx, const mpsft_signal *sig, double *out);
+
+/* Demo1::PostAnalyze (src/demo1.cc:61-112), computed on the device. */
+typedef struct {
+  int32_t hit;       /* found positions that are true positions */
+  int32_t miss;      /* the other found positions */
+  double hit_l1;     /* mean |c - xhat_k| over the hits (NaN when none) */
+  double hit_l2;     /* sqrt(mean |c - xhat_k|^2) over the hits */
+  double miss_l1;    /* the same over the misses */
+  double miss_l2;
+  double l1;         /* over all n frequencies, the found spectrum (c at */
+  double l2;         /* found positions, 0 elsewhere) against xhat: mean, */
+  double max_err;    /* root mean square and maximum of |difference| */
+} mpsft_analysis;
+
+/* Compares found modes (found_k distinct, found_c interleaved) with the true
+ * positions true_k and with the signal's spectrum xhat = FFT(x) / n (the
+ * reference compares with the generated spectrum, of which the signal is
+ * the exact backward transform). */
+int mpsft_post_analyze(mpsft_ctx *ctx, const mpsft_signal *sig,
+                       const int32_t *true_k, int64_t true_count,
+                       const int32_t *found_k, const double *found_c,
+                       int64_t found_count, mpsft_analysis *out);
 
 #ifdef __cplusplus
 }

@@ -68,6 +68,18 @@ class EstimateSetup(ctypes.Structure):
                 ("q", ctypes.c_int32 * 15)]
 
 
+class Analysis(ctypes.Structure):
+    """mpsft_analysis: Demo1::PostAnalyze's figures (src/demo1.cc:61-112)."""
+    _fields_ = [("hit", ctypes.c_int32), ("miss", ctypes.c_int32),
+                ("hit_l1", ctypes.c_double), ("hit_l2", ctypes.c_double),
+                ("miss_l1", ctypes.c_double), ("miss_l2", ctypes.c_double),
+                ("l1", ctypes.c_double), ("l2", ctypes.c_double),
+                ("max_err", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("found", ctypes.c_int32),
                 ("gathers", ctypes.c_int64), ("bin_bytes", ctypes.c_int64),
@@ -115,6 +127,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_signal_free": (I, [P]),
         "mpsft_signal_write": (I, [P, P, P]),
         "mpsft_signal_write_many": (I, [P, P, P, I32, P]),
+        "mpsft_signal_read": (I, [P, P, P]),
         "mpsft_bin_in_time": (I, [P, P, I32, I32, D, I32, I32, I32, I32, I, P, I]),
         "mpsft_bin_in_freq": (I, [P, I32, I32, I32, D, I32, I32, I32, I32, P, P,
                                   I64, P]),
@@ -128,6 +141,11 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                             ctypes.POINTER(Stats)]),
         "mpsft_solve_batched": (I, [P, P, ctypes.POINTER(SolveOptions), I32, P, P,
                                     P, P, P, ctypes.POINTER(Stats)]),
+        "mpsft_generate_mode_map": (I, [P, I32, I32, P, P]),
+        "mpsft_signal_generate": (I, [P, I64, P, P, I64, D, ctypes.c_uint64, I, PP]),
+        "mpsft_signal_spectrum": (I, [P, P, P]),
+        "mpsft_post_analyze": (I, [P, P, P, I64, P, P, I64,
+                                   ctypes.POINTER(Analysis)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -171,6 +189,15 @@ class Rng:
 
     def int32(self) -> int:
         return int(self._lib.mpsft_rng_int32(self._h))
+
+    def mode_map(self, n: int, count: int):
+        """GenerateModeMap (src/gen.cc:27-39) from this RNG: (positions in
+        draw order, unit-modulus complex128 coefficients)."""
+        k = np.zeros(count, np.int32)
+        c = np.zeros(count, np.complex128)
+        _check(None, self._lib.mpsft_generate_mode_map(self._h, int(n), int(count),
+                                                       _ptr(k), _ptr(c)))
+        return k, c
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -243,6 +270,43 @@ class Context:
         sg = Signal(self, h, n, dtype)
         self._signals.add(sg)
         return sg
+
+    def generate(self, n: int, k, coef, sigma: float, seed: int,
+                 dtype: int = C64) -> "Signal":
+        """A signal made on the device: sum_j coef_j e^{2 pi i k_j t/n} plus
+        complex Gaussian noise of per-sample variance sigma^2 from a
+        counter-based generator keyed by seed (mpsft_signal_generate)."""
+        k = np.ascontiguousarray(k, np.int32)
+        c = np.ascontiguousarray(coef, np.complex128)
+        if k.size != c.size:
+            raise ValueError("one coefficient per position")
+        h = ctypes.c_void_p()
+        _check(self, self._lib.mpsft_signal_generate(
+            self._h, int(n), _ptr(k), _ptr(c), k.size, float(sigma),
+            ctypes.c_uint64(int(seed) & (2**64 - 1)), int(dtype), ctypes.byref(h)))
+        sg = Signal(self, h, int(n), int(dtype))
+        self._signals.add(sg)
+        return sg
+
+    def spectrum(self, sig: "Signal") -> np.ndarray:
+        """xhat = FFT(x) / n in FP64, computed on the device."""
+        out = np.empty(sig.n, np.complex128)
+        _check(self, self._lib.mpsft_signal_spectrum(self._h, sig._h, _ptr(out)))
+        return out
+
+    def post_analyze(self, sig: "Signal", true_k, found_k, found_c) -> dict:
+        """Demo1::PostAnalyze (src/demo1.cc:61-112) on the device against the
+        signal's spectrum FFT(x)/n."""
+        tk = np.ascontiguousarray(true_k, np.int32)
+        fk = np.ascontiguousarray(found_k, np.int32)
+        fc = np.ascontiguousarray(found_c, np.complex128)
+        if fk.size != fc.size:
+            raise ValueError("one coefficient per found position")
+        a = Analysis()
+        _check(self, self._lib.mpsft_post_analyze(self._h, sig._h, _ptr(tk), tk.size,
+                                                  _ptr(fk), _ptr(fc), fk.size,
+                                                  ctypes.byref(a)))
+        return a.as_dict()
 
     def write_many(self, sigs: list, xs: list, stream_handle: int | None = None) -> None:
         """Refills many signals from host arrays (pinned memory for an
@@ -435,6 +499,12 @@ class Signal:
             raise ValueError("x must match the signal's n and dtype")
         _check(self.ctx, self.ctx._lib.mpsft_signal_write(self.ctx._h, self._h,
                                                           _ptr(x)))
+
+    def read(self) -> np.ndarray:
+        """The samples, copied to a new host array."""
+        x = np.empty(self.n, np.complex64 if self.dtype == C64 else np.complex128)
+        _check(self.ctx, self.ctx._lib.mpsft_signal_read(self.ctx._h, self._h, _ptr(x)))
+        return x
 
     def free(self) -> None:
         if not self._freed and self._h:

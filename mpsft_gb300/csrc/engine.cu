@@ -19,81 +19,10 @@
 #include <vector>
 
 #include "../../include/mpsft.h"
+#include "internal.h"
 #include "launch.h"
 
 using namespace mpsft;
-
-struct mpsft_ctx {
-  int device = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  // second stream, at the highest priority, for the kernels of an iteration
-  // that do not depend on the gather/fold (tables, mode preparation and
-  // bucketing): their few blocks go ahead of the fold's many, so that the
-  // FFT and the decisions do not wait for them
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // third stream, at the lowest priority, for the FP64 window tables (only
-  // the near-tie re-binning and the FP64 kernels use them): FP64
-  // transcendentals, slow on this part, that fill SMs the fold leaves idle
-  cudaStream_t side64 = nullptr;
-  cudaEvent_t ev_join64 = nullptr;
-  cudaEvent_t ev_fork_l = nullptr, ev_join_l = nullptr;  // listed-bin terms
-  cudaEvent_t ev_join_m = nullptr;  // merge of the bins not listed
-  cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
-  // stream the solve graph is captured on, and the last instantiated graph
-  cudaStream_t cap = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
-  std::vector<int64_t> graph_key;
-  // device solve state and draw tables of the current call (in the arena)
-  SolveCtl *d_solve_ctl = nullptr;
-  int32_t *d_draws = nullptr;
-  double *d_draw_bq = nullptr;
-  int64_t graph_body_kernels = 0;
-  bool graph_unavailable = false;
-  std::string err;
-  bool profiling = false;
-  float2 *tw32 = nullptr;
-  double2 *tw64 = nullptr;
-  // grow-only device arena reused across calls
-  unsigned char *arena = nullptr;
-  size_t arena_size = 0;
-  // pinned host staging for per-iteration control words
-  int32_t *h_ctl = nullptr;
-  size_t h_ctl_n = 0;
-  // pinned staging of exported mode tables
-  unsigned char *h_stage = nullptr;
-  // pinned, device-mapped staging of a solve's small uploads (copied by a
-  // kernel, see Upload), its device address and the bump offset
-  unsigned char *h_up = nullptr, *d_up = nullptr;
-  size_t h_up_n = 0, up_off = 0;
-  int64_t up_launches = 0;  // copy kernels Upload launched in this call
-  size_t h_stage_n = 0;
-  std::vector<cudaEvent_t> events;
-  // table cache of FP32 solves: window tables (FP32, FP64, float-float) and
-  // FP32 Bluestein tables per odd number of bins for one window delta, built
-  // on first use and kept, like FFT plans (win_dev: block offsets, valid and
-  // claim words, then the pool)
-  unsigned char *win_dev = nullptr;
-  size_t win_bytes = 0;
-  double win_delta = 0.0;
-  int32_t win_bmin = 0, win_bmax = 0;
-};
-
-struct mpsft_signal {
-  mpsft_ctx *ctx = nullptr;
-  void *d_x = nullptr;
-  int64_t n = 0;
-  int dtype = MPSFT_C64;
-  bool owned = false;
-};
-
-struct mpsft_rng {
-  std::mt19937 eng;
-  std::uniform_int_distribution<int32_t> uid;
-  int32_t Draw() { return uid(eng); }
-};
 
 namespace {
 
@@ -1629,6 +1558,7 @@ int mpsft_rng_seed(mpsft_rng *rng, int32_t seed) {
   if (!rng) return MPSFT_ERR_INVALID;
   rng->eng.seed(seed);
   rng->uid.reset();
+  rng->nd.reset();
   return MPSFT_OK;
 }
 int32_t mpsft_rng_int32(mpsft_rng *rng) { return rng ? rng->Draw() : -1; }
@@ -1721,6 +1651,18 @@ int mpsft_signal_write(mpsft_ctx *ctx, mpsft_signal *sig, const void *x_host) {
   const size_t bytes = size_t(sig->n) * (sig->dtype == MPSFT_C64 ? 8 : 16);
   MPSFT_CUDA(ctx, cudaMemcpyAsync(sig->d_x, x_host, bytes, cudaMemcpyHostToDevice,
                                   ctx->stream));
+  return MPSFT_OK;
+}
+
+int mpsft_signal_read(mpsft_ctx *ctx, const mpsft_signal *sig, void *x_host) {
+  if (!ctx || !sig || !x_host) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  if (sig->ctx != ctx) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "signal belongs to another context");
+  }
+  const size_t bytes = size_t(sig->n) * (sig->dtype == MPSFT_C64 ? 8 : 16);
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(x_host, sig->d_x, bytes, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return MPSFT_OK;
 }
 
@@ -2048,6 +1990,13 @@ int EstimateSetup(mpsft_ctx *ctx, int32_t n, const void *x,
 }
 
 }  // namespace
+
+namespace mpsft {
+int CtxFail(mpsft_ctx *ctx, int code, const std::string &msg) {
+  return Fail(ctx, code, msg);
+}
+int CtxCheckN(mpsft_ctx *ctx, int64_t n) { return CheckN(ctx, n); }
+}  // namespace mpsft
 
 extern "C" {
 

@@ -1,0 +1,100 @@
+// Definitions of the C ABI's opaque types, shared by the library's host
+// translation units (engine.cu: solves and bins; analysis.cu: signal
+// generation, dense spectra, result analysis).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/mpsft.h"
+#include "common.cuh"
+
+struct mpsft_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  // second stream, at the highest priority, for the kernels of an iteration
+  // that do not depend on the gather/fold (tables, mode preparation and
+  // bucketing): their few blocks go ahead of the fold's many, so that the
+  // FFT and the decisions do not wait for them
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // third stream, at the lowest priority, for the FP64 window tables (only
+  // the near-tie re-binning and the FP64 kernels use them): FP64
+  // transcendentals, slow on this part, that fill SMs the fold leaves idle
+  cudaStream_t side64 = nullptr;
+  cudaEvent_t ev_join64 = nullptr;
+  cudaEvent_t ev_fork_l = nullptr, ev_join_l = nullptr;  // listed-bin terms
+  cudaEvent_t ev_join_m = nullptr;  // merge of the bins not listed
+  cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
+  // stream the solve graph is captured on, and the last instantiated graph
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<int64_t> graph_key;
+  // device solve state and draw tables of the current call (in the arena)
+  mpsft::SolveCtl *d_solve_ctl = nullptr;
+  int32_t *d_draws = nullptr;
+  double *d_draw_bq = nullptr;
+  int64_t graph_body_kernels = 0;
+  bool graph_unavailable = false;
+  std::string err;
+  bool profiling = false;
+  float2 *tw32 = nullptr;
+  double2 *tw64 = nullptr;
+  // grow-only device arena reused across calls
+  unsigned char *arena = nullptr;
+  size_t arena_size = 0;
+  // pinned host staging for per-iteration control words
+  int32_t *h_ctl = nullptr;
+  size_t h_ctl_n = 0;
+  // pinned staging of exported mode tables
+  unsigned char *h_stage = nullptr;
+  // pinned, device-mapped staging of a solve's small uploads (copied by a
+  // kernel, see Upload), its device address and the bump offset
+  unsigned char *h_up = nullptr, *d_up = nullptr;
+  size_t h_up_n = 0, up_off = 0;
+  int64_t up_launches = 0;  // copy kernels Upload launched in this call
+  size_t h_stage_n = 0;
+  std::vector<cudaEvent_t> events;
+  // table cache of FP32 solves: window tables (FP32, FP64, float-float) and
+  // FP32 Bluestein tables per odd number of bins for one window delta, built
+  // on first use and kept, like FFT plans (win_dev: block offsets, valid and
+  // claim words, then the pool)
+  unsigned char *win_dev = nullptr;
+  size_t win_bytes = 0;
+  double win_delta = 0.0;
+  int32_t win_bmin = 0, win_bmax = 0;
+};
+
+struct mpsft_signal {
+  mpsft_ctx *ctx = nullptr;
+  void *d_x = nullptr;
+  int64_t n = 0;
+  int dtype = MPSFT_C64;
+  bool owned = false;
+};
+
+// The reference's global RNG state (src/base.cc:32-56) made explicit: one
+// engine shared by its integer and normal distributions.
+struct mpsft_rng {
+  std::mt19937 eng;
+  std::uniform_int_distribution<int32_t> uid;
+  std::normal_distribution<double> nd;
+  int32_t Draw() { return uid(eng); }
+  double Normal() { return nd(eng); }
+};
+
+namespace mpsft {
+
+// Records msg as the context's last error and returns code.
+int CtxFail(mpsft_ctx *ctx, int code, const std::string &msg);
+// MPSFT_OK when n is a length the solver supports (prime or a power of two in
+// [3, 2^31 - 1]); otherwise records why.
+int CtxCheckN(mpsft_ctx *ctx, int64_t n);
+
+}  // namespace mpsft

@@ -34,8 +34,10 @@ using ModeMap = std::unordered_map<int32_t, Cplex>;
 // uniform_int_distribution<int32_t> over [0, 2^31-1] (src/base.cc:32-56).
 std::mt19937 g_rng(123534);
 std::uniform_int_distribution<int32_t> g_uid32;
+std::normal_distribution<double> g_nd;
 
 int32_t DrawInt32() { return g_uid32(g_rng); }
+double DrawNormal() { return g_nd(g_rng); }
 
 // ---------------------------------------------------------------------------
 // Modular arithmetic in int64, truncated to int32 (src/integer.h:47-66).
@@ -568,6 +570,69 @@ int orc_demo1_run(int32_t n, const double *x, int32_t k, double sigma,
   }
   if (iters) *iters = it;
   return WriteSorted(found, out_k, out_c, cap);
+}
+
+int orc_generate_mode_map(int32_t n, int32_t k, int32_t *out_k, double *out_c) {
+  // GenerateModeMap (src/gen.cc:27-39): draw a position (RandomInt32() is
+  // non-negative, so UnsafePosMod is the remainder), skip repeats, then two
+  // normals for the coefficient. The reference builds the coefficient as
+  // Cplex(RandomNormal(), RandomNormal()); g++ evaluates those two arguments
+  // right to left, so the imaginary part takes the first draw.
+  ModeMap mm;
+  while (int32_t(mm.size()) < k) {
+    const int32_t idx = DrawInt32() % n;
+    if (mm.count(idx)) continue;
+    const double im = DrawNormal();
+    const double re = DrawNormal();
+    Cplex coef(re, im);
+    coef /= std::abs(coef);
+    mm[idx] = coef;
+  }
+  return WriteSorted(mm, out_k, out_c, k);
+}
+
+void orc_post_analyze(int32_t n, const double *xh, const int32_t *true_k,
+                      int32_t true_count, const int32_t *found_k,
+                      const double *found_c, int32_t found_count, double *out) {
+  // Demo1::PostAnalyze (src/demo1.cc:61-112): found modes at true positions
+  // are hits, the others misses, each with the error |c - xh_k|; then the
+  // sparse found spectrum against xh over all n frequencies.
+  const Cplex *x = AsCplex(xh);
+  std::unordered_map<int32_t, int> is_true;
+  for (int32_t i = 0; i < true_count; ++i) is_true[true_k[i]] = 1;
+  std::vector<Cplex> xh2(n, Cplex(0.0, 0.0));
+  int32_t hit = 0, miss = 0;
+  double hit_l1 = 0, hit_l2 = 0, miss_l1 = 0, miss_l2 = 0;
+  for (int32_t i = 0; i < found_count; ++i) {
+    const Cplex c(found_c[2 * i], found_c[2 * i + 1]);
+    xh2[found_k[i]] = c;
+    const double err = std::abs(c - x[found_k[i]]);
+    if (is_true.count(found_k[i])) {
+      ++hit;
+      hit_l1 += err;
+      hit_l2 += err * err;
+    } else {
+      ++miss;
+      miss_l1 += err;
+      miss_l2 += err * err;
+    }
+  }
+  double sum1 = 0, sum2 = 0, max_err = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    const double err = std::abs(xh2[i] - x[i]);
+    sum1 += err;
+    sum2 += err * err;
+    max_err = std::max(max_err, err);
+  }
+  out[0] = hit;
+  out[1] = hit_l1 / hit;
+  out[2] = std::sqrt(hit_l2 / hit);
+  out[3] = miss;
+  out[4] = miss_l1 / miss;
+  out[5] = std::sqrt(miss_l2 / miss);
+  out[6] = sum1 / n;
+  out[7] = std::sqrt(sum2 / n);
+  out[8] = max_err;
 }
 
 } // extern "C"

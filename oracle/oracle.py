@@ -84,6 +84,8 @@ class Oracle:
                                    _int, _int, _p, _p, _p, _i32]),
             "orc_demo1_run": (_int, [_i32, _p, _i32, _dbl, _i32, _i32, _dbl,
                                      _dbl, _i32, _i32, _p, _p, _i32, _p]),
+            "orc_generate_mode_map": (_int, [_i32, _i32, _p, _p]),
+            "orc_post_analyze": (None, [_i32, _p, _p, _i32, _p, _p, _i32, _p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -184,3 +186,28 @@ class Oracle:
         if m < 0:
             raise RuntimeError("mode capacity too small")
         return {int(ok[i]): complex(oc[i]) for i in range(m)}, int(iters[0])
+
+    # --- test data and analysis (src/gen.cc, src/demo1.cc) -----------------
+    def generate_mode_map(self, n: int, k: int, seed: int):
+        """GenerateModeMap after RandomSeed(seed): (positions sorted, coefs)."""
+        self.seed(seed)
+        ok = np.zeros(k, np.int32)
+        oc = np.zeros(k, np.complex128)
+        m = self.lib.orc_generate_mode_map(n, k, _ptr(ok), _ptr(oc))
+        return ok[:m].copy(), oc[:m].copy()
+
+    def post_analyze(self, xh: np.ndarray, true_k, found_k, found_c) -> dict:
+        """Demo1::PostAnalyze on spectrum xh: hit/miss counts and errors."""
+        xh = np.ascontiguousarray(xh, np.complex128)
+        tk = np.ascontiguousarray(true_k, np.int32)
+        fk = np.ascontiguousarray(found_k, np.int32)
+        fc = np.ascontiguousarray(found_c, np.complex128)
+        out = np.zeros(9, np.float64)
+        self.lib.orc_post_analyze(xh.size, _ptr(xh), _ptr(tk), tk.size, _ptr(fk),
+                                  _ptr(fc), fk.size, _ptr(out))
+        names = ["hit", "hit_l1", "hit_l2", "miss", "miss_l1", "miss_l2", "l1",
+                 "l2", "max_err"]
+        d = dict(zip(names, out.tolist()))
+        d["hit"] = int(d["hit"])
+        d["miss"] = int(d["miss"])
+        return d

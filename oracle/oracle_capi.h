@@ -80,6 +80,18 @@ int orc_demo1_run(int32_t n, const double *x, int32_t k, double sigma,
                   int32_t seed, int32_t *out_k, double *out_c, int32_t cap,
                   int32_t *iters);
 
+/* GenerateModeMap (src/gen.cc:27-39) on the global RNG: k distinct positions
+ * RandomInt32() mod n with coefficients (RandomNormal(), RandomNormal())
+ * normalised to modulus 1. Writes them sorted by position; returns k. */
+int orc_generate_mode_map(int32_t n, int32_t k, int32_t *out_k, double *out_c);
+
+/* Demo1::PostAnalyze (src/demo1.cc:61-112) for the spectrum xh (n values),
+ * the true positions true_k and the found modes (found_k, found_c). out
+ * receives {hit, hit_l1, hit_l2, miss, miss_l1, miss_l2, l1, l2, max_err}. */
+void orc_post_analyze(int32_t n, const double *xh, const int32_t *true_k,
+                      int32_t true_count, const int32_t *found_k,
+                      const double *found_c, int32_t found_count, double *out);
+
 #ifdef __cplusplus
 }
 #endif

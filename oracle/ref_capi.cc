@@ -7,6 +7,8 @@
 #include <cstring>
 #include <iostream>
 #include <memory>
+#include <sstream>
+#include <string>
 #include <unordered_map>
 #include <utility>
 #include <vector>
@@ -204,6 +206,39 @@ int orc_demo1_run(int32_t n, const double *x, int32_t k, double sigma,
   demo.Run();
   if (iters) *iters = -1;
   return WriteSorted(demo.found_mm_, out_k, out_c, cap);
+}
+
+int orc_generate_mode_map(int32_t n, int32_t k, int32_t *out_k, double *out_c) {
+  ModeMap mm;
+  GenerateModeMap(n, k, &mm);
+  return WriteSorted(mm, out_k, out_c, k);
+}
+
+void orc_post_analyze(int32_t n, const double *xh, const int32_t *true_k,
+                      int32_t true_count, const int32_t *found_k,
+                      const double *found_c, int32_t found_count, double *out) {
+  // Demo1::PostAnalyze itself on a Demo1 whose spectrum, true map and found
+  // map are the caller's (the constructor's own length-1 signal is replaced).
+  static Demo1Options opt;
+  Demo1 demo(opt, 1, 0, 1.0);
+  demo.x_.resize(n);
+  demo.xh_.resize(n);
+  CopyIn(xh, &demo.xh_);
+  demo.mm_.clear();
+  for (int32_t i = 0; i < true_count; ++i) demo.mm_[true_k[i]] = Cplex(1.0, 0.0);
+  demo.found_mm_.clear();
+  for (int32_t i = 0; i < found_count; ++i) {
+    demo.found_mm_[found_k[i]] = Cplex(found_c[2 * i], found_c[2 * i + 1]);
+  }
+  std::ostringstream os;
+  os.precision(17);
+  demo.PostAnalyze(os);
+  std::istringstream is(os.str());
+  for (int i = 0; i < 9; ++i) {
+    std::string tok;
+    is >> tok;
+    out[i] = std::strtod(tok.c_str(), nullptr);
+  }
 }
 
 } // extern "C"

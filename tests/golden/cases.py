@@ -70,3 +70,30 @@ def solve_signal(case) -> tuple[np.ndarray, float]:
         sig = make_signal(n, s, sseed, magnitude="loguniform", snr_db=60.0,
                           dtype=np.complex64)
     return sig.x, sig.sigma
+
+
+# GenerateModeMap cases (src/gen.cc:27-39): (n, k, seed of RandomSeed).
+MODE_MAPS = [(1 << 20, 50, 123534), (65537, 300, 5), (1009, 1000, 77)]
+
+# PostAnalyze cases (src/demo1.cc:61-112): (name, n, seed, true count,
+# found true count, found false count, error scale of the found coefficients).
+POST_ANALYZE = [
+    ("mixed", 4099, 3, 60, 50, 7, 0.01),
+    ("no_miss", 1 << 12, 4, 40, 40, 0, 1e-3),
+    ("far_off", 1 << 13, 5, 30, 10, 20, 10.0),
+]
+
+
+def post_analyze_inputs(case):
+    """(xh, true positions, found positions, found coefficients) of a case."""
+    _, n, seed, nt, nhit, nmiss, scale = case
+    rng = np.random.default_rng(seed)
+    xh = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2 * n)
+    tk = rng.choice(n, nt, replace=False)
+    xh[tk] += np.exp(2j * np.pi * rng.uniform(size=nt))
+    others = np.setdiff1d(np.arange(n), tk)
+    fk = np.concatenate([tk[:nhit], rng.choice(others, nmiss, replace=False)])
+    fc = xh[fk] + scale * (rng.standard_normal(fk.size)
+                           + 1j * rng.standard_normal(fk.size))
+    return xh, tk.astype(np.int32), fk.astype(np.int32), fc
+

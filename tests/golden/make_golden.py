@@ -26,6 +26,10 @@ from oracle.oracle import Oracle  # noqa: E402
 import cases  # noqa: E402
 
 
+PA_KEYS = ["hit", "hit_l1", "hit_l2", "miss", "miss_l1", "miss_l2", "l1", "l2",
+           "max_err"]
+
+
 def main() -> None:
     ref = Oracle("ref")
     ref2 = Oracle("ref_pow2")
@@ -119,6 +123,16 @@ def main() -> None:
         out[f"solve_{name}_k"] = kk
         out[f"solve_{name}_c"] = np.array([modes[k] for k in kk], np.complex128)
         out[f"solve_{name}_sigma"] = np.array([sigma])
+
+    # GenerateModeMap and Demo1::PostAnalyze.
+    for i, (n, k, seed) in enumerate(cases.MODE_MAPS):
+        kk, cc = ref.generate_mode_map(n, k, seed)
+        out[f"mm{i}_k"] = kk
+        out[f"mm{i}_c"] = cc
+    for case in cases.POST_ANALYZE:
+        xh, tk, fk, fc = cases.post_analyze_inputs(case)
+        r = ref.post_analyze(xh, tk, fk, fc)
+        out[f"pa_{case[0]}"] = np.array([r[k] for k in PA_KEYS], np.float64)
 
     path = os.path.join(HERE, "ref_golden.npz")
     np.savez_compressed(path, **out)

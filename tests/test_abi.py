@@ -65,3 +65,23 @@ def test_null_arguments_are_rejected(lib):
     assert lib.mpsft_solve(None, None, None, None, None, None, 0, None, None) \
         == m.ERR_INVALID
     assert lib.mpsft_rng_seed(None, 1) == m.ERR_INVALID
+
+
+@pytest.mark.parametrize("i", range(3))
+def test_mode_map_matches_reference(lib, golden, i):
+    """mpsft_generate_mode_map (host) against GenerateModeMap's own output
+    (src/gen.cc:27-39): same positions, coefficients bit for bit."""
+    import cases
+    n, k, seed = cases.MODE_MAPS[i]
+    kk, cc = m.Rng(seed).mode_map(n, k)
+    order = np.argsort(kk)
+    assert np.array_equal(kk[order], golden[f"mm{i}_k"])
+    assert np.array_equal(cc[order], golden[f"mm{i}_c"])
+    # positions in draw order are distinct
+    assert len(set(kk.tolist())) == k
+
+
+def test_mode_map_rejects_bad_arguments(lib):
+    r = m.Rng(1)
+    assert lib.mpsft_generate_mode_map(r._h, 10, 11, None, None) == m.ERR_INVALID
+    assert lib.mpsft_generate_mode_map(None, 10, 1, None, None) == m.ERR_INVALID

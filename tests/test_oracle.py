@@ -215,3 +215,33 @@ def test_port_bit_exact_vs_reference_here(port, seed):
     a |= 1
     assert np.array_equal(port.bin_in_time(x, bins, bits, 1e-5, a, b, c, q),
                           ref.bin_in_time(x, bins, bits, 1e-5, a, b, c, q))
+
+
+# ------------------------------------------- test data and analysis (gen, demo1)
+@pytest.mark.parametrize("i", range(len(cases.MODE_MAPS)))
+def test_mode_map_matches_reference(port, golden, i):
+    """GenerateModeMap (src/gen.cc:27-39): same positions and coefficients."""
+    n, k, seed = cases.MODE_MAPS[i]
+    kk, cc = port.generate_mode_map(n, k, seed)
+    assert np.array_equal(kk, golden[f"mm{i}_k"])
+    assert np.array_equal(cc, golden[f"mm{i}_c"])
+    assert np.allclose(np.abs(cc), 1.0, rtol=0, atol=1e-15)
+
+
+PA_KEYS = ["hit", "hit_l1", "hit_l2", "miss", "miss_l1", "miss_l2", "l1", "l2",
+           "max_err"]
+
+
+@pytest.mark.parametrize("case", cases.POST_ANALYZE, ids=[c[0] for c in cases.POST_ANALYZE])
+def test_post_analyze_matches_reference(port, golden, case):
+    """Demo1::PostAnalyze (src/demo1.cc:61-112): counts equal, errors within
+    1e-12 relative (summation order differs); no misses gives NaN as the
+    reference's 0/0 does."""
+    xh, tk, fk, fc = cases.post_analyze_inputs(case)
+    got = port.post_analyze(xh, tk, fk, fc)
+    want = golden[f"pa_{case[0]}"]
+    for j, key in enumerate(PA_KEYS):
+        if np.isnan(want[j]):
+            assert np.isnan(got[key]), key
+        else:
+            assert abs(got[key] - want[j]) <= 1e-12 * abs(want[j]), key
