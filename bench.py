@@ -17,8 +17,15 @@ every signal and device-to-host read of every result inside the timed region;
 the next step's copies run on a copy stream during the current step's solve).
 
 ``--impl reference`` times the reference's algorithm on the host cores: the
-oracle's FP64 restatement (oracle/liboracle.so), one process per core, each
-recovering its own signal of the same configuration.
+oracle's FP64 restatement (oracle/liboracle.so, or liboracle_fast.so with the
+reference's -O3 -ffast-math flags when that build is faster here), one
+process per core, each recovering its own signal of the same configuration.
+
+Also reported (rank 0): the plain per-signal FP64 GPU path, the accuracy of
+one recovery against an FP64 dense FFT (hits, misses, algorithm and precision
+errors), dense full-N FFT rates (scipy on the host cores, cuFFT on the
+device), and the device test-data pipeline (generation, PostAnalyze) against
+its host form.
 
 Multi-GPU: one process per GPU under torchrun; every rank recovers its own G
 signals (independent replicas, no collective on the data path); the time is the
@@ -303,6 +310,43 @@ def dense_fft(torch, sigs_host, device, reps: int = 5) -> dict:
     return out
 
 
+def test_data_pipeline(ctx, m, sg, k32, c32, reps: int = 5) -> dict:
+    """Demo1's constructor and PostAnalyze for one config-2 signal, on the
+    device (mpsft_signal_generate, mpsft_post_analyze) and on the host
+    (numpy's FFT and normal draws; the oracle's PostAnalyze over a numpy
+    spectrum). Times in ms per signal, each call synchronous."""
+    from mpsft_gb300.signals import make_signal
+    out = {}
+    sig = ctx.generate(sg.n, sg.k, sg.c, sg.sigma, 1, m.C64)
+    sig.free()
+    t0 = time.perf_counter()
+    for r in range(reps):
+        sig = ctx.generate(sg.n, sg.k, sg.c, sg.sigma, 1 + r, m.C64)
+        sig.free()
+    out["generate_device_ms"] = 1e3 * (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    make_signal(sg.n, S, 99, magnitude="loguniform", mag_range=(1e-2, 1.0),
+                snr_db=60.0)
+    out["generate_host_ms"] = 1e3 * (time.perf_counter() - t0)
+    sig = ctx.upload(sg.x)
+    ctx.post_analyze(sig, sg.k, k32, c32)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        dev = ctx.post_analyze(sig, sg.k, k32, c32)
+    out["post_analyze_device_ms"] = 1e3 * (time.perf_counter() - t0) / reps
+    sig.free()
+    port = _oracle_lib("port")
+    t0 = time.perf_counter()
+    host = port.post_analyze(np.fft.fft(sg.x.astype(np.complex128)) / sg.n, sg.k,
+                             k32, c32)
+    out["post_analyze_host_ms"] = 1e3 * (time.perf_counter() - t0)
+    out["post_analyze_same"] = all(
+        (np.isnan(host[key]) and np.isnan(dev[key])) or
+        abs(host[key] - dev[key]) <= 1e-9 * abs(host[key]) for key in host)
+    out["analysis"] = dev
+    return out
+
+
 def accuracy(sg, k32, c32, k64, c64) -> dict:
     """Errors of one recovery against an FP64 dense FFT x^ = fft(x)/N, as
     Demo1::PostAnalyze (src/demo1.cc:61-112) reports them: found modes that
@@ -584,6 +628,7 @@ def run_gpu(args) -> None:
                  "fp32_vs_fp64": {"same_frequency_set": same,
                                   "coef_precision_err": perr},
                  "accuracy": accuracy(sg0, k32, c32, k64, c64),
+                 "test_data_pipeline": test_data_pipeline(ctx, m, sg0, k32, c32),
                  "dense_fft": dense_fft(torch, sigs_host, torch.device("cuda", local))}
 
     if rank == 0:
