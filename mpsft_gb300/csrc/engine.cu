@@ -585,16 +585,31 @@ Maxima MaximaOf(const std::vector<SigIter> &h_its) {
 // The kernels of one iteration of every active signal, on stream s (and the
 // context's side stream, forked from and joined back into s). any_forced:
 // some signal of an FP32 call takes the FP64 kernels (precision policy).
+// The fixed-bins phase's pipelined body: while this iteration decides, the
+// next one (descriptors its_ahead) is planned and gathered/folded on the
+// prefold stream. Only the row FFT reads the fold buffer, so the next fold
+// starts once this iteration's FFT is done.
+struct Ahead {
+  SigIter *its_ahead;
+  SolveCtl *ctl;
+  int32_t plan_max;
+};
+
 int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
                            const Maxima &mx, bool x_c128, bool fp64,
                            bool any_forced, BinTimer *timer, int64_t *launched,
-                           cudaStream_t s) {
+                           cudaStream_t s, const Ahead *ahead = nullptr) {
   if (mx.bins == 0) return MPSFT_OK;
   // fork: tables, mode preparation and bucketing on the side stream while
-  // the window and the gather/fold run on the main one
+  // the window and the gather/fold run on the main one; the row FFT waits
+  // for the Bluestein tables only, the decisions for the rest (ahead: this
+  // iteration's tables were set up with its fold, in the previous body)
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-  LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
+  if (!ahead) {
+    LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_blue, ctx->side));
+  }
   LaunchModePrep(d_its, nsig, mx.cap, ctx->side);
   LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
@@ -608,7 +623,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   }
   if (fp64) {
     LaunchWindow(d_its, nsig, mx.p2, s);
-  } else {
+  } else if (!ahead) {
     LaunchWindow32(d_its, nsig, mx.p2, s);
   }
   if (timer && ctx->profiling) {
@@ -623,14 +638,30 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     int rc = timer->Begin();
     if (rc) return rc;
   }
-  LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, fp64, s);
+  if (!ahead) LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, fp64, s);
   if (timer) {
     int rc = timer->End();
     if (rc) return rc;
   }
-  MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));  // join
+  if (!ahead) MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_blue, 0));
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
+  if (ahead) {
+    // the next iteration's plan, window, gather/fold and Bluestein tables
+    // (only this iteration's row FFT, now done, read the fold buffer and
+    // the Bluestein tables)
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_p, s));
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->pre, ctx->ev_fork_p, 0));
+    LaunchPlan(ahead->ctl, ahead->its_ahead, nsig, ahead->plan_max, ctx->pre, true);
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_plan_p, ctx->pre));
+    LaunchWindow32(ahead->its_ahead, nsig, mx.p2, ctx->pre);
+    LaunchBinFold(ahead->its_ahead, nsig, mx.bins, mx.bits, mx.trials, x_c128, false,
+                  ctx->pre);
+    LaunchBluesteinSetup(ahead->its_ahead, nsig, mx.m, false, ctx->tw32, ctx->tw64,
+                         ctx->pre);
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_p, ctx->pre));
+  }
+  MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));  // join
   // near ties of the FP32 pass: listed bins re-binned and re-decided in
   // FP64; signals that the precision policy sends to FP64 (and signals whose
   // near-tie list overflowed) run the FP64 kernels (redo). Without redo the
@@ -640,7 +671,8 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   const bool side_merge = !fp64 && !redo;
   LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s, false, side_merge);
   // Bluestein setup, mode preparation, bucketing, window(s), fold, FFT, decide
-  if (launched) *launched += fp64 ? 7 : 8;
+  // (ahead: the next iteration's plan in addition)
+  if (launched) *launched += (fp64 ? 7 : 8) + (ahead ? 1 : 0);
   if (!fp64) {
     // side stream: the listed bins' FP64 mode terms (before any merge
     // changes a coefficient), then the merge of the other bins, beside the
@@ -818,7 +850,8 @@ void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
 int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
               const mpsft_solve_options *opts, int nsig,
               mpsft_rng *const *rngs, const std::vector<Shape> &shapes,
-              SigIter *d_its, std::vector<SigIter> *its, DrawTables *dt,
+              SigIter *d_its, SigIter *d_its_ahead, std::vector<SigIter> *its,
+              DrawTables *dt,
               const std::vector<int32_t> &force, bool any_forced, bool fp64,
               bool x_c128, int64_t *launches) {
   const int tmax = dt->tmax;
@@ -849,7 +882,10 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     it.active = 0;
   }
   {
-    const int rc = Upload(ctx, d_its, its->data(), sizeof(SigIter) * nsig, ctx->stream);
+    int rc = Upload(ctx, d_its, its->data(), sizeof(SigIter) * nsig, ctx->stream);
+    if (rc == MPSFT_OK) {
+      rc = Upload(ctx, d_its_ahead, its->data(), sizeof(SigIter) * nsig, ctx->stream);
+    }
     if (rc) return rc;
   }
   std::vector<SolveCtl> &hc = dt->hc;
@@ -888,11 +924,13 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       }
     }
   }
+  // the fixed-bins phase runs pipelined on the FP32 path without FP64 redo
+  const bool pipe = !fp64 && !(any_forced && mx.m <= kMaxFFT64);
   // graph (rebuilt when the launch shape or the arena changes)
   const std::vector<int64_t> key = {
       int64_t(reinterpret_cast<uintptr_t>(ctx->arena)), nsig, mx.bins, mx.bits,
       mx.rows, mx.p2, mx.m, mx.cap, mx.trials, fp64, x_c128, any_forced,
-      small_bins, mx_small.p2};
+      small_bins, mx_small.p2, pipe};
   if (ctx->graph_key != key || ctx->graph_exec == nullptr) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -906,23 +944,60 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     // One while node per phase: the first runs every signal with launch
     // shapes for the largest bins; once no signal needs more than small_bins,
     // the second runs with shapes for small_bins (the late iterations, where
-    // most of a solve's iterations are, then launch no idle blocks).
+    // most of a solve's iterations are, then launch no idle blocks). With
+    // pipelining, the second ends when every signal with work is at fixed
+    // bins (min_bins from then on), and a third runs the rest with the next
+    // iteration's plan and gather/fold beside the current one's decisions,
+    // after a prologue that plans and folds its first iteration.
     struct Phase {
       Maxima shape;
       int32_t plan_max, cond_lo, cond_hi;
+      bool exclude_fixed, pipelined;
     };
     std::vector<Phase> phases;
     if (two_phase) {
-      phases.push_back({mx, INT32_MAX, small_bins, INT32_MAX});
-      phases.push_back({mx_small, small_bins, 0, small_bins});
+      phases.push_back({mx, INT32_MAX, small_bins, INT32_MAX, false, false});
+      phases.push_back({mx_small, small_bins, 0, small_bins, pipe, false});
     } else {
-      phases.push_back({mx, INT32_MAX, 0, INT32_MAX});
+      phases.push_back({mx, INT32_MAX, 0, INT32_MAX, pipe, false});
+    }
+    if (pipe) {
+      Phase last = phases.back();
+      last.exclude_fixed = false;
+      last.pipelined = true;
+      phases.push_back(last);
     }
     int rc = MPSFT_OK;
     cudaError_t ce = cudaSuccess;
     int64_t per_body = 1;
     cudaGraphNode_t prev = nullptr;
     for (const Phase &ph : phases) {
+      if (ph.pipelined) {
+        // prologue: plan, fold and Bluestein tables of the phase's first
+        // iteration
+        cudaGraph_t pg = nullptr;
+        MPSFT_CUDA(ctx, cudaGraphCreate(&pg, 0));
+        ce = cudaStreamBeginCaptureToGraph(ctx->cap, pg, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+          LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ph.plan_max, ctx->cap);
+          LaunchWindow32(d_its, nsig, ph.shape.p2, ctx->cap);
+          LaunchBinFold(d_its, nsig, ph.shape.bins, ph.shape.bits, ph.shape.trials,
+                        x_c128, false, ctx->cap);
+          LaunchBluesteinSetup(d_its, nsig, ph.shape.m, false, ctx->tw32, ctx->tw64,
+                               ctx->cap);
+          cudaGraph_t captured = nullptr;
+          ce = cudaStreamEndCapture(ctx->cap, &captured);
+        }
+        cudaGraphNode_t child = nullptr;
+        if (ce == cudaSuccess) {
+          ce = cudaGraphAddChildGraphNode(&child, g, prev ? &prev : nullptr,
+                                          prev ? 1 : 0, pg);
+        }
+        cudaGraphDestroy(pg);  // the node holds its own copy
+        if (ce != cudaSuccess) break;
+        prev = child;
+      }
       cudaGraphConditionalHandle handle;
       MPSFT_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, g, 1,
                                                        cudaGraphCondAssignDefault));
@@ -941,14 +1016,29 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       cudaGraph_t body = p.conditional.phGraph_out[0];
       MPSFT_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->cap, body, nullptr, nullptr,
                                                     0, cudaStreamCaptureModeThreadLocal));
-      LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ph.plan_max, ctx->cap);
+      if (!ph.pipelined) LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ph.plan_max, ctx->cap);
       per_body = 1;
+      const Ahead ah{d_its_ahead, ctx->d_solve_ctl, ph.plan_max};
       rc = LaunchIterationKernels(ctx, d_its, nsig, ph.shape, x_c128, fp64,
-                                  any_forced, nullptr, &per_body, ctx->cap);
-      LaunchFinish(ctx->d_solve_ctl, d_its, nsig, handle, true, ph.cond_lo,
-                   ph.cond_hi, ctx->cap);
+                                  any_forced, nullptr, &per_body, ctx->cap,
+                                  ph.pipelined ? &ah : nullptr);
+      cudaError_t we = cudaSuccess;
+      if (ph.pipelined) {
+        // the stop rule after the plan ahead has read the solve state; the
+        // planned descriptors become current once the next fold is done
+        we = cudaStreamWaitEvent(ctx->cap, ctx->ev_plan_p, 0);
+        LaunchFinish(ctx->d_solve_ctl, d_its, nsig, handle, true, ph.cond_lo,
+                     ph.cond_hi, ctx->cap, d_its_ahead, false);
+        if (we == cudaSuccess) we = cudaStreamWaitEvent(ctx->cap, ctx->ev_join_p, 0);
+        LaunchCopyMapped(d_its_ahead, d_its, sizeof(SigIter) * nsig, ctx->cap);
+        per_body += 1;
+      } else {
+        LaunchFinish(ctx->d_solve_ctl, d_its, nsig, handle, true, ph.cond_lo,
+                     ph.cond_hi, ctx->cap, nullptr, ph.exclude_fixed);
+      }
       cudaGraph_t captured = nullptr;
       ce = cudaStreamEndCapture(ctx->cap, &captured);
+      if (ce == cudaSuccess) ce = we;
       if (rc != MPSFT_OK || ce != cudaSuccess) break;
     }
     cudaGraphExec_t exec = nullptr;
@@ -1096,7 +1186,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     CarveSignal(probe, s, &dummy, &ctl);
     bytes += probe.off + 256;
   }
-  bytes += sizeof(SigIter) * nsig + 256;
+  bytes += 2 * (sizeof(SigIter) * nsig + 256);
   bytes += (sizeof(double) * kEnergyStride + sizeof(void *) + sizeof(int64_t)) *
                nsig + 1024;
   int max_trials_all = 1;
@@ -1116,6 +1206,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
 
   Carve cv{ctx->arena};
   SigIter *d_its = cv.take<SigIter>(nsig);
+  SigIter *d_its_ahead = cv.take<SigIter>(nsig);  // fixed-bins phase
   double *d_energy = cv.take<double>(size_t(kEnergyStride) * nsig);
   const void **d_xs = cv.take<const void *>(nsig);
   int64_t *d_ns = cv.take<int64_t>(nsig);
@@ -1135,10 +1226,10 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     its[i].n = int32_t(sigs[i]->n);
     phase_entries = std::max(phase_entries, PhaseTableEntries(sigs[i]->n));
   }
-  // the call's small uploads (descriptors twice, signal pointers and lengths,
-  // draw tables, solve state) fit the staging without a wait
+  // the call's small uploads (descriptors three times, signal pointers and
+  // lengths, draw tables, solve state) fit the staging without a wait
   rc = EnsureUploadStage(
-      ctx, 2 * sizeof(SigIter) * nsig + 16 * size_t(nsig) +
+      ctx, 3 * sizeof(SigIter) * nsig + 16 * size_t(nsig) +
                size_t(nsig) * kDrawChunk * (4 + max_trials_all) * sizeof(int32_t) +
                size_t(nsig) * kDrawChunk * max_trials_all * 2 * sizeof(double) +
                sizeof(SolveCtl) * nsig + 16 * 256);
@@ -1225,7 +1316,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
   if (!host_loop) {
-    rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, &its, &draws,
+    rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, d_its_ahead, &its, &draws,
                    force, any_forced, fp64, x_c128, &launches);
     if (rc == kGraphUnavailable) {
       // no iteration ran and the tables are untouched; the RNGs are back
@@ -1454,6 +1545,9 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   if (e == cudaSuccess) {
     e = cudaStreamCreateWithPriority(&ctx->side64, cudaStreamNonBlocking, prio_least);
   }
+  if (e == cudaSuccess) {
+    e = cudaStreamCreateWithPriority(&ctx->pre, cudaStreamNonBlocking, prio_least);
+  }
   // the solve graph's main chain sits between the two side streams
   if (e == cudaSuccess) {
     e = cudaStreamCreateWithPriority(&ctx->cap, cudaStreamNonBlocking,
@@ -1463,10 +1557,14 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_loop1);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_blue, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join64, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork_l, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_l, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_m, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork_p, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_plan_p, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_p, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
   if (e != cudaSuccess) {
@@ -1512,6 +1610,10 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
     cudaStreamSynchronize(ctx->side);
     cudaStreamDestroy(ctx->side);
   }
+  if (ctx->pre) {
+    cudaStreamSynchronize(ctx->pre);
+    cudaStreamDestroy(ctx->pre);
+  }
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   if (ctx->cap) cudaStreamDestroy(ctx->cap);
@@ -1519,10 +1621,14 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->ev_loop0) cudaEventDestroy(ctx->ev_loop0);
   if (ctx->ev_loop1) cudaEventDestroy(ctx->ev_loop1);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->ev_blue) cudaEventDestroy(ctx->ev_blue);
   if (ctx->ev_join64) cudaEventDestroy(ctx->ev_join64);
   if (ctx->ev_fork_l) cudaEventDestroy(ctx->ev_fork_l);
   if (ctx->ev_join_l) cudaEventDestroy(ctx->ev_join_l);
   if (ctx->ev_join_m) cudaEventDestroy(ctx->ev_join_m);
+  if (ctx->ev_fork_p) cudaEventDestroy(ctx->ev_fork_p);
+  if (ctx->ev_plan_p) cudaEventDestroy(ctx->ev_plan_p);
+  if (ctx->ev_join_p) cudaEventDestroy(ctx->ev_join_p);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return MPSFT_OK;

@@ -23,6 +23,7 @@ struct mpsft_ctx {
   // FFT and the decisions do not wait for them
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_blue = nullptr;  // Bluestein tables (the row FFT waits for them)
   // third stream, at the lowest priority, for the FP64 window tables (only
   // the near-tie re-binning and the FP64 kernels use them): FP64
   // transcendentals, slow on this part, that fill SMs the fold leaves idle
@@ -30,6 +31,10 @@ struct mpsft_ctx {
   cudaEvent_t ev_join64 = nullptr;
   cudaEvent_t ev_fork_l = nullptr, ev_join_l = nullptr;  // listed-bin terms
   cudaEvent_t ev_join_m = nullptr;  // merge of the bins not listed
+  // fourth stream, at the lowest priority: in the fixed-bins phase, the plan
+  // and gather/fold of the next iteration while the current one decides
+  cudaStream_t pre = nullptr;
+  cudaEvent_t ev_fork_p = nullptr, ev_plan_p = nullptr, ev_join_p = nullptr;
   cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
   // stream the solve graph is captured on, and the last instantiated graph
   cudaStream_t cap = nullptr;

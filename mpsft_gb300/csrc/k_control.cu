@@ -14,6 +14,13 @@
 // stale one when nothing was found, stop after max_stale_iter stale ones (never
 // reset), on a status, or at max_iter; then it sets the while condition to
 // "some signal still has work and draws".
+//
+// Fixed bins: once 2 (k - found) + 1 <= min_bins, every later iteration of a
+// signal has bins = min_bins (found never decreases). When every signal of a
+// batch is there, the next iteration can be planned ahead ("ahead" plan,
+// into a second descriptor array) and its gather/fold run while the current
+// iteration decides; k_finish then drops the planned iteration of a signal
+// that stopped.
 #include <algorithm>
 
 #include "common.cuh"
@@ -41,19 +48,21 @@ __device__ inline int32_t NextBins(const SolveCtl &c, const SigIter &it) {
 }
 
 // max_bins: signals needing more bins wait (the launch shapes of this body
-// do not cover them).
+// do not cover them). ahead = 1 plans iteration iter + 1 of a signal in the
+// fixed-bins state while iteration iter runs (bins = min_bins; the flags,
+// which iteration iter still uses, are cleared by its k_finish instead).
 __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
-                       int nsig, int32_t max_bins) {
+                       int nsig, int32_t max_bins, int ahead) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nsig) return;
   SolveCtl &c = ctl[i];
   SigIter &it = its[i];
-  const int local = c.iter - c.draw_base;
+  const int local = c.iter + ahead - c.draw_base;
   if (c.done || local >= c.draws_avail) {
     it.active = 0;
     return;
   }
-  const int32_t bins = NextBins(c, it);
+  const int32_t bins = ahead ? c.min_bins : NextBins(c, it);
   if (bins > max_bins) {
     it.active = 0;
     return;
@@ -138,18 +147,23 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
   } else {
     it.tables_valid = (c.last_bins == bins && !c.force_fp64) ? 1 : 0;
   }
-  it.flags[0] = 0;
-  it.flags[1] = 0;
-  it.flags[2] = 0;
+  if (!ahead) {
+    it.flags[0] = 0;
+    it.flags[1] = 0;
+    it.flags[2] = 0;
+  }
   it.active = 1;
 }
 
 // The while condition: some signal has work (not stopped, draws left) and
-// its next iteration's bins lie in (cond_lo, cond_hi].
+// its next iteration's bins lie in (cond_lo, cond_hi] (and, with
+// exclude_fixed, exceed its min_bins). its_ahead (or null): the iteration
+// planned ahead (pipelined body).
 __global__ void __launch_bounds__(1024)
     k_finish(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its, int nsig,
              cudaGraphConditionalHandle handle, int set_condition,
-             int32_t cond_lo, int32_t cond_hi) {
+             int32_t cond_lo, int32_t cond_hi, SigIter *__restrict__ its_ahead,
+             int exclude_fixed) {
   int any = 0;
   for (int i = threadIdx.x; i < nsig; i += blockDim.x) {
     SolveCtl &c = ctl[i];
@@ -183,9 +197,17 @@ __global__ void __launch_bounds__(1024)
       if (it.win_slot >= 0) c.win_valid[it.win_slot] = 1;
       it.active = 0;
     }
+    if (its_ahead != nullptr) {
+      if (c.done) its_ahead[i].active = 0;
+      it.flags[0] = 0;
+      it.flags[1] = 0;
+      it.flags[2] = 0;
+    }
     if (!c.done && c.iter - c.draw_base < c.draws_avail) {
       const int32_t nb = NextBins(c, it);
-      if (nb > cond_lo && nb <= cond_hi) any = 1;
+      if (nb > cond_lo && nb <= cond_hi && !(exclude_fixed && nb <= c.min_bins)) {
+        any = 1;
+      }
     }
   }
   any = __syncthreads_or(any);
@@ -244,15 +266,16 @@ void LaunchDelay(unsigned long long ns, cudaStream_t s) {
 }
 
 void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, int32_t max_bins,
-                cudaStream_t s) {
-  k_plan<<<(nsig + 127) / 128, 128, 0, s>>>(ctl, its, nsig, max_bins);
+                cudaStream_t s, bool ahead) {
+  k_plan<<<(nsig + 127) / 128, 128, 0, s>>>(ctl, its, nsig, max_bins, ahead ? 1 : 0);
 }
 
 void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
                   cudaGraphConditionalHandle handle, bool set_condition,
-                  int32_t cond_lo, int32_t cond_hi, cudaStream_t s) {
+                  int32_t cond_lo, int32_t cond_hi, cudaStream_t s,
+                  SigIter *its_ahead, bool exclude_fixed) {
   k_finish<<<1, 1024, 0, s>>>(ctl, its, nsig, handle, set_condition ? 1 : 0,
-                              cond_lo, cond_hi);
+                              cond_lo, cond_hi, its_ahead, exclude_fixed ? 1 : 0);
 }
 
 bool ControlKernelsLaunchable() {

@@ -115,13 +115,18 @@ void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,
 
 // Device-side control of a solve: iteration planning and the stop rule
 // (sets the while condition of the solve graph when set_condition).
-// k_plan runs signals needing at most max_bins bins; k_finish continues the
-// loop while a signal with work needs bins in (cond_lo, cond_hi].
+// k_plan runs signals needing at most max_bins bins (ahead: plans the
+// iteration after the running one, for signals at fixed bins); k_finish
+// continues the loop while a signal with work needs bins in
+// (cond_lo, cond_hi] (exclude_fixed: and more than its min_bins), and drops
+// the iteration planned ahead into its_ahead (if not null) of a signal that
+// stopped.
 void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, int32_t max_bins,
-                cudaStream_t s);
+                cudaStream_t s, bool ahead = false);
 void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
                   cudaGraphConditionalHandle handle, bool set_condition,
-                  int32_t cond_lo, int32_t cond_hi, cudaStream_t s);
+                  int32_t cond_lo, int32_t cond_hi, cudaStream_t s,
+                  SigIter *its_ahead = nullptr, bool exclude_fixed = false);
 
 // Batched 2x2 pencils.
 void LaunchPencil(const double2 *u3, int64_t count, double *sigma,

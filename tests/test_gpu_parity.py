@@ -342,6 +342,41 @@ def test_graph_loop_equals_host_loop(ctx, prec):
     assert s1.escalated == s2.escalated and s1.status == s2.status == 0
 
 
+def test_batched_graph_equals_host_loop(ctx):
+    """An uneven FP32 batch through the solve graph (its phases: large bins,
+    small bins, then fixed bins with the next iteration planned and folded
+    ahead) against the host-driven loop: signals that reach fixed bins at
+    different iterations (k from 10 to 400, min_bins 31 to 101), one long
+    enough to refill its draw table; same modes bit for bit, same iteration
+    counts and statistics."""
+    from mpsft_gb300.signals import make_signal
+
+    spec = [(1 << 16, 10, 51, 5), (1 << 17, 400, 51, 5), (65537, 60, 31, 5),
+            (1 << 16, 120, 101, 5), (1 << 18, 30, 51, 40)]
+    sigs, opts = [], []
+    for i, (n, S, mb, stale) in enumerate(spec):
+        sg = make_signal(n, S, 500 + i, sigma=1e-5)
+        sigs.append(ctx.upload(sg.x))
+        opts.append(ctx.solve_options(S, sg.sigma, min_bins=mb, window_delta=1e-5,
+                                      max_stale_iter=stale))
+    out1, st1 = ctx.solve_batched(sigs, [m.Rng(80 + i) for i in range(len(spec))], opts)
+    ctx.set_profiling(True)
+    try:
+        out2, st2 = ctx.solve_batched(sigs, [m.Rng(80 + i) for i in range(len(spec))],
+                                      opts)
+    finally:
+        ctx.set_profiling(False)
+    assert st1[4]["iterations"] > 32
+    for (k1, c1), (k2, c2), a, b in zip(out1, out2, st1, st2):
+        assert a["status"] == b["status"] == 0
+        assert a["iterations"] == b["iterations"]
+        assert a["gathers"] == b["gathers"] and a["escalated"] == b["escalated"]
+        assert np.array_equal(k1, k2)
+        assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64))
+    for sg in sigs:
+        sg.free()
+
+
 def test_table_cache_across_solves(ctx):
     """The solve graph takes its window and Bluestein tables from the
     context's cache (built on first use per number of bins and window delta):
