@@ -281,6 +281,17 @@ __host__ __device__ inline int64_t PhaseTableHi(int64_t n) {
   return ((n - 1) >> PhaseTableK(n)) + 1;
 }
 
+// Programmatic dependent launch (the solve graph's kernels): every iteration
+// kernel starts here. Launched with programmatic stream serialization, it
+// waits until the kernel before it in its stream has completed and its
+// writes are visible, then lets the kernel after it launch (its blocks are
+// scheduled while this one runs, and wait here in turn). Launched without
+// that attribute, both instructions return at once.
+__device__ __forceinline__ void PdlEnter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // v mod n (non-negative) for |v| < 2^63 by Barrett reduction with
 // inv = floor(2^64 / n), or a mask when n is a power of two (inv = 0).
 __host__ __device__ __forceinline__ uint64_t MulHi64(uint64_t a, uint64_t b) {

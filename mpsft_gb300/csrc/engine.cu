@@ -970,6 +970,11 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     int rc = MPSFT_OK;
     cudaError_t ce = cudaSuccess;
     int64_t per_body = 1;
+    // the captured kernels use programmatic dependent launch
+    struct PdlScope {
+      PdlScope() { g_launch_pdl = true; }
+      ~PdlScope() { g_launch_pdl = false; }
+    } pdl_scope;
     cudaGraphNode_t prev = nullptr;
     for (const Phase &ph : phases) {
       if (ph.pipelined) {

@@ -103,6 +103,7 @@ constexpr int kFoldBins = 256 / kFoldSplit;  // bins per CTA
 template <typename TX>
 __global__ void __launch_bounds__(256, 4)
     k_bin_fold32(const SigIter *__restrict__ its, int gmax) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.z];
   if (!it.active || it.force_fp64) return;
   const int B = it.bins;
@@ -203,6 +204,7 @@ __global__ void __launch_bounds__(256, 4)
 template <typename TX>
 __global__ void __launch_bounds__(256)
     k_bin_fold64(const SigIter *__restrict__ its, int gmax, int cond) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.z];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
@@ -277,16 +279,16 @@ void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
   dim3 grid((max_bins + 31) / 32, gmax * max_trials, nsig);
   if (fp64) {
     if (x_c128) {
-      k_bin_fold64<double2><<<grid, 256, 0, s>>>(d_its, gmax, cond ? 1 : 0);
+      Launch(k_bin_fold64<double2>, grid, 256, 0, s, d_its, gmax, cond ? 1 : 0);
     } else {
-      k_bin_fold64<float2><<<grid, 256, 0, s>>>(d_its, gmax, cond ? 1 : 0);
+      Launch(k_bin_fold64<float2>, grid, 256, 0, s, d_its, gmax, cond ? 1 : 0);
     }
   } else {
     dim3 grid32((max_bins + kFoldBins - 1) / kFoldBins, gmax * max_trials, nsig);
     if (x_c128) {
-      k_bin_fold32<double2><<<grid32, 256, 0, s>>>(d_its, gmax);
+      Launch(k_bin_fold32<double2>, grid32, 256, 0, s, d_its, gmax);
     } else {
-      k_bin_fold32<float2><<<grid32, 256, 0, s>>>(d_its, gmax);
+      Launch(k_bin_fold32<float2>, grid32, 256, 0, s, d_its, gmax);
     }
   }
 }

@@ -28,6 +28,8 @@
 
 namespace mpsft {
 
+thread_local bool g_launch_pdl = false;
+
 namespace {
 
 __device__ int32_t NumBitsDev(int32_t n, int32_t bins) {
@@ -53,6 +55,7 @@ __device__ inline int32_t NextBins(const SolveCtl &c, const SigIter &it) {
 // which iteration iter still uses, are cleared by its k_finish instead).
 __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
                        int nsig, int32_t max_bins, int ahead) {
+  PdlEnter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nsig) return;
   SolveCtl &c = ctl[i];
@@ -164,6 +167,7 @@ __global__ void __launch_bounds__(1024)
              cudaGraphConditionalHandle handle, int set_condition,
              int32_t cond_lo, int32_t cond_hi, SigIter *__restrict__ its_ahead,
              int exclude_fixed) {
+  PdlEnter();
   int any = 0;
   for (int i = threadIdx.x; i < nsig; i += blockDim.x) {
     SolveCtl &c = ctl[i];
@@ -234,6 +238,7 @@ __global__ void k_delay(unsigned long long ns) {
 __global__ void __launch_bounds__(256)
     k_copy_mapped(const unsigned char *__restrict__ src, unsigned char *__restrict__ dst,
                   size_t bytes) {
+  PdlEnter();
   const size_t stride = size_t(gridDim.x) * blockDim.x;
   const size_t t0 = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uintptr_t al = reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst);
@@ -257,7 +262,7 @@ void LaunchCopyMapped(const void *src_dev, void *dst, size_t bytes, cudaStream_t
   if (bytes == 0) return;
   const size_t words = bytes / 16 + 1;
   const unsigned blocks = unsigned(std::min<size_t>(152, (words + 255) / 256));
-  k_copy_mapped<<<blocks, 256, 0, s>>>(static_cast<const unsigned char *>(src_dev),
+  Launch(k_copy_mapped, blocks, 256, 0, s, static_cast<const unsigned char *>(src_dev),
                                        static_cast<unsigned char *>(dst), bytes);
 }
 
@@ -267,14 +272,14 @@ void LaunchDelay(unsigned long long ns, cudaStream_t s) {
 
 void LaunchPlan(SolveCtl *ctl, SigIter *its, int nsig, int32_t max_bins,
                 cudaStream_t s, bool ahead) {
-  k_plan<<<(nsig + 127) / 128, 128, 0, s>>>(ctl, its, nsig, max_bins, ahead ? 1 : 0);
+  Launch(k_plan, (nsig + 127) / 128, 128, 0, s, ctl, its, nsig, max_bins, ahead ? 1 : 0);
 }
 
 void LaunchFinish(SolveCtl *ctl, SigIter *its, int nsig,
                   cudaGraphConditionalHandle handle, bool set_condition,
                   int32_t cond_lo, int32_t cond_hi, cudaStream_t s,
                   SigIter *its_ahead, bool exclude_fixed) {
-  k_finish<<<1, 1024, 0, s>>>(ctl, its, nsig, handle, set_condition ? 1 : 0,
+  Launch(k_finish, 1, 1024, 0, s, ctl, its, nsig, handle, set_condition ? 1 : 0,
                               cond_lo, cond_hi, its_ahead, exclude_fixed ? 1 : 0);
 }
 

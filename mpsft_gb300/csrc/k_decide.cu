@@ -48,6 +48,7 @@ __device__ inline float WindowInFreq32(const SigIter &it, int64_t k1, int bin) {
 }
 
 __global__ void k_mode_prep(const SigIter *__restrict__ its, int cond) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   if (cond && !RedoFP64(it)) return;
@@ -106,6 +107,7 @@ __device__ void BitonicSort(unsigned long long *keys, int m) {
 // an order that does not depend on the table layout. Thread 0 also evaluates
 // this iteration's FP32 error scale eps.
 __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its) {
+  PdlEnter();
   extern __shared__ unsigned long long keys[];  // pow2 >= occupied slots
   const SigIter &it = its[blockIdx.x];
   if (!it.active) return;
@@ -155,6 +157,7 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
 template <typename T, int TMAX>
 __global__ void __launch_bounds__(256)
     k_decide(const SigIter *__restrict__ its, int mode, int cond, int mark) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
@@ -192,6 +195,7 @@ __device__ void MergeBin(const SigIter &it, int beta);
 template <int TMAX, int W, int G>
 __global__ void __launch_bounds__(32 * W)
     k_decide_listed(const SigIter *__restrict__ its, int redo, int merge) {
+  PdlEnter();
   __shared__ double2 s_p0[W][TMAX];
   __shared__ double2 s_pp[W][32][TMAX];
   __shared__ double2 s_pm[W][32][TMAX];
@@ -335,6 +339,7 @@ __global__ void __launch_bounds__(32 * W)
 // signal's listed bins, a thread per mode. Runs on the side stream while the
 // listed bins are re-binned.
 __global__ void __launch_bounds__(128) k_listed_terms(const SigIter *__restrict__ its) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.force_fp64 || it.esc_mask == nullptr) return;
   const int nf = *(volatile int32_t *)&it.flags[2];
@@ -412,6 +417,7 @@ __device__ void MergeBin(const SigIter &it, int beta) {
 // Candidates -> table, one thread per bin; bins held back for their FP64
 // near-tie decision (cand_valid >= kCandListed) are merged by that decision.
 __global__ void k_merge(const SigIter *__restrict__ its) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   const int beta = blockIdx.x * blockDim.x + threadIdx.x;
@@ -499,7 +505,7 @@ template <typename T, int TMAX>
 void LaunchDecideT(const SigIter *d_its, int nsig, int max_bins, int mode,
                    int cond, int mark, cudaStream_t s) {
   dim3 grid((max_bins + 7) / 8, nsig);
-  k_decide<T, TMAX><<<grid, 256, 0, s>>>(d_its, mode, cond, mark);
+  Launch(k_decide<T, TMAX>, grid, 256, 0, s, d_its, mode, cond, mark);
 }
 
 template <typename T>
@@ -537,7 +543,7 @@ void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,
   // the occupied count is only known on the device: cover the whole table,
   // blocks past the count exit at once
   dim3 grid((max_cap + 255) / 256, nsig);
-  k_mode_prep<<<grid, 256, 0, s>>>(d_its, cond ? 1 : 0);
+  Launch(k_mode_prep, grid, 256, 0, s, d_its, cond ? 1 : 0);
 }
 
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
@@ -546,7 +552,7 @@ void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
   const size_t sm = size_t(BucketKeys(max_cap)) * sizeof(unsigned long long);
   cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        int(sm));
-  k_bucket<<<nsig, 1024, sm, s>>>(d_its);
+  Launch(k_bucket, nsig, 1024, sm, s, d_its);
 }
 
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
@@ -567,23 +573,23 @@ void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
   dim3 grid(kListedBlocks, nsig);
   const int r = redo ? 1 : 0, mg = merge ? 1 : 0;
   if (max_trials <= 1) {
-    k_decide_listed<1, 8, 4><<<grid, 32 * 8, 0, s>>>(d_its, r, mg);
+    Launch(k_decide_listed<1, 8, 4>, grid, 32 * 8, 0, s, d_its, r, mg);
   } else if (max_trials <= 5) {
-    k_decide_listed<5, 4, 2><<<grid, 32 * 4, 0, s>>>(d_its, r, mg);
+    Launch(k_decide_listed<5, 4, 2>, grid, 32 * 4, 0, s, d_its, r, mg);
   } else {
-    k_decide_listed<kMaxTrials, 2, 1><<<grid, 32 * 2, 0, s>>>(d_its, r, mg);
+    Launch(k_decide_listed<kMaxTrials, 2, 1>, grid, 32 * 2, 0, s, d_its, r, mg);
   }
 }
 
 void LaunchListedTerms(const SigIter *d_its, int nsig, cudaStream_t s) {
   dim3 grid(kListedBlocks, nsig);
-  k_listed_terms<<<grid, 128, 0, s>>>(d_its);
+  Launch(k_listed_terms, grid, 128, 0, s, d_its);
 }
 
 void LaunchMerge(const SigIter *d_its, int nsig, int max_bins,
                  cudaStream_t s) {
   dim3 grid((max_bins + 255) / 256, nsig);
-  k_merge<<<grid, 256, 0, s>>>(d_its);
+  Launch(k_merge, grid, 256, 0, s, d_its);
 }
 
 void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,

@@ -62,6 +62,7 @@ template <typename V>
 __global__ void __launch_bounds__(kRowFftThreads)
     k_row_fft(const SigIter *__restrict__ its, int max_trials,
               const V *__restrict__ tw, int cond, int rpb_cap) {
+  PdlEnter();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned row_max_bits[kRowsMax];
   const SigIter &it = its[blockIdx.z];
@@ -216,13 +217,13 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
     const size_t sm = RowFftSlots(max_m) * sizeof(double2);
     cudaFuncSetAttribute(k_row_fft<double2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_row_fft<double2><<<grid, kRowFftThreads, sm, s>>>(d_its, max_trials, tw64,
+    Launch(k_row_fft<double2>, grid, kRowFftThreads, sm, s, d_its, max_trials, tw64,
                                                         cond ? 1 : 0, rpb_cap);
   } else {
     const size_t sm = RowFftSlots(max_m) * sizeof(float2);
     cudaFuncSetAttribute(k_row_fft<float2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_row_fft<float2><<<grid, kRowFftThreads, sm, s>>>(d_its, max_trials, tw32,
+    Launch(k_row_fft<float2>, grid, kRowFftThreads, sm, s, d_its, max_trials, tw32,
                                                        cond ? 1 : 0, rpb_cap);
   }
 }

@@ -86,6 +86,7 @@ __device__ __forceinline__ void SampleTimesWindow(double2 v, float2 w, FF *re,
 // FP64_DIRECT): one warp per listed bin. A solve's FP32 decide kernel
 // prepares its listed bins itself when it lists them.
 __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ its) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.force_fp64) return;
   const int nf = *(volatile int32_t *)&it.flags[2];
@@ -98,6 +99,7 @@ __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ 
 template <typename TX>
 __global__ void __launch_bounds__(256, 2)
     k_rebin_ff(const SigIter *__restrict__ its, int nsig) {
+  PdlEnter();
   __shared__ int64_t items_end[kRebinMaxSignals];
   __shared__ float4 pw_s[8][kPowLen];
   for (int s = threadIdx.x; s < nsig; s += blockDim.x) {
@@ -243,15 +245,15 @@ void LaunchRebin(const SigIter *d_its, int nsig, int max_listed, bool x_c128,
   // work items; batches are cut into groups of at most kRebinMaxSignals
   if (prepare) {
     dim3 pgrid((max_listed + 7) / 8, nsig);
-    k_rebin_prep<<<pgrid, 256, 0, s>>>(d_its);
+    Launch(k_rebin_prep, pgrid, 256, 0, s, d_its);
   }
   const int blocks = 152 * 2;  // two resident blocks per SM (124 registers)
   for (int s0 = 0; s0 < nsig; s0 += kRebinMaxSignals) {
     const int cnt = nsig - s0 < kRebinMaxSignals ? nsig - s0 : kRebinMaxSignals;
     if (x_c128) {
-      k_rebin_ff<double2><<<blocks, 256, 0, s>>>(d_its + s0, cnt);
+      Launch(k_rebin_ff<double2>, blocks, 256, 0, s, d_its + s0, cnt);
     } else {
-      k_rebin_ff<float2><<<blocks, 256, 0, s>>>(d_its + s0, cnt);
+      Launch(k_rebin_ff<float2>, blocks, 256, 0, s, d_its + s0, cnt);
     }
   }
 }

@@ -45,6 +45,7 @@ __device__ double SincPi(double x) {
 // FP64 window (the reference's evaluation order) into wt64 and, when
 // present, the float-float copy wtff; with_fp32 also rounds it into wt32.
 __global__ void k_window64(const SigIter *__restrict__ its, int with_fp32) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.tables_valid) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -70,6 +71,7 @@ __global__ void k_window64(const SigIter *__restrict__ its, int with_fp32) {
 // The same window evaluated in FP32 for the FP32 binning (a few ulp; the
 // FP64 tables are built beside it, off the binning's critical path).
 __global__ void k_window32(const SigIter *__restrict__ its) {
+  PdlEnter();
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.tables_valid || it.force_fp64) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -113,6 +115,7 @@ template <typename V>
 __global__ void __launch_bounds__(512)
     k_bluestein_setup(const SigIter *__restrict__ its, const V *__restrict__ tw,
                       int cond) {
+  PdlEnter();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *a = reinterpret_cast<V *>(smem_raw);
   const SigIter &it = its[blockIdx.x];
@@ -164,17 +167,17 @@ void LaunchPhaseTables(const SigIter *d_its, int nsig, int64_t entries,
 
 void LaunchWindow(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
   dim3 grid((max_p2 + 1 + 255) / 256, nsig);
-  k_window64<<<grid, 256, 0, s>>>(d_its, 1);
+  Launch(k_window64, grid, 256, 0, s, d_its, 1);
 }
 
 void LaunchWindow64(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
   dim3 grid((max_p2 + 1 + 255) / 256, nsig);
-  k_window64<<<grid, 256, 0, s>>>(d_its, 0);
+  Launch(k_window64, grid, 256, 0, s, d_its, 0);
 }
 
 void LaunchWindow32(const SigIter *d_its, int nsig, int max_p2, cudaStream_t s) {
   dim3 grid((max_p2 + 1 + 255) / 256, nsig);
-  k_window32<<<grid, 256, 0, s>>>(d_its);
+  Launch(k_window32, grid, 256, 0, s, d_its);
 }
 
 void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
@@ -184,12 +187,12 @@ void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
     const size_t sm = size_t(PadLen(max_m)) * sizeof(double2);
     cudaFuncSetAttribute(k_bluestein_setup<double2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_bluestein_setup<double2><<<nsig, 512, sm, s>>>(d_its, tw64, cond ? 1 : 0);
+    Launch(k_bluestein_setup<double2>, nsig, 512, sm, s, d_its, tw64, cond ? 1 : 0);
   } else {
     const size_t sm = size_t(PadLen(max_m)) * sizeof(float2);
     cudaFuncSetAttribute(k_bluestein_setup<float2>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_bluestein_setup<float2><<<nsig, 512, sm, s>>>(d_its, tw32, cond ? 1 : 0);
+    Launch(k_bluestein_setup<float2>, nsig, 512, sm, s, d_its, tw32, cond ? 1 : 0);
   }
 }
 

@@ -7,6 +7,32 @@
 
 namespace mpsft {
 
+// True while the calling thread captures a solve graph: the iteration
+// kernels are then launched with programmatic stream serialization (each
+// starts with PdlEnter), so that a kernel's launch overlaps the end of the
+// kernel before it.
+extern thread_local bool g_launch_pdl;
+
+template <typename... P, typename... A>
+inline void Launch(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
+                   cudaStream_t s, A... args) {
+  if (!g_launch_pdl) {
+    kernel<<<grid, block, smem, s>>>(args...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
+}
+
 // e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2, for the FFT twiddles.
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s);
 // dst (device) = src_dev (device address of pinned, mapped host memory), any
