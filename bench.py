@@ -270,6 +270,27 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- multi-rank helpers
+def rank_seeds(rank: int, batch: int) -> list[int]:
+    """Signal seeds of one rank: every rank recovers its own batch (replicas)."""
+    return [10_000 + rank * batch + i for i in range(batch)]
+
+
+def max_over_ranks(ms: float, dist, device) -> float:
+    """The slowest rank's time (the job's time); ms itself on one rank."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, batch: int, steps: int, ms: float) -> float:
+    """Recoveries per second of the whole job: every rank's signals over the
+    slowest rank's time."""
+    return world * batch * steps / (ms / 1e3)
+
+
 # ----------------------------------------------------------------- GPU arm
 def dense_fft(torch, sigs_host, device, reps: int = 5) -> dict:
     """Dense full-N FFTs of the same signals, the comparators of a sparse
@@ -470,7 +491,7 @@ def run_gpu(args) -> None:
         raise SystemExit("library not built: run __graft_entry__.build() first")
 
     G = args.batch
-    sigs_host = [config2(10_000 + rank * G + i) for i in range(G)]
+    sigs_host = [config2(s) for s in rank_seeds(rank, G)]
     ctx = m.Context(local)
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
@@ -525,12 +546,8 @@ def run_gpu(args) -> None:
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    t_rank = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t_rank, op=dist.ReduceOp.MAX)
-    ms_max = float(t_rank.item())
-    value = world * G * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
+    value = job_rate(world, G, args.steps, ms_max)
 
     # ---- the same steps again with an event pair around every binning
     # launch (the host drives the iterations here); gives the binning roofline
@@ -587,11 +604,8 @@ def run_gpu(args) -> None:
     e1.record(stream)
     writer.shutdown()
     torch.cuda.synchronize()
-    e_ms = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(e_ms, op=dist.ReduceOp.MAX)
-    e2e_ms = float(e_ms.item())
-    e2e_value = world * G * args.steps / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
+    e2e_value = job_rate(world, G, args.steps, e2e_ms)
     # the link alone: one set's copies with nothing else running
     link_ms = []
     for _ in range(3):
