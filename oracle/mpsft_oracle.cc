@@ -591,6 +591,53 @@ int orc_generate_mode_map(int32_t n, int32_t k, int32_t *out_k, double *out_c) {
   return WriteSorted(mm, out_k, out_c, k);
 }
 
+int orc_demo_signal(int32_t n, int32_t k, double sigma, int xhat_kind,
+                    double *x, int32_t *out_k, double *out_c) {
+  // GenerateModeMap, then GenerateXhat / GenerateXhatAlt (src/gen.cc:27-89),
+  // then FFTPlan(n, FFTW_BACKWARD) (src/demo1.cc:27-34). Each complex normal
+  // is Cplex(RandomNormal(), RandomNormal()), imaginary part first (g++
+  // evaluates the two arguments right to left); the noise energy subtracts
+  // the mode positions in the map's own iteration order.
+  ModeMap mm;
+  while (int32_t(mm.size()) < k) {
+    const int32_t idx = DrawInt32() % n;
+    if (mm.count(idx)) continue;
+    const double im = DrawNormal();
+    const double re = DrawNormal();
+    Cplex coef(re, im);
+    coef /= std::abs(coef);
+    mm[idx] = coef;
+  }
+  std::vector<Cplex> xh(n, Cplex(0.0, 0.0));
+  if (xhat_kind == 0) {
+    double noise_energy = 0;
+    for (int32_t i = 0; i < n; ++i) {
+      const double im = DrawNormal();
+      const double re = DrawNormal();
+      xh[i] = Cplex(re, im);
+      noise_energy += re * re + im * im;
+    }
+    for (const auto &kv : mm) {
+      const Cplex v = xh[kv.first];
+      noise_energy -= v.real() * v.real() + v.imag() * v.imag();
+    }
+    const double factor = sigma / std::sqrt(noise_energy);
+    for (int32_t i = 0; i < n; ++i) xh[i] *= factor;
+    for (const auto &kv : mm) xh[kv.first] = kv.second;
+  } else {
+    for (const auto &kv : mm) xh[kv.first] = kv.second;
+    const double scale = sigma / std::sqrt(2 * n);
+    for (int32_t i = 0; i < n; ++i) {
+      const double im = DrawNormal();
+      const double re = DrawNormal();
+      xh[i] += Cplex(re, im) * scale;
+    }
+  }
+  fft64::Plan plan(n, +1);
+  plan.Run(xh.data(), reinterpret_cast<Cplex *>(x));
+  return WriteSorted(mm, out_k, out_c, k);
+}
+
 void orc_post_analyze(int32_t n, const double *xh, const int32_t *true_k,
                       int32_t true_count, const int32_t *found_k,
                       const double *found_c, int32_t found_count, double *out) {

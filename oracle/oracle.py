@@ -86,6 +86,7 @@ class Oracle:
                                      _dbl, _i32, _i32, _p, _p, _i32, _p]),
             "orc_generate_mode_map": (_int, [_i32, _i32, _p, _p]),
             "orc_post_analyze": (None, [_i32, _p, _p, _i32, _p, _p, _i32, _p]),
+            "orc_demo_signal": (_int, [_i32, _i32, _dbl, _int, _p, _p, _p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -195,6 +196,18 @@ class Oracle:
         oc = np.zeros(k, np.complex128)
         m = self.lib.orc_generate_mode_map(n, k, _ptr(ok), _ptr(oc))
         return ok[:m].copy(), oc[:m].copy()
+
+    def demo_signal(self, n: int, k: int, sigma: float, seed: int, alt: bool = False):
+        """RandomSeed(seed), then Demo1's signal construction (GenerateModeMap,
+        GenerateXhat or GenerateXhatAlt, backward FFT): (x, positions sorted,
+        coefficients). The RNG is left where the construction leaves it."""
+        self.seed(seed)
+        x = np.zeros(n, np.complex128)
+        ok = np.zeros(k, np.int32)
+        oc = np.zeros(k, np.complex128)
+        m = self.lib.orc_demo_signal(n, k, sigma, 1 if alt else 0, _ptr(x), _ptr(ok),
+                                     _ptr(oc))
+        return x, ok[:m].copy(), oc[:m].copy()
 
     def post_analyze(self, xh: np.ndarray, true_k, found_k, found_c) -> dict:
         """Demo1::PostAnalyze on spectrum xh: hit/miss counts and errors."""

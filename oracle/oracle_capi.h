@@ -85,6 +85,16 @@ int orc_demo1_run(int32_t n, const double *x, int32_t k, double sigma,
  * normalised to modulus 1. Writes them sorted by position; returns k. */
 int orc_generate_mode_map(int32_t n, int32_t k, int32_t *out_k, double *out_c);
 
+/* Demo1's signal (src/demo1.cc:27-34) on the global RNG as it stands (seed it
+ * first): GenerateModeMap (k modes), then GenerateXhat (xhat_kind 0,
+ * src/gen.cc:55-75: unit normals rescaled so that the noise outside the
+ * modes has energy sigma^2) or GenerateXhatAlt (xhat_kind 1, src/gen.cc:77-89),
+ * then the unnormalised backward FFT. Writes x (n values) and the modes
+ * sorted by position; returns k. Later draws continue the same stream, as
+ * the reference's tests' Iterate calls do. */
+int orc_demo_signal(int32_t n, int32_t k, double sigma, int xhat_kind,
+                    double *x, int32_t *out_k, double *out_c);
+
 /* Demo1::PostAnalyze (src/demo1.cc:61-112) for the spectrum xh (n values),
  * the true positions true_k and the found modes (found_k, found_c). out
  * receives {hit, hit_l1, hit_l2, miss, miss_l1, miss_l2, l1, l2, max_err}. */

@@ -214,6 +214,23 @@ int orc_generate_mode_map(int32_t n, int32_t k, int32_t *out_k, double *out_c) {
   return WriteSorted(mm, out_k, out_c, k);
 }
 
+int orc_demo_signal(int32_t n, int32_t k, double sigma, int xhat_kind,
+                    double *x, int32_t *out_k, double *out_c) {
+  ModeMap mm;
+  GenerateModeMap(n, k, &mm);
+  CplexArray xh(n);
+  if (xhat_kind == 0) {
+    GenerateXhat(n, mm, sigma, &xh);
+  } else {
+    GenerateXhatAlt(n, mm, sigma, &xh);
+  }
+  CplexArray xt(n);
+  FFTPlan plan(n, FFTW_BACKWARD);
+  plan.Run(xh, &xt);
+  std::memcpy(x, reinterpret_cast<const void *>(xt.data()), sizeof(double) * 2 * n);
+  return WriteSorted(mm, out_k, out_c, k);
+}
+
 void orc_post_analyze(int32_t n, const double *xh, const int32_t *true_k,
                       int32_t true_count, const int32_t *found_k,
                       const double *found_c, int32_t found_count, double *out) {

@@ -97,3 +97,35 @@ def post_analyze_inputs(case):
                            + 1j * rng.standard_normal(fk.size))
     return xh, tk.astype(np.int32), fk.astype(np.int32), fc
 
+
+# The reference's statistical Iterate tests (src/iterate_test.cc:84-175): n =
+# kPrimes[20], 1000 unit modes, GenerateXhat noise, RandomSeed(123537) before
+# the signal is built, trials = 3, window_delta = 1e-6, window_threshold = 0.1.
+# IterateMore: sigma = 1e-2, bin_threshold = 0.01, bins 2001 then 1401.
+# IterateFull: sigma = 1e-7, thresholds 3 sigma / sqrt(bins) and
+# sigma / sqrt(bins), bins 2001 four times. Each step's REQUIREs: at least
+# `good` true modes found, at most `bad` others.
+ITERATE_STATS_N = 1048573
+ITERATE_MORE = dict(sigma=1e-2, bins=[2001, 1401], good=[300, 600], bad=[100, 100])
+ITERATE_FULL = dict(sigma=1e-7, bins=[2001] * 4, good=[250, 450, 600, 700], bad=[30] * 4)
+
+
+def iterate_stats(oracle, spec):
+    """Runs one of the reference's statistical scenarios on an oracle:
+    [(good, bad)] after each Iterate call, and the final mode map."""
+    x, k, _ = oracle.demo_signal(ITERATE_STATS_N, 1000, spec["sigma"], 123537)
+    truth = set(k.tolist())
+    sigma = spec["sigma"]
+    mm, out = {}, []
+    for bins in spec["bins"]:
+        if spec is ITERATE_FULL:
+            kw = dict(bin_threshold=3 * sigma / np.sqrt(bins),
+                      sv_threshold=sigma / np.sqrt(bins))
+        else:
+            kw = dict(bin_threshold=0.01)
+        _, mm = oracle.iterate(x, bins, window_delta=1e-6, trials=3,
+                               window_threshold=0.1, mm=mm, **kw)
+        good = sum(1 for kk in mm if kk in truth)
+        out.append((good, len(mm) - good))
+    return out, mm
+

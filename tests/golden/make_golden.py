@@ -134,6 +134,12 @@ def main() -> None:
         r = ref.post_analyze(xh, tk, fk, fc)
         out[f"pa_{case[0]}"] = np.array([r[k] for k in PA_KEYS], np.float64)
 
+    # The reference's statistical Iterate scenarios: (good, bad) per call.
+    # (n = kPrimes[20] is prime: the reference's own Transform)
+    for name, spec in (("more", cases.ITERATE_MORE), ("full", cases.ITERATE_FULL)):
+        counts, _ = cases.iterate_stats(ref, spec)
+        out[f"iterstats_{name}"] = np.array(counts, np.int32)
+
     path = os.path.join(HERE, "ref_golden.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path}: {len(out)} arrays, {os.path.getsize(path)} bytes")

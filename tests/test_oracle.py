@@ -245,3 +245,34 @@ def test_post_analyze_matches_reference(port, golden, case):
             assert np.isnan(got[key]), key
         else:
             assert abs(got[key] - want[j]) <= 1e-12 * abs(want[j]), key
+
+
+# ------------------------------- the reference's statistical Iterate tests
+@pytest.mark.parametrize("name", ["more", "full"])
+def test_iterate_statistics_match_reference(port, golden, name):
+    """IterateMore / IterateFull (src/iterate_test.cc:84-175): Demo1's signal
+    construction (GenerateModeMap, GenerateXhat, backward FFT) from
+    RandomSeed(123537), then Iterate calls continuing the same draw stream.
+    The port finds exactly the reference's counts after every call, and they
+    meet the reference test's own bounds."""
+    spec = cases.ITERATE_MORE if name == "more" else cases.ITERATE_FULL
+    counts, mm = cases.iterate_stats(port, spec)
+    assert np.array_equal(np.array(counts, np.int32), golden[f"iterstats_{name}"])
+    for (good, bad), lo, hi in zip(counts, spec["good"], spec["bad"]):
+        assert good >= lo and bad <= hi
+    if orc.available("ref"):
+        _, ref_mm = cases.iterate_stats(orc.Oracle("ref"), spec)
+        assert sorted(mm) == sorted(ref_mm)
+
+
+def test_demo_signal_matches_reference_here():
+    """Demo1's signal construction in the port equals the reference's bit for
+    bit (both noise forms), where the reference is built on this host."""
+    if not orc.available("ref"):
+        pytest.skip("oracle/_ref is built only where the reference tree is")
+    ref, port = orc.Oracle("ref"), orc.Oracle("port")
+    for alt in (False, True):
+        a = ref.demo_signal(65537, 50, 1e-3, 11, alt)
+        b = port.demo_signal(65537, 50, 1e-3, 11, alt)
+        for u, v in zip(a, b):
+            assert np.array_equal(u, v)
