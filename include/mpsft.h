@@ -77,6 +77,10 @@ int mpsft_rng_create(int32_t seed, mpsft_rng **out);
 int mpsft_rng_destroy(mpsft_rng *rng);
 int mpsft_rng_seed(mpsft_rng *rng, int32_t seed);
 int32_t mpsft_rng_int32(mpsft_rng *rng);
+/* count draws of std::normal_distribution<double> on the same engine (the
+ * reference's RandomNormal, src/base.cc:55), into out or discarded (out =
+ * NULL): positions the stream after the reference's signal construction. */
+int mpsft_rng_normals(mpsft_rng *rng, int64_t count, double *out);
 
 /* ---- small host helpers -------------------------------------------------- */
 /* NumBits: 1 + floor(log2(n / bins)) counted by halving (1 if n < bins). */

@@ -119,6 +119,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_rng_destroy": (I, [P]),
         "mpsft_rng_seed": (I, [P, I32]),
         "mpsft_rng_int32": (I32, [P]),
+        "mpsft_rng_normals": (I, [P, I64, P]),
         "mpsft_num_bits": (I32, [I32, I32]),
         "mpsft_window_support": (I32, [I32, I32, D]),
         "mpsft_window_table": (I, [P, I32, I32, D, P, I32]),
@@ -189,6 +190,13 @@ class Rng:
 
     def int32(self) -> int:
         return int(self._lib.mpsft_rng_int32(self._h))
+
+    def normals(self, count: int, keep: bool = True):
+        """count RandomNormal draws (returned, or only consumed)."""
+        out = np.empty(count if keep else 0, np.float64)
+        _check(None, self._lib.mpsft_rng_normals(self._h, int(count),
+                                                 _ptr(out) if keep else None))
+        return out if keep else None
 
     def mode_map(self, n: int, count: int):
         """GenerateModeMap (src/gen.cc:27-39) from this RNG: (positions in

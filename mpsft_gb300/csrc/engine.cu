@@ -1674,6 +1674,15 @@ int mpsft_rng_seed(mpsft_rng *rng, int32_t seed) {
 }
 int32_t mpsft_rng_int32(mpsft_rng *rng) { return rng ? rng->Draw() : -1; }
 
+int mpsft_rng_normals(mpsft_rng *rng, int64_t count, double *out) {
+  if (!rng || count < 0) return MPSFT_ERR_INVALID;
+  for (int64_t i = 0; i < count; ++i) {
+    const double v = rng->Normal();
+    if (out) out[i] = v;
+  }
+  return MPSFT_OK;
+}
+
 int32_t mpsft_num_bits(int32_t n, int32_t bins) {
   return bins > 0 ? NumBits(n, bins) : 0;
 }

@@ -451,3 +451,43 @@ def test_errors_are_statuses(ctx):
     modes, _ = ctx.solve(sig, m.Rng(1), ctx.solve_options(30, 1e-6, min_bins=51,
                                                          max_stale_iter=5))
     assert len(modes) >= 30
+
+
+@pytest.mark.parametrize("prec", PRECS, ids=PREC_IDS)
+@pytest.mark.parametrize("name", ["more", "full"])
+def test_iterate_statistics_match_reference(ctx, port, golden, name, prec):
+    """The reference's statistical Iterate tests (src/iterate_test.cc:84-175)
+    through mpsft_iterate: the signal is Demo1's construction from
+    RandomSeed(123537) (built by the oracle; the library's RNG is advanced by
+    the same draws, GenerateModeMap then 2n normals), then Iterate calls that
+    continue the stream. Every call finds the reference's counts and the
+    oracle's exact mode set. Coefficients: relative error (norm over the set)
+    within 1e-6 (FP64) / 1e-2 (FP32); the largest per-mode deviations, 2.4e-7
+    and 4.5e-3, are on modes the noisy scenario re-finds, whose sums are far
+    below the unit modes."""
+    spec = cases.ITERATE_MORE if name == "more" else cases.ITERATE_FULL
+    counts, mm_o = cases.iterate_stats(port, spec)
+    n = cases.ITERATE_STATS_N
+    x, k, _ = port.demo_signal(n, 1000, spec["sigma"], 123537)
+    truth = set(k.tolist())
+    sig = ctx.upload(x)
+    rng = m.Rng(123537)
+    rng.mode_map(n, 1000)
+    rng.normals(2 * n, keep=False)
+    sigma = spec["sigma"]
+    mm, got = {}, []
+    for bins in spec["bins"]:
+        if spec is cases.ITERATE_FULL:
+            kw = dict(bin_threshold=3 * sigma / np.sqrt(bins),
+                      sv_threshold=sigma / np.sqrt(bins))
+        else:
+            kw = dict(bin_threshold=0.01)
+        _, mm = ctx.iterate(sig, rng, bins, window_delta=1e-6, trials=3,
+                            window_threshold=0.1, mm=mm, precision=prec, **kw)
+        good = sum(1 for kk in mm if kk in truth)
+        got.append((good, len(mm) - good))
+    sig.free()
+    assert np.array_equal(np.array(got, np.int32), golden[f"iterstats_{name}"])
+    assert sorted(mm) == sorted(mm_o)
+    kk = sorted(mm_o)
+    assert coef_err(mm, kk, [mm_o[q] for q in kk]) < (1e-6 if prec == m.FP64 else 1e-2)
