@@ -21,11 +21,21 @@ oracle's FP64 restatement (oracle/liboracle.so, or liboracle_fast.so with the
 reference's -O3 -ffast-math flags when that build is faster here), one
 process per core, each recovering its own signal of the same configuration.
 
-Also reported (rank 0): the plain per-signal FP64 GPU path, the accuracy of
-one recovery against an FP64 dense FFT (hits, misses, algorithm and precision
-errors), dense full-N FFT rates (scipy on the host cores, cuFFT on the
-device), and the device test-data pipeline (generation, PostAnalyze) against
-its host form.
+Also reported (rank 0): the plain per-signal FP64 GPU path and the same
+64-signal batch on the FP64 kernels (batching and precision gains apart), the
+accuracy of one recovery against an FP64 dense FFT (hits, misses, algorithm
+and precision errors), dense full-N FFT rates (scipy on the host cores, cuFFT
+on the device), the device test-data pipeline (generation, PostAnalyze)
+against its host form, the 256-signal uneven batch (config 3), the N = 2^26
+stress signal alone and four at a time (config 5), and the reference's own
+binning micro-benchmark shape (N = 4194301, B = 501, bits = 15).
+
+``roofline`` is the binning kernel's: algorithmic bytes over event-timed
+launch durations of a profiled pass (every binning launch timed alone), for
+all launches and per phase (``first``: the first iteration, B = 2001;
+``fixed_bins``: the late iterations at B = min_bins = 51), with each phase's
+DRAM bytes per gathered sample as ncu measured them on this workload
+(profiles/bin_fold_phases_config2_batch64.md).
 
 Multi-GPU: one process per GPU under torchrun; every rank recovers its own G
 signals (independent replicas, no collective on the data path); the time is the
@@ -71,6 +81,9 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="bounded CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the extra workloads (batched FP64, configs 3 and 5, "
+                        "the reference's binning micro-benchmark shape)")
     p.add_argument("--profile-case", action="store_true",
                    help="one batched solve with the host-driven loop and "
                         "nothing else (the case the ncu summaries capture)")
@@ -401,19 +414,237 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profile_traffic() -> float | None:
-    """DRAM bytes per gathered sample of the binning kernel, from the ncu
-    summary committed under profiles/ (None when absent)."""
-    p = os.path.join(ROOT, "profiles", "bin_fold_config2.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("dram_bytes_per_gather:"):
+PHASE_PROFILE = os.path.join(ROOT, "profiles", "bin_fold_phases_config2_batch64.md")
+
+
+def profile_traffic() -> dict:
+    """Measured DRAM traffic of the binning launches per phase, from the ncu
+    summary committed under profiles/: {phase: {"dram_bytes_per_launch",
+    "gathers_per_launch", "dram_bytes_per_gather"}} ({} when absent). Lines
+    read: ``traffic <phase>: key=value ...``."""
+    out = {}
+    if not os.path.exists(PHASE_PROFILE):
+        return out
+    for line in open(PHASE_PROFILE):
+        if not line.startswith("traffic "):
+            continue
+        head, _, rest = line.partition(":")
+        phase = head.split()[1]
+        vals = {}
+        for tok in rest.split():
+            k, _, v = tok.partition("=")
             try:
-                return float(line.split(":", 1)[1].split()[0])
+                vals[k] = float(v)
             except ValueError:
-                return None
-    return None
+                pass
+        out[phase] = vals
+    return out
+
+
+def phase_of(rec: dict, min_bins: int) -> list[str]:
+    """Phases a binning launch belongs to: "first" (the first iteration, the
+    largest bins), "fixed_bins" (every signal at min_bins: the late
+    iterations), and "all"."""
+    ph = ["all"]
+    if rec["iteration"] == 0:
+        ph.append("first")
+    if rec["max_bins"] == min_bins:
+        ph.append("fixed_bins")
+    return ph
+
+
+def binning_roofline(records: list[dict], min_bins: int, peak: float,
+                     traffic: dict) -> dict:
+    """Achieved GB/s (algorithmic bytes / event-timed duration) per phase over
+    the profiled launches, with the measured DRAM bytes of that phase's
+    launches (ncu) where the summary has them."""
+    acc = {}
+    for r in records:
+        for ph in phase_of(r, min_bins):
+            a = acc.setdefault(ph, {"launches": 0, "bytes": 0, "gathers": 0, "ms": 0.0})
+            a["launches"] += 1
+            a["bytes"] += r["bytes"]
+            a["gathers"] += r["gathers"]
+            a["ms"] += r["ms"]
+    out = {}
+    for ph, a in acc.items():
+        if a["ms"] <= 0:
+            continue
+        achieved = a["bytes"] / (a["ms"] / 1e3) / 1e9
+        d = {"achieved": achieved, "frac": achieved / peak,
+             "launches": a["launches"], "kernel_ms": a["ms"],
+             "bytes_per_launch": a["bytes"] / a["launches"],
+             "gathers_per_launch": a["gathers"] / a["launches"],
+             "traffic": None}
+        t = traffic.get(ph)
+        if t and "dram_bytes_per_gather" in t:
+            # the measured launches are this workload's own (same signals and
+            # draws); per gathered sample so that a different step count or
+            # phase mix reads the same figure
+            d["dram_bytes_per_gather"] = t["dram_bytes_per_gather"]
+            d["traffic"] = t["dram_bytes_per_gather"] * d["gathers_per_launch"]
+            d["algorithmic_bytes_per_gather"] = a["bytes"] / a["gathers"]
+        out[ph] = d
+    return out
+
+
+def _event_ms(torch, stream, fn, steps: int, warmup: int) -> float:
+    """Mean ms per call of fn over steps calls after warmup calls, from CUDA
+    events on stream (the context's stream), synchronised on both sides."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _profiled_roofline(ctx, fn, peak: float, min_bins: int = 51) -> dict:
+    """One call of fn with every binning launch timed: all-launch and
+    per-phase achieved GB/s (no measured traffic)."""
+    ctx.set_profiling(True)
+    try:
+        fn()
+        recs = ctx.bin_launches()
+    finally:
+        ctx.set_profiling(False)
+    ph = binning_roofline(recs, min_bins, peak, {})
+    return {k: {kk: v[kk] for kk in ("achieved", "frac", "launches", "kernel_ms")}
+            for k, v in ph.items()}
+
+
+def extra_batched_fp64(torch, ctx, m, stream, sigs, sigs_host) -> dict:
+    """The same 64-signal batch through the FP64 kernels (the plain path's
+    arithmetic, batched): separates the batching gain from the precision
+    gain."""
+    opts = [solve_opts(ctx, sg.sigma, m.FP64) for sg in sigs_host]
+    rngs = [m.Rng(SEED_RNG + i) for i in range(len(sigs))]
+
+    def step():
+        for i, r in enumerate(rngs):
+            r.seed(SEED_RNG + i)
+        return ctx.solve_batched(sigs, rngs, opts)
+
+    ms = _event_ms(torch, stream, step, 2, 1)
+    return {"value": len(sigs) / (ms / 1e3), "unit": "solves/s",
+            "ms_per_step": ms, "batch": len(sigs)}
+
+
+def extra_config3(torch, ctx, m, stream, peak: float) -> dict:
+    """Config 3: 256 signals, N = 2^e with e uniform in 16..24, S uniform in
+    [10, 2000], unit modes, sigma = 1e-6, made on the device; one batched
+    solve per step. Reports the share of iterations the precision policy ran
+    on the FP64 kernels."""
+    from mpsft_gb300.signals import config3_spec
+    specs = [config3_spec(i) for i in range(256)]
+    sigs = [ctx.generate(sp.n, sp.k, sp.c, sp.sigma, sp.seed, m.C64) for sp in specs]
+    opts = [ctx.solve_options(sp.k.size, sp.sigma, trials=1, min_bins=51,
+                              window_delta=1e-5, window_threshold=0.1,
+                              max_stale_iter=5, precision=m.FP32) for sp in specs]
+    rngs = [m.Rng(SEED_RNG + i) for i in range(256)]
+    last = {}
+
+    def step():
+        for i, r in enumerate(rngs):
+            r.seed(SEED_RNG + i)
+        last["stats"] = ctx.solve_batched(sigs, rngs, opts)[1]
+
+    try:
+        ms = _event_ms(torch, stream, step, 3, 1)
+        st = last["stats"]
+        iters = sum(x["iterations"] for x in st)
+        fp64 = sum(x["fp64_iterations"] for x in st)
+        roof = _profiled_roofline(ctx, step, peak)
+    finally:
+        for sg in sigs:
+            sg.free()
+    return {"value": 256 / (ms / 1e3), "unit": "solves/s", "ms_per_step": ms,
+            "signals": 256, "samples": int(sum(sp.n for sp in specs)),
+            "iterations_per_step": iters, "fp64_iterations_per_step": fp64,
+            "fp64_iteration_share": fp64 / iters,
+            "binning_roofline": roof.get("all")}
+
+
+def extra_config5(torch, ctx, m, stream, peak: float) -> dict:
+    """Config 5: N = 2^26 complex64 (512 MiB, x far beyond L2), S = 4000 with
+    25% close pairs, |c| log-uniform [1e-3, 1], 40 dB, made on the device;
+    one signal and a batch of four. The binning gathers from HBM: its
+    achieved GB/s against the measured HBM copy rate."""
+    from mpsft_gb300.signals import config5_spec
+    specs = [config5_spec(5 + i) for i in range(4)]
+    sigs = [ctx.generate(sp.n, sp.k, sp.c, sp.sigma, sp.seed, m.C64) for sp in specs]
+    opts = [ctx.solve_options(4000, sp.sigma, trials=1, min_bins=51,
+                              window_delta=1e-5, window_threshold=0.1,
+                              max_stale_iter=5, precision=m.FP32) for sp in specs]
+    out = {}
+    try:
+        for g in (1, 4):
+            rngs = [m.Rng(SEED_RNG + i) for i in range(g)]
+
+            def step(g=g, rngs=rngs):
+                for i, r in enumerate(rngs):
+                    r.seed(SEED_RNG + i)
+                ctx.solve_batched(sigs[:g], rngs, opts[:g])
+
+            ms = _event_ms(torch, stream, step, 2, 1)
+            roof = _profiled_roofline(ctx, step, peak)
+            out[f"batch{g}"] = {"value": g / (ms / 1e3), "unit": "solves/s",
+                                "ms_per_step": ms, "binning_roofline": roof}
+    finally:
+        for sg in sigs:
+            sg.free()
+    return out
+
+
+def extra_bm_bin_in_time(ctx, m) -> dict:
+    """The reference's own binning micro-benchmark shape (BM_BinInTime,
+    src/binner_bench.cc:28-53): N = 4194301, B = 501, bits = 15 (31 rows),
+    delta = 1e-6; each call draws a transform and q from the RNG and bins one
+    signal resident on the device, the bins returned to host memory (the
+    reference's Run writes a host matrix). Published reference time: 13.18 ms
+    per call (BinInTimeV4, one i7-6700K core, README.md:82)."""
+    n, bins, bits, delta = 4194301, 501, 15, 1e-6
+    rng = np.random.default_rng(28)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex128)
+    out = {"config": "N=4194301 B=501 bits=15 delta=1e-6", "published_ref_ms": 13.18}
+    for name, dt, prec in (("fp32_c64", np.complex64, m.FP32),
+                           ("fp64_c128", np.complex128, m.FP64)):
+        sig = ctx.upload(x.astype(dt))
+        r = m.Rng(123534)
+
+        def call():
+            a = (r.int32() % (n - 1)) + 1
+            b = r.int32() % n
+            c = r.int32() % n
+            q = r.int32() % n
+            return ctx.bin_in_time(sig, bins, bits, delta, a, b, c, q, precision=prec)
+
+        for _ in range(3):
+            call()
+        reps = 30
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        call_ms = 1e3 * (time.perf_counter() - t0) / reps
+        ctx.set_profiling(True)
+        kms, kbytes = [], []
+        for _ in range(5):
+            call()
+            rec = ctx.bin_launches()[0]
+            kms.append(rec["ms"])
+            kbytes.append(rec["bytes"])
+        ctx.set_profiling(False)
+        sig.free()
+        kern = statistics.median(kms)
+        out[name] = {"call_ms": call_ms, "kernel_ms": kern,
+                     "kernel_gb_per_s": statistics.median(kbytes) / (kern / 1e3) / 1e9,
+                     "speedup_vs_published": 13.18 / call_ms}
+    return out
 
 
 def run_config3(args) -> None:
@@ -552,16 +783,10 @@ def run_gpu(args) -> None:
     # ---- the same steps again with an event pair around every binning
     # launch (the host drives the iterations here); gives the binning roofline
     ctx.set_profiling(True)
-    bin_ms = 0.0
-    bin_bytes = 0
-    bin_launches = 0
-    bin_gathers = 0
+    bin_records = []
     for _ in range(args.steps):
         out, stats = step()
-        bin_ms += stats[0]["bin_ms"]
-        bin_launches += stats[0]["bin_launches"]
-        bin_bytes += sum(s["bin_bytes"] for s in stats)
-        bin_gathers += sum(s["gathers"] for s in stats)
+        bin_records += ctx.bin_launches()
     torch.cuda.synchronize()
     ctx.set_profiling(False)
 
@@ -644,16 +869,21 @@ def run_gpu(args) -> None:
                  "accuracy": accuracy(sg0, k32, c32, k64, c64),
                  "test_data_pipeline": test_data_pipeline(ctx, m, sg0, k32, c32),
                  "dense_fft": dense_fft(torch, sigs_host, torch.device("cuda", local))}
+        if not args.no_extras:
+            peak = load_peaks()["hbm_gbs"]
+            extra["batched_fp64"] = extra_batched_fp64(torch, ctx, m, stream, sigs,
+                                                       sigs_host)
+            extra["batched_fp64"]["batching_gain"] = (
+                extra["batched_fp64"]["value"] / extra["plain_fp64_gpu"]["value"])
+            extra["config3"] = extra_config3(torch, ctx, m, stream, peak)
+            extra["config5"] = extra_config5(torch, ctx, m, stream, peak)
+            extra["bm_bin_in_time"] = extra_bm_bin_in_time(ctx, m)
 
     if rank == 0:
         peaks = load_peaks()
-        achieved = (bin_bytes / (bin_ms / 1e3)) / 1e9 if bin_ms > 0 else None
-        gathers_per_launch = None
-        traffic_per_gather = profile_traffic()
-        # DRAM bytes of an average binning launch: the captured launch's bytes
-        # per gathered sample times the gathers of an average launch
-        traffic = (traffic_per_gather * bin_gathers / bin_launches
-                   if traffic_per_gather and bin_launches else None)
+        phases = binning_roofline(bin_records, 51, peaks["hbm_gbs"], profile_traffic())
+        allp = phases.get("all", {})
+        achieved = allp.get("achieved")
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3),
@@ -676,15 +906,16 @@ def run_gpu(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-                         "traffic": traffic,
-                         "achieved_bytes_per_launch": (bin_bytes / bin_launches
-                                                       if bin_launches else None),
+                         "traffic": allp.get("traffic"),
+                         "achieved_bytes_per_launch": allp.get("bytes_per_launch"),
                          "kernel": "k_bin_fold32 (gather/window/modulate/fold)",
                          "bytes_model": "32 B sector per gathered sample + window "
                                         "table + fold output",
-                         "launches": bin_launches,
-                         "kernel_ms": bin_ms,
-                         "peak_source": peaks["source"]},
+                         "launches": allp.get("launches"),
+                         "kernel_ms": allp.get("kernel_ms"),
+                         "peak_source": peaks["source"],
+                         "traffic_source": os.path.relpath(PHASE_PROFILE, ROOT),
+                         "phases": {k: v for k, v in phases.items() if k != "all"}},
             "clocks": clk,
             "gpu_launches": int(launches),
         }

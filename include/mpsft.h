@@ -67,6 +67,23 @@ int mpsft_ctx_set_stream(mpsft_ctx *ctx, void *stream);
 /* Time every binning-kernel launch with CUDA events (0 = off, default). The
  * totals are reported in mpsft_stats. */
 int mpsft_ctx_set_profiling(mpsft_ctx *ctx, int enable);
+/* One timed binning launch (gather, window, modulate, fold) of a call made
+ * with profiling on. */
+typedef struct {
+  int32_t iteration;  /* iteration of the call's loop (0 = the first)        */
+  int32_t signals;    /* signals the launch binned                           */
+  int32_t max_bins;   /* largest and smallest bins among them                */
+  int32_t min_bins;
+  int64_t gathers;    /* samples gathered                                    */
+  int64_t bytes;      /* algorithmic bytes: 32 per gathered sample (one      */
+                      /* sector) + the window table + the fold output        */
+  double ms;          /* duration from CUDA events around the launch         */
+} mpsft_bin_launch;
+/* The binning launches of the context's last call made with profiling on, in
+ * launch order: writes min(cap, total) records to out and the total to
+ * *count. */
+int mpsft_ctx_bin_launches(const mpsft_ctx *ctx, mpsft_bin_launch *out,
+                           int32_t cap, int32_t *count);
 const char *mpsft_last_error(const mpsft_ctx *ctx);
 const char *mpsft_status_string(int status);
 
@@ -75,6 +92,8 @@ const char *mpsft_status_string(int status);
  * [0, 2^31 - 1]; mpsft_rng_create(123534) is the state MainInit leaves. */
 int mpsft_rng_create(int32_t seed, mpsft_rng **out);
 int mpsft_rng_destroy(mpsft_rng *rng);
+/* Reseeds the engine only, as RandomSeed does: a normal draw held back by
+ * the normal distribution (the second of a pair) survives the reseed. */
 int mpsft_rng_seed(mpsft_rng *rng, int32_t seed);
 int32_t mpsft_rng_int32(mpsft_rng *rng);
 /* count draws of std::normal_distribution<double> on the same engine (the
@@ -137,10 +156,14 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
  * NULL = the legacy default stream). Scratch is one fixed array of about
  * 2.5 MiB compiled into the library and held on every GPU that loads it.
  * Limits: bins <= 2047, bits <= 20, window folds p/bins <= 80; larger sizes
- * return MPSFT_ERR_CAPACITY. The first call on a device resolves the array's
- * address and fills its twiddle table, synchronising stream; make that first
- * call before any stream capture. Calls share the array, so calls that overlap
- * on the GPU race; calls on one stream are ordered and safe. */
+ * return MPSFT_ERR_CAPACITY. n must be prime or a power of two, as for
+ * mpsft_bin_in_time (MPSFT_ERR_UNSUPPORTED_N otherwise). Every call resolves
+ * the array's address on the current device (cudaGetSymbolAddress, which
+ * allocates nothing) and passes its descriptor as a kernel argument, so it
+ * copies nothing from host memory; the FFT twiddle table in the array is
+ * filled on the device by the first call after the library's device code is
+ * loaded. Calls share the array, so calls that overlap on the GPU race; calls
+ * on one stream are ordered and safe. */
 int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n, int dtype,
                               int32_t bins, int32_t bits, double delta,
                               int32_t a, int32_t b, int32_t c, int32_t q,

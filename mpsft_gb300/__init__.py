@@ -80,6 +80,17 @@ class Analysis(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class BinLaunch(ctypes.Structure):
+    """One timed binning launch (mpsft_bin_launch)."""
+    _fields_ = [("iteration", ctypes.c_int32), ("signals", ctypes.c_int32),
+                ("max_bins", ctypes.c_int32), ("min_bins", ctypes.c_int32),
+                ("gathers", ctypes.c_int64), ("bytes", ctypes.c_int64),
+                ("ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("found", ctypes.c_int32),
                 ("gathers", ctypes.c_int64), ("bin_bytes", ctypes.c_int64),
@@ -113,6 +124,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_ctx_destroy": (I, [P]),
         "mpsft_ctx_set_stream": (I, [P, P]),
         "mpsft_ctx_set_profiling": (I, [P, I]),
+        "mpsft_ctx_bin_launches": (I, [P, P, I32, P]),
         "mpsft_last_error": (ctypes.c_char_p, [P]),
         "mpsft_status_string": (ctypes.c_char_p, [I]),
         "mpsft_rng_create": (I, [I32, PP]),
@@ -254,6 +266,16 @@ class Context:
 
     def set_profiling(self, on: bool) -> None:
         _check(self, self._lib.mpsft_ctx_set_profiling(self._h, int(bool(on))))
+
+    def bin_launches(self) -> list[dict]:
+        """The timed binning launches of the last call made with profiling
+        on (mpsft_ctx_bin_launches), in launch order."""
+        count = np.zeros(1, np.int32)
+        _check(self, self._lib.mpsft_ctx_bin_launches(self._h, None, 0, _ptr(count)))
+        recs = (BinLaunch * max(1, int(count[0])))()
+        _check(self, self._lib.mpsft_ctx_bin_launches(self._h, recs, int(count[0]),
+                                                      _ptr(count)))
+        return [recs[j].as_dict() for j in range(int(count[0]))]
 
     # ---- signals --------------------------------------------------------
     def upload(self, x: np.ndarray) -> "Signal":

@@ -2,9 +2,11 @@
 
 Every CUDA source in mpsft_gb300/csrc is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, and linked with
-``nvcc -shared``. The host C++ adapters (mpsft_gb300/host) go into the same
-library. No cmake, no torch extension machinery: the product is a plain C-ABI
-library that any FFI (ctypes, cgo, JNI) can load.
+``nvcc -shared``. No cmake, no torch extension machinery: the product is a
+plain C-ABI library that any FFI (ctypes, cgo, JNI) can load. The C++ adapter
+that plugs the library into the reference's own binner factory
+(mpsft_gb300/adapter) is compiled against the reference's headers by its user,
+not here.
 """
 from __future__ import annotations
 
@@ -18,7 +20,6 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-HOST = os.path.join(HERE, "host")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libmpsft_gb300.so")
 OBJ_DIR = os.path.join(HERE, "_build")
@@ -42,7 +43,6 @@ def _nvcc() -> str:
 
 def _sources() -> list[str]:
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    srcs += sorted(glob.glob(os.path.join(HOST, "*.cc")))
     return srcs
 
 
@@ -58,7 +58,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(
-        os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(HOST, "*.h")) + [
+        os.path.join(CSRC, "*.h")) + [
         os.path.join(ROOT, "include", "mpsft.h")]
     srcs = _sources()
     objs = []
@@ -67,11 +67,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            if src.endswith(".cu"):
-                cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]
-            else:
-                cmd = [nvcc, "-x", "cu"] + NVCC_FLAGS + ["-c", src, "-o", obj]
-            cmds.append(cmd)
+            cmds.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

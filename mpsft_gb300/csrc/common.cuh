@@ -333,6 +333,15 @@ struct ModN {
 };
 
 
+// FFT twiddle e of the shared table: e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2,
+// in FP64 and rounded to FP32 (every table of the library is filled by this).
+__device__ inline void TwiddleAt(int e, float2 *tw32, double2 *tw64) {
+  double s, c;
+  sincospi(-2.0 * double(e) / double(kMaxFFT), &s, &c);
+  tw64[e] = make_double2(c, s);
+  tw32[e] = make_float2(float(c), float(s));
+}
+
 __device__ inline float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

@@ -47,6 +47,12 @@ int Fail(mpsft_ctx *ctx, int code, const std::string &msg) {
     }                                                                          \
   } while (0)
 
+}  // namespace
+
+// Integer and window helpers shared with the other host translation units
+// (declared in internal.h).
+namespace mpsft {
+
 bool IsPow2(int64_t n) { return n > 0 && (n & (n - 1)) == 0; }
 
 uint64_t MulModU64(uint64_t a, uint64_t b, uint64_t m) {
@@ -117,10 +123,6 @@ int32_t NumBits(int32_t n, int32_t bins) {
 }
 
 // Window scalars, in the reference's operation order (src/window.cc:28-51).
-struct WinParams {
-  int32_t p = 0, p2 = 0, folds = 0;
-  double width = 0, sigma_f = 0, sigma_t = 0, erf_d = 0;
-};
 WinParams MakeWindow(int32_t bins, double delta) {
   WinParams w;
   w.width = 1.0 / (2.0 * bins);
@@ -143,9 +145,13 @@ int FFTLog2(int32_t bins) {
   return l;
 }
 
-struct Transform {
-  int32_t a, b, c, a_inv;
-};
+bool SupportedN(int64_t n) {
+  return n >= 3 && n <= INT32_MAX && (IsPow2(n) || IsPrime(n));
+}
+
+}  // namespace mpsft
+
+namespace {
 
 // Transform(n) (src/integer.cc:44-49): a, b, c drawn in that order; a is made
 // odd for power-of-two n so that it is invertible.
@@ -454,6 +460,10 @@ int32_t NextPow2(int64_t v) {
   return p;
 }
 
+}  // namespace
+
+namespace mpsft {
+
 // Fills the per-iteration scalars of it for (bins, bits, transform, q's).
 // bq = e^{2 pi i (b q mod n)/n}, as Sinusoid(MulMod(b, q, n) / n); always
 // computed here on the host so that every loop uses the same values.
@@ -499,6 +509,10 @@ void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
   it->fft_log2m = FFTLog2(bins);
   it->fft_m = 1 << it->fft_log2m;
 }
+
+}  // namespace mpsft
+
+namespace {
 
 int CheckWindow(mpsft_ctx *ctx, int32_t bins, double delta, bool fp64) {
   if (bins <= 0 || bins % 2 == 0) {
@@ -1353,7 +1367,11 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
   }
   int active = host_loop ? nsig : 0;
+  if (ctx->profiling) ctx->bin_launches.clear();
   while (active > 0) {
+    mpsft_bin_launch rec{};
+    rec.iteration = int32_t(ctx->bin_launches.size());
+    rec.min_bins = INT32_MAX;
     for (int i = 0; i < nsig; ++i) {
       SigIter &it = its[i];
       if (run[i].done) {
@@ -1381,7 +1399,13 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       run[i].last_bins = it.force_fp64 ? -1 : bins;
       run[i].gathers += int64_t(it.trials) * it.p * it.rows;
       run[i].bin_bytes += BinBytes(it, fp64 || it.force_fp64);
+      rec.signals += 1;
+      rec.max_bins = std::max(rec.max_bins, bins);
+      rec.min_bins = std::min(rec.min_bins, bins);
+      rec.gathers += int64_t(it.trials) * it.p * it.rows;
+      rec.bytes += BinBytes(it, fp64 || it.force_fp64);
     }
+    if (ctx->profiling) ctx->bin_launches.push_back(rec);
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
                                     cudaMemcpyHostToDevice, ctx->stream));
     for (int i = 0; i < nsig; ++i) {
@@ -1429,6 +1453,14 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
   int first_err = MPSFT_OK;
   const double bin_ms = timer.TotalMs();
+  if (ctx->profiling) {
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t j = 0; j < ctx->bin_launches.size() && j < timer.used.size(); ++j) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, timer.used[j].first, timer.used[j].second);
+      ctx->bin_launches[j].ms = ms;
+    }
+  }
   // the call's own kernels outside the loop: table clearing, phase tables,
   // the energy pair (FP32), the export and the upload copies
   launches += 2 + (fp64 ? 0 : 2) + 1 + ctx->up_launches;
@@ -1651,6 +1683,15 @@ int mpsft_ctx_set_profiling(mpsft_ctx *ctx, int enable) {
   return MPSFT_OK;
 }
 
+int mpsft_ctx_bin_launches(const mpsft_ctx *ctx, mpsft_bin_launch *out,
+                           int32_t cap, int32_t *count) {
+  if (!ctx || !count || (cap > 0 && !out)) return MPSFT_ERR_INVALID;
+  const int32_t total = int32_t(ctx->bin_launches.size());
+  for (int32_t j = 0; j < total && j < cap; ++j) out[j] = ctx->bin_launches[j];
+  *count = total;
+  return MPSFT_OK;
+}
+
 const char *mpsft_last_error(const mpsft_ctx *ctx) {
   return ctx ? ctx->err.c_str() : "null context";
 }
@@ -1667,9 +1708,9 @@ int mpsft_rng_destroy(mpsft_rng *rng) {
 }
 int mpsft_rng_seed(mpsft_rng *rng, int32_t seed) {
   if (!rng) return MPSFT_ERR_INVALID;
+  // RandomSeed (src/base.cc:52) reseeds the engine only: a normal draw the
+  // distribution holds back (the second of a pair) survives the reseed
   rng->eng.seed(seed);
-  rng->uid.reset();
-  rng->nd.reset();
   return MPSFT_OK;
 }
 int32_t mpsft_rng_int32(mpsft_rng *rng) { return rng ? rng->Draw() : -1; }
@@ -1973,6 +2014,15 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
                                     : cudaMemcpyDeviceToHost,
                       st));
   MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  if (ctx->profiling) {
+    mpsft_bin_launch rec{};
+    rec.signals = 1;
+    rec.max_bins = rec.min_bins = bins;
+    rec.gathers = int64_t(it.p) * it.rows;
+    rec.bytes = BinBytes(it, fp64);
+    rec.ms = timer.TotalMs();
+    ctx->bin_launches.assign(1, rec);
+  }
   return MPSFT_OK;
 }
 

@@ -66,6 +66,8 @@ struct mpsft_ctx {
   int64_t up_launches = 0;  // copy kernels Upload launched in this call
   size_t h_stage_n = 0;
   std::vector<cudaEvent_t> events;
+  // binning launches of the last call made with profiling on
+  std::vector<mpsft_bin_launch> bin_launches;
   // table cache of FP32 solves: window tables (FP32, FP64, float-float) and
   // FP32 Bluestein tables per odd number of bins for one window delta, built
   // on first use and kept, like FFT plans (win_dev: block offsets, valid and
@@ -98,6 +100,37 @@ namespace mpsft {
 
 // Records msg as the context's last error and returns code.
 int CtxFail(mpsft_ctx *ctx, int code, const std::string &msg);
+
+// ---- integer and window helpers (engine.cu) ----
+bool IsPow2(int64_t n);
+// Deterministic Miller-Rabin, exact for n < 3.2e9.
+bool IsPrime(int64_t n);
+// A length the solver supports: prime or a power of two in [3, 2^31 - 1].
+bool SupportedN(int64_t n);
+// a^{-1} mod m by the extended Euclidean algorithm; 0 if not invertible.
+int32_t InverseMod(int64_t a, int64_t m);
+// NumBits (src/iterate.cc:30-42).
+int32_t NumBits(int32_t n, int32_t bins);
+// Window scalars, in the reference's operation order (src/window.cc:28-51).
+struct WinParams {
+  int32_t p = 0, p2 = 0, folds = 0;
+  double width = 0, sigma_f = 0, sigma_t = 0, erf_d = 0;
+};
+WinParams MakeWindow(int32_t bins, double delta);
+// log2 of the Bluestein transform size M (the power of two >= 2 bins - 1).
+int FFTLog2(int32_t bins);
+// The transform of one Iterate call (src/integer.h:68-82).
+struct Transform {
+  int32_t a, b, c, a_inv;
+};
+// e^{2 pi i (b q mod n)/n} (re, im) as the reference's
+// Sinusoid(MulMod(b, q, n) / n).
+void RowPhase(int32_t b, int32_t q, int32_t n, double *re, double *im);
+// The per-iteration scalars of it (everything but its buffers) for one
+// signal, bins, bits, window delta, transform and trials q's.
+void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
+              double delta, const Transform &tf, const int32_t *q,
+              int32_t trials);
 // MPSFT_OK when n is a length the solver supports (prime or a power of two in
 // [3, 2^31 - 1]); otherwise records why.
 int CtxCheckN(mpsft_ctx *ctx, int64_t n);

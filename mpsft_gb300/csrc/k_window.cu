@@ -20,10 +20,7 @@ namespace {
 __global__ void k_twiddles(float2 *tw32, double2 *tw64) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= kMaxFFT / 2) return;
-  double s, c;
-  sincospi(-2.0 * double(e) / double(kMaxFFT), &s, &c);
-  tw64[e] = make_double2(c, s);
-  tw32[e] = make_float2(float(c), float(s));
+  TwiddleAt(e, tw32, tw64);
 }
 
 // sin(x)/x with the reference's Taylor guard (src/sincos.cc:69-88).

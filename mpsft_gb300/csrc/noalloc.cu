@@ -7,19 +7,22 @@
 // (kNoAllocScratchBytes, 2.5 MiB), which every GPU that loads this
 // library holds until the process exits. The caller passes the input samples
 // and the output bin matrix as device pointers and a stream; nothing here calls
-// cudaMalloc, cudaFree or any allocating library routine.
+// cudaMalloc, cudaFree or any allocating library routine, and nothing is
+// copied from host memory: the call's descriptor travels as a kernel
+// argument.
 //
 // Host code cannot use the array's name as a device address (it names a host
-// stand-in), so the first call on each device, with that device current,
-// resolves the address with cudaGetSymbolAddress and fills the FFT twiddle
-// table in the array; that first call synchronises its stream and should come
-// before any stream capture. All calls share the array and leave their data in
-// it: calls that overlap on the GPU (two streams, or two threads) race.
-#include <cmath>
+// stand-in), so every call, with the caller's device current, resolves the
+// address with cudaGetSymbolAddress (a lookup, no allocation; a context reset
+// reloads the module, possibly elsewhere). The FFT twiddle table inside the
+// array is filled on the device by the first call after the module is loaded:
+// a word in the array records that it is in place, and a reloaded module
+// starts with that word clear. All calls share the array and leave their data
+// in it: calls that overlap on the GPU (two streams, or two threads) race.
 #include <cstring>
-#include <mutex>
 
 #include "../../include/mpsft.h"
+#include "internal.h"
 #include "launch.h"
 
 namespace {
@@ -34,7 +37,8 @@ constexpr int64_t kNaMaxP2 =
     (int64_t(kFoldLanes) * kMaxFoldsPerLane * kNaMaxBins - 1) / 2;
 
 constexpr size_t Align256(size_t v) { return (v + 255) & ~size_t(255); }
-constexpr size_t kOffIter = 0;
+constexpr size_t kOffReady = 0;
+constexpr size_t kOffIter = kOffReady + 256;
 constexpr size_t kOffTw32 = kOffIter + Align256(sizeof(SigIter));
 constexpr size_t kOffTw64 = kOffTw32 + Align256(sizeof(float2) * kMaxFFT / 2);
 constexpr size_t kOffWt32 = kOffTw64 + Align256(sizeof(double2) * kMaxFFT / 2);
@@ -48,37 +52,25 @@ constexpr size_t kNoAllocScratchBytes =
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char *g_scratch_addr[kMaxDevices] = {};
+// value of the ready word once the twiddles are in the array
+constexpr uint32_t kTwiddlesReady = 0x54574431u;
 
-// Resolves the scratch address on the current device and fills the twiddles
-// (once per device).
-int ScratchForCurrentDevice(cudaStream_t stream, unsigned char **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    cudaGetLastError();
-    return MPSFT_ERR_CUDA;
+// Stores the call's descriptor (a kernel argument, so nothing is copied from
+// host memory) and, when the ready word is clear, fills the twiddle table and
+// then sets the word. One block: every thread has finished its share of the
+// table before the word is set, and later kernels of the call, ordered after
+// this one on the stream, see the whole table.
+__global__ void __launch_bounds__(1024)
+    k_noalloc_setup(SigIter it, SigIter *dst, float2 *tw32, double2 *tw64,
+                    uint32_t *ready) {
+  if (threadIdx.x == 0) *dst = it;
+  if (*(volatile uint32_t *)ready == kTwiddlesReady) return;
+  for (int e = threadIdx.x; e < kMaxFFT / 2; e += blockDim.x) {
+    TwiddleAt(e, tw32, tw64);
   }
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (g_scratch_addr[dev] == nullptr) {
-    void *ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess ||
-        ptr == nullptr) {
-      cudaGetLastError();
-      return MPSFT_ERR_CUDA;
-    }
-    unsigned char *base = static_cast<unsigned char *>(ptr);
-    LaunchTwiddles(reinterpret_cast<float2 *>(base + kOffTw32),
-                   reinterpret_cast<double2 *>(base + kOffTw64), stream);
-    if (cudaStreamSynchronize(stream) != cudaSuccess ||
-        cudaGetLastError() != cudaSuccess) {
-      return MPSFT_ERR_CUDA;
-    }
-    g_scratch_addr[dev] = base;
-  }
-  *out = g_scratch_addr[dev];
-  return MPSFT_OK;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) *(volatile uint32_t *)ready = kTwiddlesReady;
 }
 
 }  // namespace
@@ -101,51 +93,32 @@ extern "C" int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n,
     return MPSFT_ERR_INVALID;
   }
 
-  // Window scalars in the reference's operation order (src/window.cc:28-51).
-  const double width = 1.0 / (2.0 * bins);
-  const double sq = std::sqrt(-std::log(delta));
-  const double sigma_f = 0.5 / (bins * 2.0 * M_SQRT2 * sq);
-  const double sigma_t = 1.0 / ((2.0 * M_PI) * sigma_f);
-  const double tmp = 2.0 * M_SQRT2 * sigma_t * sq + 1;
-  int32_t folds = int32_t(std::ceil(tmp / double(bins)));
-  if (folds % 2 == 0) ++folds;
-  if (folds > kFoldLanes * kMaxFoldsPerLane) return MPSFT_ERR_CAPACITY;
-  const int32_t p = folds * bins;
-  int log2m = 0;
-  while ((1 << log2m) < 2 * bins - 1) ++log2m;
+  // the same lengths as mpsft_bin_in_time (the permutation needs an
+  // invertible a: prime or power-of-two n)
+  if (!SupportedN(n)) return MPSFT_ERR_UNSUPPORTED_N;
+  const WinParams w = MakeWindow(bins, delta);
+  if (w.folds > kFoldLanes * kMaxFoldsPerLane) return MPSFT_ERR_CAPACITY;
 
+  void *ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess ||
+      ptr == nullptr) {
+    cudaGetLastError();
+    return MPSFT_ERR_CUDA;
+  }
+  unsigned char *base = static_cast<unsigned char *>(ptr);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  unsigned char *base = nullptr;
-  const int rc = ScratchForCurrentDevice(st, &base);
-  if (rc != MPSFT_OK) return rc;
 
+  // the descriptor mpsft_bin_in_time builds, over the caller's buffers and
+  // the array
   const bool fp64 = precision == MPSFT_PREC_FP64;
+  mpsft_signal sig;
+  sig.d_x = const_cast<void *>(x_device);
+  sig.n = n;
+  sig.dtype = dtype;
+  const Transform tf{a, b, c, InverseMod(a, n)};
   SigIter it;
   std::memset(&it, 0, sizeof(it));
-  it.x = x_device;
-  it.n = int32_t(n);
-  it.bins = bins;
-  it.bits = bits;
-  it.rows = 1 + 2 * bits;
-  it.p = p;
-  it.p2 = (p - 1) / 2;
-  it.folds = folds;
-  it.a = a;
-  it.b = b;
-  it.c = c;
-  it.trials = 1;
-  it.active = 1;
-  it.q[0] = q;
-  const int64_t m = (int64_t(b) * q) % n;
-  const double f = double(m) / double(n) * (2.0 * M_PI);
-  it.bq_re[0] = std::cos(f);
-  it.bq_im[0] = std::sin(f);
-  it.width = width;
-  it.sigma_f = sigma_f;
-  it.erf_d = M_SQRT2 * M_PI * sigma_t;
-  it.fft_log2m = log2m;
-  it.fft_m = 1 << log2m;
-  SetFixedPoint(&it);
+  FillIter(&it, &sig, bins, bits, delta, tf, &q, 1);
   it.wt32 = reinterpret_cast<float *>(base + kOffWt32);
   it.wt64 = reinterpret_cast<double *>(base + kOffWt64);
   it.fold = base + kOffFold;
@@ -158,13 +131,10 @@ extern "C" int mpsft_bin_in_time_noalloc(const void *x_device, int64_t n,
   it.chat64 = reinterpret_cast<double2 *>(base + kOffChat);
 
   SigIter *d_it = reinterpret_cast<SigIter *>(base + kOffIter);
-  if (cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice, st) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    return MPSFT_ERR_CUDA;
-  }
-  const float2 *tw32 = reinterpret_cast<const float2 *>(base + kOffTw32);
-  const double2 *tw64 = reinterpret_cast<const double2 *>(base + kOffTw64);
+  float2 *tw32 = reinterpret_cast<float2 *>(base + kOffTw32);
+  double2 *tw64 = reinterpret_cast<double2 *>(base + kOffTw64);
+  k_noalloc_setup<<<1, 1024, 0, st>>>(it, d_it, tw32, tw64,
+                                      reinterpret_cast<uint32_t *>(base + kOffReady));
   if (fp64) {
     LaunchWindow(d_it, 1, it.p2, st);
   } else {

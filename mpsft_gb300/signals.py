@@ -112,8 +112,44 @@ def config3(index: int, base_seed: int = 300) -> SparseSignal:
     return make_signal(1 << e, s, base_seed * 1000 + index, sigma=1e-6)
 
 
+@dataclass
+class SignalSpec:
+    """The modes and noise level of a signal whose samples are made on the
+    device (mpsft_signal_generate): no host-side synthesis."""
+    n: int
+    k: np.ndarray          # int64 distinct positions
+    c: np.ndarray          # complex128 coefficients
+    sigma: float
+    seed: int              # key of the device noise generator
+
+
+def config3_spec(index: int, base_seed: int = 300) -> SignalSpec:
+    """config3(index)'s length, modes and noise level (the same draws), for
+    generation on the device."""
+    rng = np.random.default_rng(base_seed + index)
+    e = int(rng.integers(16, 25))
+    s = int(rng.integers(10, 2001))
+    seed = base_seed * 1000 + index
+    r2 = np.random.default_rng(seed)
+    k = distinct_positions(r2, 1 << e, s)
+    c = np.exp(2j * np.pi * r2.uniform(size=s))
+    return SignalSpec(n=1 << e, k=k, c=c, sigma=1e-6, seed=seed)
+
+
 def config5(seed: int = 5) -> SparseSignal:
     """N = 2^26 complex64 (512 MiB), S = 4000 with 25% of the modes in close
     pairs 1-3 apart, |c| log-uniform in [1e-3, 1], 40 dB SNR."""
     return make_signal(1 << 26, 4000, seed, magnitude="loguniform",
                        mag_range=(1e-3, 1.0), snr_db=40.0, pair_frac=0.25)
+
+
+def config5_spec(seed: int = 5) -> SignalSpec:
+    """config5(seed)'s modes and noise level (the same draws), for generation
+    on the device (512 MiB per signal)."""
+    rng = np.random.default_rng(seed)
+    n, s = 1 << 26, 4000
+    k = paired_positions(rng, n, s, 0.25)
+    mag = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), s))
+    c = mag * np.exp(2j * np.pi * rng.uniform(size=s))
+    sigma = float(10.0 ** (-40.0 / 20.0) * np.sqrt(np.sum(mag ** 2)))
+    return SignalSpec(n=n, k=k, c=c, sigma=sigma, seed=seed)

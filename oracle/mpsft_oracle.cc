@@ -455,6 +455,7 @@ extern "C" {
 
 void orc_seed(int32_t seed) { g_rng.seed(seed); }
 int32_t orc_random_int32(void) { return DrawInt32(); }
+double orc_random_normal(void) { return DrawNormal(); }
 int32_t orc_num_bits(int32_t n, int32_t bins) { return NumBits(n, bins); }
 
 int32_t orc_window(int32_t n, int32_t bins, double delta, double *wt,

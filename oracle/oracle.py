@@ -70,6 +70,7 @@ class Oracle:
         sig = {
             "orc_seed": (None, [_i32]),
             "orc_random_int32": (_i32, []),
+            "orc_random_normal": (_dbl, []),
             "orc_num_bits": (_i32, [_i32, _i32]),
             "orc_window": (_i32, [_i32, _i32, _dbl, _p, _i32]),
             "orc_window_sample_in_freq": (_dbl, [_i32, _i32, _dbl, _dbl]),
@@ -100,6 +101,9 @@ class Oracle:
 
     def random_int32(self) -> int:
         return int(self.lib.orc_random_int32())
+
+    def random_normal(self) -> float:
+        return float(self.lib.orc_random_normal())
 
     # --- primitives --------------------------------------------------------
     def num_bits(self, n: int, bins: int) -> int:

@@ -23,6 +23,9 @@ extern "C" {
 /* mps::RandomSeed / mps::RandomInt32 (src/base.cc:52-53). */
 void orc_seed(int32_t seed);
 int32_t orc_random_int32(void);
+/* mps::RandomNormal (src/base.cc:55): std::normal_distribution<double> on the
+ * same engine (RandomSeed reseeds the engine only, src/base.cc:52). */
+double orc_random_normal(void);
 
 /* NumBits (src/iterate.cc:30-42). */
 int32_t orc_num_bits(int32_t n, int32_t bins);

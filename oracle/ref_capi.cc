@@ -77,6 +77,7 @@ extern "C" {
 
 void orc_seed(int32_t seed) { RandomSeed(seed); }
 int32_t orc_random_int32(void) { return RandomInt32(); }
+double orc_random_normal(void) { return RandomNormal(); }
 
 int32_t orc_num_bits(int32_t n, int32_t bins) {
   // NumBits is file-local in src/iterate.cc; its definition is one loop:

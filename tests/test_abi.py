@@ -31,6 +31,29 @@ def test_rng_matches_reference(lib, golden):
     assert r.int32() == int(golden["rng_123534"][0])
 
 
+@pytest.mark.parametrize("kind", ["port", "ref"])
+def test_rng_reseed_keeps_the_held_normal(lib, kind):
+    """RandomSeed (src/base.cc:52) reseeds the engine only: after an odd
+    number of RandomNormal draws the distribution still holds the second value
+    of its last pair, and the first draw after a reseed returns it."""
+    from oracle import oracle
+    if not oracle.available(kind):
+        pytest.skip(f"oracle {kind} not built here")
+    o = oracle.Oracle(kind)
+    r = m.Rng(1)
+    o.seed(123537)
+    r.seed(123537)
+    want = [o.random_normal() for _ in range(3)]
+    assert r.normals(3).tolist() == want
+    o.seed(99)
+    r.seed(99)
+    # the held value, then two whole pairs: nothing is held afterwards, so
+    # the oracle's global state is as other tests expect it
+    want = [o.random_normal() for _ in range(5)] + [o.random_int32() for _ in range(3)]
+    got = r.normals(5).tolist() + [r.int32() for _ in range(3)]
+    assert got == want
+
+
 def test_num_bits_and_window_support(lib, port):
     for n in (1109, 4099, 1 << 16, 65537, 1 << 20, 1 << 22, 1048573):
         for bins in (1, 5, 11, 51, 101, 501, 2001, 8001):

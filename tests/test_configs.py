@@ -1,11 +1,16 @@
-"""The uneven batch (config 3) and the large stress case (config 5).
+"""The uneven batch (config 3), the large stress case (config 5) and the
+headline configuration at the reference's own prime length.
 
 Config 3: many signals of uneven N and S solved as one batch must give each
 signal exactly what its own single solve gives, and the oracle's frequency
-set. The test batch keeps config 3's distribution but draws N from
-{2^16, ..., 2^20} and S from [10, 400] so that host signal generation and the
-oracle stay within seconds (the full 256-signal batch with N up to 2^24 runs
-in bench.py's --workload config3 mode).
+set. The full batch (256 signals, N in 2^16..2^24, S in [10, 2000]) is made on
+the device (mpsft_signal_generate); a 40-signal batch of host-made signals
+checks more signals against the oracle.
+
+Prime N: the reference's benchmarks and tests run at primes near powers of two
+(kPrimes, src/base.h:50-55; published solve times at N = 4194301). At prime N
+the reference's own Transform applies (no power-of-two override) and the
+binning reduces indices by Barrett reduction instead of a mask.
 
 Config 5: N = 2^26 (512 MiB, far beyond L2), S = 4000 with 25% close pairs,
 40 dB: the FP32 batched path returns the oracle's exact frequency set (same
@@ -51,6 +56,70 @@ def test_config3_uneven_batch(ctx, port):
                                  500 + i, min_bins=51, window_delta=1e-5,
                                  max_stale_iter=5)
         assert out[i][0].tolist() == sorted(want), i
+
+
+def test_config3_full_batch(ctx, port):
+    """The 256-signal uneven batch at its stated sizes: every signal equals its
+    own single solve bit for bit, and for eight of them (the largest N and S
+    among them) the oracle's frequency set, coefficients within the FP32
+    tolerance."""
+    from mpsft_gb300.signals import config3_spec
+
+    specs = [config3_spec(i) for i in range(256)]
+    sigs = [ctx.generate(sp.n, sp.k, sp.c, sp.sigma, sp.seed, m.C64) for sp in specs]
+    opts = [_opts(ctx, sp.k.size, sp.sigma) for sp in specs]
+    out, stats = ctx.solve_batched(sigs, [m.Rng(900 + i) for i in range(256)], opts)
+    iters = sum(st["iterations"] for st in stats)
+    fp64_iters = sum(st["fp64_iterations"] for st in stats)
+    print(f"config3: {iters} iterations, {fp64_iters} on the FP64 kernels "
+          f"({fp64_iters / iters:.1%}) by the precision policy")
+    for i, ((k, c), st) in enumerate(zip(out, stats)):
+        assert st["status"] == 0, i
+        k1, c1, _ = ctx.solve_arrays(sigs[i], m.Rng(900 + i), opts[i])
+        assert np.array_equal(k, k1), i
+        assert np.array_equal(c.view(np.uint64), c1.view(np.uint64)), i
+    big_n = [i for i, sp in enumerate(specs) if sp.n == 1 << 24][:2]
+    big_s = sorted(range(256), key=lambda i: -specs[i].k.size)[:2]
+    picks = sorted(set(big_n + big_s + [0, 64, 128, 192]))
+    assert len(picks) >= 8
+    for i in picks:
+        sp = specs[i]
+        x = sigs[i].read().astype(np.complex128)
+        want, _ = port.demo1_run(x, sp.k.size, sp.sigma, 900 + i, min_bins=51,
+                                 window_delta=1e-5, max_stale_iter=5)
+        k, c = out[i]
+        assert k.tolist() == sorted(want), i
+        wk = np.array(sorted(want))
+        wc = np.array([want[v] for v in wk])
+        assert np.linalg.norm(c - wc) / np.linalg.norm(wc) < 1e-5, i
+    for sg in sigs:
+        sg.free()
+
+
+@pytest.mark.parametrize("prec", [m.FP64, m.FP32], ids=["fp64", "fp32"])
+def test_prime_n_headline_config(ctx, port, prec):
+    """The headline configuration (S = 1000, |c| log-uniform [1e-2, 1], 60 dB)
+    at N = kPrimes[22] = 4194301, the reference's own benchmark length: the
+    oracle's frequency set (FP64, the reference's Transform, same draws);
+    coefficients within 1e-9 (FP64) / 1e-5 (FP32) of the oracle's."""
+    from mpsft_gb300.signals import make_signal
+
+    n = 4194301
+    sg = make_signal(n, 1000, 22, magnitude="loguniform", mag_range=(1e-2, 1.0),
+                     snr_db=60.0)
+    want, _ = port.demo1_run(sg.x.astype(np.complex128), 1000, sg.sigma, 123537,
+                             min_bins=51, window_delta=1e-5, max_stale_iter=5)
+    sig = ctx.upload(sg.x)
+    k, c, st = ctx.solve_arrays(sig, m.Rng(123537), _opts(ctx, 1000, sg.sigma, prec))
+    sig.free()
+    assert st.status == 0
+    assert k.tolist() == sorted(want)
+    wk = np.array(sorted(want))
+    wc = np.array([want[v] for v in wk])
+    err = float(np.linalg.norm(c - wc) / np.linalg.norm(wc))
+    print(f"prime n: prec={prec} iterations={st.iterations} found={k.size} "
+          f"true={int(np.isin(k, sg.k).sum())} precision_err={err:.2e}")
+    assert err < (1e-9 if prec == m.FP64 else 1e-5), err
 
 
 def test_config5_stress(ctx, port):

@@ -15,7 +15,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = "/root/reference/src"
+REF_SRC = os.environ.get("MPSFT_REFERENCE_SRC", "/root/reference/src")
 TESTS = ["base_test", "binner_test", "freqid_test", "gen_test", "integer_test",
          "iterate_test", "sincos_test", "window_test"]
 

@@ -5,9 +5,11 @@ a caller-managed memory pool or a plugin host that forbids allocation after
 start-up: they pass their own device buffers for the samples and the bins, and
 the library works in a fixed scratch array compiled into it. These tests call it
 through the C ABI with device buffers owned by the test and compare its bins
-with those of mpsft_bin_in_time (which allocates its own work buffers), within
-the tolerances of the other binning tests, on two calls in a row (the second
-with other sizes, so stale scratch from the first would show).
+with those of mpsft_bin_in_time (which allocates its own work buffers) on two
+calls in a row (the second with other sizes, so stale scratch from the first
+would show). Both entry points run the same kernels on the same descriptor,
+window and twiddles, so the bins must be equal bit for bit: a tolerance would
+hide an offset or stride fault in the array's hand-made layout.
 
 This file is collected last on purpose: it runs after every other test.
 """
@@ -22,8 +24,6 @@ import cases
 import mpsft_gb300 as m
 
 pytestmark = pytest.mark.gpu
-
-TOL_BINS = {m.FP64: 1e-11, m.FP32: 1e-5}
 
 
 def _noalloc_fn(lib):
@@ -67,8 +67,8 @@ def test_noalloc_matches_allocating_entry_point(ctx, prec):
         x_dev = torch.from_numpy(x).to("cuda")
         got = _noalloc_bins(fn, x_dev, n, dtype, bins, bits, delta, a, b, c, q,
                             prec, stream)
-        err = np.abs(got - want).max() / np.abs(want).max()
-        assert err < TOL_BINS[prec], (n, bins, err)
+        assert np.array_equal(got, want), (
+            n, bins, np.abs(got - want).max() / np.abs(want).max())
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
@@ -82,3 +82,7 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
     rc = fn(x.data_ptr(), 1 << 16, m.C64, 101, 21, 1e-5, 3, 1, 1, 1, m.FP32,
             out.data_ptr(), None)
     assert rc == m.ERR_CAPACITY
+    # the lengths of mpsft_bin_in_time: prime or a power of two
+    rc = fn(x.data_ptr(), 60000, m.C64, 101, 2, 1e-5, 7, 1, 1, 1, m.FP32,
+            out.data_ptr(), None)
+    assert rc == m.ERR_UNSUPPORTED_N
