@@ -11,7 +11,13 @@
  *
  * Reference interfaces replaced (file:line in jiaweichiu/mpsft):
  *   mpsft_bin_in_time   BinInTime::Run         src/binner.h:30-41, src/binner.cc:394-521
+ *   mpsft_bin_in_time_wt  the same, windowed by the binner's own Window table
+ *                       (src/binner.h:30-38, src/window.h:27-32)
  *   mpsft_bin_in_freq   BinInFreq::Run         src/binner.h:123-133, src/binner.cc:565-591
+ *   mpsft_bin_in_freq_wf  the same, with Window::SampleInFreq's responses given
+ *                       (src/binner.cc:575-580, src/window.cc:77-81)
+ *   mpsft_iterate_draws Iterate on the caller's Transform and q draws
+ *                       (src/iterate.cc:92-104, src/integer.h:75-82)
  *   mpsft_mat_pencil    MatPencil              src/freqid.h:28, src/freqid.cc:27-48
  *   mpsft_iterate       Iterate                src/iterate.h:65, src/iterate.cc:80-176
  *   mpsft_solve         Demo1::Run             src/demo1.h:39, src/demo1.cc:36-59
@@ -147,6 +153,19 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
                       int32_t c, int32_t q, int precision, double *out,
                       int out_on_device);
 
+/* BinInTime::Run of a binner built from the reference's Window
+ * (src/binner.h:30-38: BinInTime(const Window &win, int32_t bits)): the
+ * window is the Window's own table, wt = Window::wt() (src/window.h:32), p =
+ * Window::p(), in its index order t = 0, 1..p2, -p2..-1; the window's delta
+ * (private to Window) is not needed. p must be an odd multiple of bins and the
+ * table even (wt[p - i] == wt[i]), as Window builds it. FP64 precisions bin
+ * with the table as given, FP32 with it rounded to FP32. Otherwise as
+ * mpsft_bin_in_time. */
+int mpsft_bin_in_time_wt(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
+                         int32_t bits, int32_t p, const double *wt, int32_t a,
+                         int32_t b, int32_t c, int32_t q, int precision,
+                         double *out, int out_on_device);
+
 /* ---- BinInTime::Run without device allocation --------------------------- */
 /* No counterpart in the reference. The same bins as mpsft_bin_in_time, for
  * callers that cannot call cudaMalloc (a caller-managed memory pool, a plugin
@@ -176,6 +195,19 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
                       double delta, int32_t a, int32_t b, int32_t c, int32_t q,
                       const int32_t *k0, const double *coef, int64_t m,
                       double *inout);
+
+/* BinInFreq::Run of a binner built from the reference's Window
+ * (src/binner.h:123-133): wf[i] is mode i's window response
+ * Window::SampleInFreq(xi_i) (src/window.cc:77-81) at xi_i =
+ * (bin_i + 1/2)/bins - k1_i/n, k1_i = (a k0[i] + b) mod n, bin_i =
+ * floor(k1_i bins / n) (src/binner.cc:571-575), evaluated by the caller's
+ * Window, so that no window delta is needed. Each mode's term is
+ * wf[i] coef_i e^{2 pi i (q k1_i + c k0[i])/n} (src/binner.cc:577-580), times
+ * the row factors. Otherwise as mpsft_bin_in_freq. */
+int mpsft_bin_in_freq_wf(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
+                         int32_t a, int32_t b, int32_t c, int32_t q,
+                         const int32_t *k0, const double *coef, const double *wf,
+                         int64_t m, double *inout);
 
 /* ---- coefficient estimation for a fixed frequency set, and its adjoint ---
  * No entry point of the reference corresponds: these expose, as a linear map
@@ -237,6 +269,19 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
                   const mpsft_iterate_options *opt, mpsft_rng *rng,
                   int32_t *mm_k, double *mm_c, int32_t *mm_size,
                   int32_t mm_cap, int32_t *found);
+
+/* mpsft_iterate with the draws made by the caller: the transform as the
+ * reference's Transform holds it (a, b, c, a_inv; src/integer.h:75-82, drawn
+ * by Transform(n), src/integer.cc:44-49) and q[t] for each of opt->trials
+ * trials (RandomInt32() % n, src/iterate.cc:102-104), all in [0, n). a_inv is
+ * used as given (k0 = a_inv (k1 - b) mod n, src/iterate.cc:169), as the
+ * reference does. This is the drop-in for Iterate driven by the reference's
+ * own global RNG. */
+int mpsft_iterate_draws(mpsft_ctx *ctx, const mpsft_signal *sig,
+                        const mpsft_iterate_options *opt, int32_t a, int32_t b,
+                        int32_t c, int32_t a_inv, const int32_t *q,
+                        int32_t *mm_k, double *mm_c, int32_t *mm_size,
+                        int32_t mm_cap, int32_t *found);
 
 /* ---- Demo1::Run ------------------------------------------------------------ */
 typedef struct {

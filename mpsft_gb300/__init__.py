@@ -144,6 +144,12 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_bin_in_time": (I, [P, P, I32, I32, D, I32, I32, I32, I32, I, P, I]),
         "mpsft_bin_in_freq": (I, [P, I32, I32, I32, D, I32, I32, I32, I32, P, P,
                                   I64, P]),
+        "mpsft_bin_in_time_wt": (I, [P, P, I32, I32, I32, P, I32, I32, I32, I32, I,
+                                     P, I]),
+        "mpsft_bin_in_freq_wf": (I, [P, I32, I32, I32, I32, I32, I32, I32, P, P, P,
+                                     I64, P]),
+        "mpsft_iterate_draws": (I, [P, P, ctypes.POINTER(IterateOptions), I32, I32,
+                                    I32, I32, P, P, P, P, I32, P]),
         "mpsft_mat_pencil": (I, [P, P, I64, P, P]),
         "mpsft_estimate": (I, [P, P, ctypes.POINTER(EstimateSetup), P, I64, P]),
         "mpsft_adjoint": (I, [P, I32, ctypes.POINTER(EstimateSetup), P, I64, P, P]),
@@ -373,6 +379,31 @@ class Context:
             self._h, sig._h, bins, bits, delta, a, b, c, q, precision, _ptr(out), 0))
         return out
 
+    def bin_in_time_wt(self, sig: "Signal", bins: int, bits: int, wt: np.ndarray,
+                       a: int, b: int, c: int, q: int,
+                       precision: int = FP32) -> np.ndarray:
+        """BinInTime::Run windowed by a Window's own table wt (p entries, the
+        reference's index order t = 0, 1..p2, -p2..-1)."""
+        wt = np.ascontiguousarray(wt, np.float64)
+        out = np.zeros((1 + 2 * bits, bins), np.complex128)
+        _check(self, self._lib.mpsft_bin_in_time_wt(
+            self._h, sig._h, bins, bits, wt.size, _ptr(wt), a, b, c, q, precision,
+            _ptr(out), 0))
+        return out
+
+    def bin_in_freq_wf(self, out: np.ndarray, n: int, bins: int, bits: int,
+                       a: int, b: int, c: int, q: int, k0: np.ndarray,
+                       coef: np.ndarray, wf: np.ndarray) -> np.ndarray:
+        """BinInFreq::Run with each mode's window response wf given."""
+        out = np.ascontiguousarray(out, np.complex128).copy()
+        k0 = np.ascontiguousarray(k0, np.int32)
+        coef = np.ascontiguousarray(coef, np.complex128)
+        wf = np.ascontiguousarray(wf, np.float64)
+        _check(self, self._lib.mpsft_bin_in_freq_wf(
+            self._h, n, bins, bits, a, b, c, q, _ptr(k0), _ptr(coef), _ptr(wf),
+            k0.size, _ptr(out)))
+        return out
+
     def bin_in_freq(self, out: np.ndarray, n: int, bins: int, bits: int,
                     delta: float, a: int, b: int, c: int, q: int,
                     k0: np.ndarray, coef: np.ndarray) -> np.ndarray:
@@ -445,6 +476,31 @@ class Context:
                                              cap, _ptr(found)))
         m = int(size[0])
         return bool(found[0]), {int(k[i]): complex(c[i]) for i in range(m)}
+
+    def iterate_draws(self, sig: "Signal", a: int, b: int, c: int, a_inv: int,
+                      q, bins: int, window_delta: float = 1e-6,
+                      bin_threshold: float = 0.0, window_threshold: float = 0.1,
+                      sv_threshold: float = 0.0, mm: dict | None = None,
+                      precision: int = FP32):
+        """Iterate on the caller's draws: transform (a, b, c, a_inv) and one q
+        per trial (trials = len(q))."""
+        mm = dict(mm or {})
+        cap = len(mm) + bins + 16
+        k = np.zeros(cap, np.int32)
+        cc = np.zeros(cap, np.complex128)
+        for i, (kk, v) in enumerate(mm.items()):
+            k[i] = kk
+            cc[i] = v
+        qq = np.ascontiguousarray(q, np.int32)
+        size = np.array([len(mm)], np.int32)
+        found = np.zeros(1, np.int32)
+        opt = IterateOptions(bins, window_delta, qq.size, bin_threshold,
+                             window_threshold, sv_threshold, precision, 0.0)
+        _check(self, self._lib.mpsft_iterate_draws(
+            self._h, sig._h, ctypes.byref(opt), a, b, c, a_inv, _ptr(qq), _ptr(k),
+            _ptr(cc), _ptr(size), cap, _ptr(found)))
+        m = int(size[0])
+        return bool(found[0]), {int(k[i]): complex(cc[i]) for i in range(m)}
 
     @staticmethod
     def solve_options(k: int, sigma: float, **kw) -> SolveOptions:

@@ -166,6 +166,9 @@ struct SigIter {
   int32_t tables_valid;
   // table cache slot (bins >> 1) this signal builds in this iteration, or -1
   int32_t win_slot;
+  // 1 when the table's coefficients already carry their window responses
+  // (wf * coef, from a caller's window), so that the mode terms use wf = 1
+  int32_t unit_wf;
   int32_t *esc_list;    // esc_cap bins
   uint32_t *esc_mask;   // per listed bin: bit s set = rows 2s+1, 2s+2 near
   int32_t esc_cap;
@@ -414,7 +417,8 @@ __device__ inline double WindowInFreq(const SigIter &it, double xi) {
 // src/binner.cc:565-591).
 __device__ inline void ModeTerms64(const SigIter &it, int s, int64_t k1, int bin) {
   const double xi = (double(bin) + 0.5) / double(it.bins) - double(k1) / double(it.n);
-  const double2 wc = cscale(it.tab_coef[s], WindowInFreq(it, xi));
+  const double2 wc =
+      it.unit_wf ? it.tab_coef[s] : cscale(it.tab_coef[s], WindowInFreq(it, xi));
   const int32_t key = it.tab_key[s];
   for (int t = 0; t < it.trials; ++t) {
     const int64_t ph = int64_t(it.q[t]) * k1 + int64_t(it.c) * key;

@@ -477,7 +477,12 @@ void RowPhase(int32_t b, int32_t q, int32_t n, double *re, double *im) {
 void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
               double delta, const Transform &tf, const int32_t *q,
               int32_t trials) {
-  const WinParams w = MakeWindow(bins, delta);
+  FillIter(it, sig, bins, bits, MakeWindow(bins, delta), tf, q, trials);
+}
+
+void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
+              const WinParams &w, const Transform &tf, const int32_t *q,
+              int32_t trials) {
   it->x = sig->d_x;
   it->n = int32_t(sig->n);
   it->bins = bins;
@@ -1900,10 +1905,84 @@ int mpsft_window_table(mpsft_ctx *ctx, int32_t n, int32_t bins, double delta,
   return MPSFT_OK;
 }
 
-int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
-                      int32_t bits, double delta, int32_t a, int32_t b,
-                      int32_t c, int32_t q, int precision, double *out,
-                      int out_on_device) {
+}  // extern "C"
+
+namespace {
+
+// A caller's window table (the reference's Window::wt(), src/window.h:32,
+// filled by src/window.cc:65-69): p entries for t = 0, 1..p2, -p2..-1, p an
+// odd multiple of bins, even in t (the kernels read it at |t|), finite.
+int CheckWindowTable(mpsft_ctx *ctx, int32_t bins, int32_t p, const double *wt,
+                     bool fp64) {
+  if (bins <= 0 || bins % 2 == 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "bins must be odd and positive");
+  }
+  if (p <= 0 || p % 2 == 0 || p % bins != 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "p must be an odd multiple of bins");
+  }
+  if (p / bins > kFoldLanes * kMaxFoldsPerLane) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "window too wide (p/bins > 80)");
+  }
+  const int32_t p2 = (p - 1) / 2;
+  for (int32_t i = 0; i <= p2; ++i) {
+    if (!std::isfinite(wt[i])) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "window table must be finite");
+    }
+    if (i > 0 && wt[p - i] != wt[i]) {
+      return Fail(ctx, MPSFT_ERR_INVALID,
+                  "window table must be even (wt[p - i] == wt[i])");
+    }
+  }
+  const int m = 1 << FFTLog2(bins);
+  if (m > (fp64 ? kMaxFFT64 : kMaxFFT)) {
+    return Fail(ctx, MPSFT_ERR_INVALID,
+                fp64 ? "bins too large for the FP64 path (max 4096)"
+                     : "bins too large (max 8192)");
+  }
+  return MPSFT_OK;
+}
+
+// The window scalars a binning call needs from a caller's table: the support
+// and the width (wt[0] = 1 / (2 bins), src/window.cc:65).
+WinParams TableWindow(int32_t bins, int32_t p, const double *wt) {
+  WinParams w;
+  w.p = p;
+  w.p2 = (p - 1) / 2;
+  w.folds = p / bins;
+  w.width = wt[0];
+  return w;
+}
+
+// Copies the t >= 0 half of a caller's window table into it's device tables:
+// FP64 as given, FP32 rounded, float-float (hi, lo) split; waits for the
+// copies (pageable staging).
+int UploadWindowTable(mpsft_ctx *ctx, const SigIter &it, const double *wt,
+                      cudaStream_t st) {
+  const size_t e = size_t(it.p2) + 1;
+  std::vector<float> w32(e);
+  std::vector<float2> wff(e);
+  for (size_t i = 0; i < e; ++i) {
+    const float hi = float(wt[i]);
+    w32[i] = hi;
+    wff[i] = make_float2(hi, float(wt[i] - double(hi)));
+  }
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(it.wt64, wt, sizeof(double) * e,
+                                  cudaMemcpyHostToDevice, st));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(it.wt32, w32.data(), sizeof(float) * e,
+                                  cudaMemcpyHostToDevice, st));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(it.wtff, wff.data(), sizeof(float2) * e,
+                                  cudaMemcpyHostToDevice, st));
+  MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
+  return MPSFT_OK;
+}
+
+// BinInTime::Run over a window evaluated on the device from delta (wt null)
+// or given by the caller as the reference's table (wt: p entries, index order
+// t = 0, 1..p2, -p2..-1).
+int BinInTimeImpl(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
+                  int32_t bits, double delta, int32_t p, const double *wt,
+                  int32_t a, int32_t b, int32_t c, int32_t q, int precision,
+                  double *out, int out_on_device) {
   if (!ctx || !out) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
   int rc = CheckSignal(ctx, sig);
   if (rc) return rc;
@@ -1911,8 +1990,16 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   if (precision < MPSFT_PREC_FP32 || precision > MPSFT_PREC_FP64_DIRECT) {
     return Fail(ctx, MPSFT_ERR_INVALID, "unknown precision");
   }
-  rc = CheckWindow(ctx, bins, delta, fp64);
-  if (rc) return rc;
+  WinParams w;
+  if (wt) {
+    rc = CheckWindowTable(ctx, bins, p, wt, fp64);
+    if (rc) return rc;
+    w = TableWindow(bins, p, wt);
+  } else {
+    rc = CheckWindow(ctx, bins, delta, fp64);
+    if (rc) return rc;
+    w = MakeWindow(bins, delta);
+  }
   if (bits < 0 || bits > kMaxBits) {
     return Fail(ctx, MPSFT_ERR_INVALID, "bits must be in [0, 31]");
   }
@@ -1926,7 +2013,7 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   s.bins_cap = bins;
   s.rows_cap = 1 + 2 * bits;
   s.trials = 1;
-  s.p2_cap = MakeWindow(bins, delta).p2;
+  s.p2_cap = w.p2;
   s.m_cap = 1 << FFTLog2(bins);
   s.tab_cap = 64;
   s.fp64 = fp64;
@@ -1948,8 +2035,18 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   std::memset(&it, 0, sizeof(it));
   CarveSignal(cv, s, &it, &ctl);
   const Transform tf{a, b, c, InverseMod(a, n)};
-  FillIter(&it, sig, bins, bits, delta, tf, &q, 1);
+  FillIter(&it, sig, bins, bits, w, tf, &q, 1);
   cudaStream_t st = ctx->stream;
+  // the window tables: evaluated on the device, or the caller's uploaded
+  auto window = [&](bool all64) -> int {
+    if (wt) return UploadWindowTable(ctx, it, wt, st);
+    if (all64) {
+      LaunchWindow(d_it, 1, it.p2, st);
+    } else {
+      LaunchWindow32(d_it, 1, it.p2, st);
+    }
+    return MPSFT_OK;
+  };
   if (direct) {
     // every bin is a listed bin of the FP64 re-binning kernel
     it.esc_part = cv.take<double2>(direct_cells);
@@ -1970,7 +2067,8 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
                                     cudaMemcpyHostToDevice, st));
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                     st));
-    LaunchWindow(d_it, 1, it.p2, st);
+    rc = window(true);
+    if (rc) return rc;
     LaunchRebin(d_it, 1, bins, sig->dtype == MPSFT_C128, true, st);
     MPSFT_CUDA(ctx, cudaGetLastError());
     std::vector<double2> sum(direct_cells / kRebinChunks);
@@ -1991,12 +2089,10 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   }
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   ctx->stream));
-  // the window the solves use: FP64 for the FP64 path, FP32-evaluated for FP32
-  if (fp64) {
-    LaunchWindow(d_it, 1, it.p2, st);
-  } else {
-    LaunchWindow32(d_it, 1, it.p2, st);
-  }
+  // the window the solves use: FP64 for the FP64 path, FP32-evaluated for
+  // FP32 (a caller's table: as given, and rounded to FP32)
+  rc = window(fp64);
+  if (rc) return rc;
   LaunchBluesteinSetup(d_it, 1, it.fft_m, fp64, ctx->tw32, ctx->tw64, st);
   BinTimer timer{ctx};
   rc = timer.Begin();
@@ -2026,17 +2122,32 @@ int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   return MPSFT_OK;
 }
 
-int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
-                      double delta, int32_t a, int32_t b, int32_t c, int32_t q,
-                      const int32_t *k0, const double *coef, int64_t m,
-                      double *inout) {
+// BinInFreq::Run: subtracts the modes' window responses from a host bin
+// matrix. wf null: responses evaluated on the device from delta; otherwise
+// wf[i] is mode i's response (the caller's Window::SampleInFreq), folded into
+// its coefficient here as the reference's wf * coef.
+int BinInFreqImpl(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
+                  double delta, int32_t a, int32_t b, int32_t c, int32_t q,
+                  const int32_t *k0, const double *coef, const double *wf,
+                  int64_t m, double *inout) {
   if (!ctx || !inout || (m > 0 && (!k0 || !coef))) {
     return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
   }
   int rc = CheckN(ctx, n);
   if (rc) return rc;
-  rc = CheckWindow(ctx, bins, delta, false);
-  if (rc) return rc;
+  if (wf) {
+    if (bins <= 0 || bins % 2 == 0) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "bins must be odd and positive");
+    }
+    for (int64_t i = 0; i < m; ++i) {
+      if (!std::isfinite(wf[i])) {
+        return Fail(ctx, MPSFT_ERR_INVALID, "window responses must be finite");
+      }
+    }
+  } else {
+    rc = CheckWindow(ctx, bins, delta, false);
+    if (rc) return rc;
+  }
   if (bits < 0 || bits > kMaxBits || m < 0) {
     return Fail(ctx, MPSFT_ERR_INVALID, "bad bits or mode count");
   }
@@ -2067,8 +2178,11 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   const Transform tf{a, b, c, 0};
   mpsft_signal fake;
   fake.n = n;
-  FillIter(&it, &fake, bins, bits, delta, tf, &q, 1);
+  // the window's scalars serve only the device's responses
+  FillIter(&it, &fake, bins, bits, wf ? WinParams{} : MakeWindow(bins, delta),
+           tf, &q, 1);
   it.x = nullptr;
+  it.unit_wf = wf ? 1 : 0;
   cudaStream_t st = ctx->stream;
   MPSFT_CUDA(ctx, cudaMemcpyAsync(d_it, &it, sizeof(it), cudaMemcpyHostToDevice,
                                   st));
@@ -2078,9 +2192,22 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   if (m > 0) {
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_k0, k0, sizeof(int32_t) * m,
                                     cudaMemcpyHostToDevice, st));
-    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_coef, coef, sizeof(double2) * m,
+    std::vector<double> wc;
+    const double *src = coef;
+    if (wf) {
+      // wf * coef, the reference's first product (src/binner.cc:580)
+      wc.resize(2 * size_t(m));
+      for (int64_t i = 0; i < m; ++i) {
+        wc[2 * i] = coef[2 * i] * wf[i];
+        wc[2 * i + 1] = coef[2 * i + 1] * wf[i];
+      }
+      src = wc.data();
+    }
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(d_coef, src, sizeof(double2) * m,
                                     cudaMemcpyHostToDevice, st));
     LaunchTableInsert(d_it, d_k0, d_coef, m, st);
+    // the pageable source must outlive the copy
+    if (wf) MPSFT_CUDA(ctx, cudaStreamSynchronize(st));
   }
   const size_t row_bytes = sizeof(double2) * size_t(bins);
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(it.ubuf, sizeof(double2) * it.bins_cap,
@@ -2101,6 +2228,45 @@ int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
     return Fail(ctx, MPSFT_ERR_CAPACITY, "mode table full");
   }
   return MPSFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpsft_bin_in_time(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
+                      int32_t bits, double delta, int32_t a, int32_t b,
+                      int32_t c, int32_t q, int precision, double *out,
+                      int out_on_device) {
+  return BinInTimeImpl(ctx, sig, bins, bits, delta, 0, nullptr, a, b, c, q,
+                       precision, out, out_on_device);
+}
+
+int mpsft_bin_in_time_wt(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
+                         int32_t bits, int32_t p, const double *wt, int32_t a,
+                         int32_t b, int32_t c, int32_t q, int precision,
+                         double *out, int out_on_device) {
+  if (!wt) return Fail(ctx, MPSFT_ERR_INVALID, "null window table");
+  return BinInTimeImpl(ctx, sig, bins, bits, 0.0, p, wt, a, b, c, q, precision,
+                       out, out_on_device);
+}
+
+int mpsft_bin_in_freq(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
+                      double delta, int32_t a, int32_t b, int32_t c, int32_t q,
+                      const int32_t *k0, const double *coef, int64_t m,
+                      double *inout) {
+  return BinInFreqImpl(ctx, n, bins, bits, delta, a, b, c, q, k0, coef, nullptr,
+                       m, inout);
+}
+
+int mpsft_bin_in_freq_wf(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
+                         int32_t a, int32_t b, int32_t c, int32_t q,
+                         const int32_t *k0, const double *coef, const double *wf,
+                         int64_t m, double *inout) {
+  if (m > 0 && !wf) return Fail(ctx, MPSFT_ERR_INVALID, "null window responses");
+  static const double kNone = 0.0;
+  return BinInFreqImpl(ctx, n, bins, bits, 0.0, a, b, c, q, k0, coef,
+                       wf ? wf : &kNone, m, inout);
 }
 
 }  // extern "C"
@@ -2276,11 +2442,19 @@ int mpsft_mat_pencil(mpsft_ctx *ctx, const double *u3, int64_t count,
   return MPSFT_OK;
 }
 
-int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
-                  const mpsft_iterate_options *opt, mpsft_rng *rng,
-                  int32_t *mm_k, double *mm_c, int32_t *mm_size,
-                  int32_t mm_cap, int32_t *found) {
-  if (!ctx || !opt || !rng || !mm_size || !found || (mm_cap > 0 && (!mm_k || !mm_c))) {
+}  // extern "C"
+
+namespace {
+
+// One Iterate call for a transform and q's drawn by the caller (draw set:
+// the draws come from rng after the argument checks, in the reference's
+// order).
+int IterateImpl(mpsft_ctx *ctx, const mpsft_signal *sig,
+                const mpsft_iterate_options *opt, mpsft_rng *rng,
+                const Transform *tf_in, const int32_t *q_in, int32_t *mm_k,
+                double *mm_c, int32_t *mm_size, int32_t mm_cap, int32_t *found) {
+  if (!ctx || !opt || (!rng && !(tf_in && q_in)) || !mm_size || !found ||
+      (mm_cap > 0 && (!mm_k || !mm_c))) {
     return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
   }
   int rc = CheckSignal(ctx, sig);
@@ -2331,9 +2505,15 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
   double *d_energy = cv.take<double>(kEnergyStride);
   const void **d_xs = cv.take<const void *>(1);
   int64_t *d_ns = cv.take<int64_t>(1);
-  const Transform tf = DrawTransform(rng, n);
+  Transform tf;
   int32_t q[kMaxTrials];
-  for (int t = 0; t < opt->trials; ++t) q[t] = rng->Draw() % n;
+  if (tf_in) {
+    tf = *tf_in;
+    for (int t = 0; t < opt->trials; ++t) q[t] = q_in[t];
+  } else {
+    tf = DrawTransform(rng, n);
+    for (int t = 0; t < opt->trials; ++t) q[t] = rng->Draw() % n;
+  }
   FillIter(&it, sig, bins, bits, opt->window_delta, tf, q, opt->trials);
   it.bin_thr = opt->bin_threshold;
   it.sv_thr = opt->sv_threshold;
@@ -2397,6 +2577,42 @@ int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
   *mm_size = int32_t(modes.size());
   *found = h_ctl[0] ? 1 : 0;
   return MPSFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpsft_iterate(mpsft_ctx *ctx, const mpsft_signal *sig,
+                  const mpsft_iterate_options *opt, mpsft_rng *rng,
+                  int32_t *mm_k, double *mm_c, int32_t *mm_size,
+                  int32_t mm_cap, int32_t *found) {
+  if (!rng) return Fail(ctx, MPSFT_ERR_INVALID, "null rng");
+  return IterateImpl(ctx, sig, opt, rng, nullptr, nullptr, mm_k, mm_c, mm_size,
+                     mm_cap, found);
+}
+
+int mpsft_iterate_draws(mpsft_ctx *ctx, const mpsft_signal *sig,
+                        const mpsft_iterate_options *opt, int32_t a, int32_t b,
+                        int32_t c, int32_t a_inv, const int32_t *q,
+                        int32_t *mm_k, double *mm_c, int32_t *mm_size,
+                        int32_t mm_cap, int32_t *found) {
+  if (!sig || !q) return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  const int64_t n = sig->n;
+  if (a < 0 || a >= n || b < 0 || b >= n || c < 0 || c >= n || a_inv < 0 ||
+      a_inv >= n) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "transform values must be in [0, n)");
+  }
+  if (opt && opt->trials >= 1 && opt->trials <= kMaxTrials) {
+    for (int t = 0; t < opt->trials; ++t) {
+      if (q[t] < 0 || q[t] >= n) {
+        return Fail(ctx, MPSFT_ERR_INVALID, "q must be in [0, n)");
+      }
+    }
+  }
+  const Transform tf{a, b, c, a_inv};
+  return IterateImpl(ctx, sig, opt, nullptr, &tf, q, mm_k, mm_c, mm_size,
+                     mm_cap, found);
 }
 
 int mpsft_solve(mpsft_ctx *ctx, const mpsft_signal *sig,

@@ -131,6 +131,10 @@ void RowPhase(int32_t b, int32_t q, int32_t n, double *re, double *im);
 void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
               double delta, const Transform &tf, const int32_t *q,
               int32_t trials);
+// The same with the window's scalars given.
+void FillIter(SigIter *it, const mpsft_signal *sig, int32_t bins, int32_t bits,
+              const WinParams &w, const Transform &tf, const int32_t *q,
+              int32_t trials);
 // MPSFT_OK when n is a length the solver supports (prime or a power of two in
 // [3, 2^31 - 1]); otherwise records why.
 int CtxCheckN(mpsft_ctx *ctx, int64_t n);
