@@ -80,9 +80,14 @@ typedef struct {
   int32_t signals;    /* signals the launch binned                           */
   int32_t max_bins;   /* largest and smallest bins among them                */
   int32_t min_bins;
-  int64_t gathers;    /* samples gathered                                    */
-  int64_t bytes;      /* algorithmic bytes: 32 per gathered sample (one      */
-                      /* sector) + the window table + the fold output        */
+  int32_t precision;  /* MPSFT_PREC_FP32 or MPSFT_PREC_FP64 (the FP64 kernels */
+                      /* that an FP32 call runs for the signals its          */
+                      /* precision policy sends there)                       */
+  int64_t gathers;    /* samples the launch gathered (the FP32 kernels read  */
+                      /* each sample of overlapping row windows once)        */
+  int64_t bytes;      /* algorithmic bytes: 32 (one sector) per sample of    */
+                      /* every row's window, as the reference reads them     */
+                      /* (p per row), + the window table + the fold output   */
   double ms;          /* duration from CUDA events around the launch         */
 } mpsft_bin_launch;
 /* The binning launches of the context's last call made with profiling on, in
@@ -307,7 +312,8 @@ typedef struct {
   int32_t iterations;     /* Iterate calls made                              */
   int32_t found;          /* distinct modes in the result                    */
   int64_t gathers;        /* samples gathered by the binning kernel          */
-  int64_t bin_bytes;      /* algorithmic bytes of the binning launches       */
+  int64_t bin_bytes;      /* algorithmic bytes of the binning launches (32   */
+                          /* per sample of every row's window, p per row)    */
   int32_t bin_launches;   /* binning launches timed (profiling on)           */
   double bin_ms;          /* summed binning-kernel time (profiling on)       */
   int32_t escalated;      /* FP32 near-tie escalations to FP64 (bins)        */

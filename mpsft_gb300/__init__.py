@@ -84,6 +84,7 @@ class BinLaunch(ctypes.Structure):
     """One timed binning launch (mpsft_bin_launch)."""
     _fields_ = [("iteration", ctypes.c_int32), ("signals", ctypes.c_int32),
                 ("max_bins", ctypes.c_int32), ("min_bins", ctypes.c_int32),
+                ("precision", ctypes.c_int32),
                 ("gathers", ctypes.c_int64), ("bytes", ctypes.c_int64),
                 ("ms", ctypes.c_double)]
 

@@ -489,6 +489,53 @@ __device__ inline bool RedoFP64(const SigIter &it) {
   return it.force_fp64 || *(volatile int32_t *)&it.flags[2] > it.esc_cap;
 }
 
+// ---- the FP32 binning's row cluster -------------------------------------
+// Row r's window covers u = off_r + t, |t| <= p2, of the permuted, modulated
+// samples y_u = x[a (q + u) + c] e^{2 pi i (b u / n - u / (2 bins))}, with
+// off_r = m bins, m in {0, +-1, +-2, ..., +-2^(bits-1)}. Row 0 and the pair
+// groups g = 1..ClusterGroups (m = +-2^(g-1)) have overlapping windows (that
+// of m = 2^(g-1) overlaps that of 2^(g-2) while 2^(g-2) <= folds - 1), so
+// they are binned together from the union of their windows: each sample of
+// the union is gathered once and serves every row whose window covers it.
+// The span of the union is folds + 2 Mc bins-steps per bin (Mc the largest
+// m of the cluster), kept at most kMaxClusterSpan (shared-memory tile).
+constexpr int kMaxClusterSpan = 96;
+__host__ __device__ inline int ClusterGroups(int folds, int bits) {
+  int s = 0;
+  while (s < bits) {
+    const int g = s + 1;
+    if (g >= 2 && (1 << (g - 2)) > folds - 1) break;
+    if (folds + 2 * (1 << (g - 1)) > kMaxClusterSpan) break;
+    ++s;
+  }
+  return s;
+}
+__host__ __device__ inline int ClusterSpan(int folds, int bits) {
+  const int sc = ClusterGroups(folds, bits);
+  return folds + (sc > 0 ? 2 << (sc - 1) : 0);
+}
+
+// Samples the binning gathers in one iteration: FP32 path, the cluster's
+// union (bins * span per trial) plus both rows of every other pair group
+// (2 p each); FP64 kernels, every row's p samples.
+__host__ __device__ inline int64_t BinGathers(const SigIter &it, bool fp64) {
+  if (fp64) return int64_t(it.trials) * it.p * it.rows;
+  const int sc = ClusterGroups(it.folds, it.bits);
+  return int64_t(it.trials) *
+         (int64_t(it.bins) * ClusterSpan(it.folds, it.bits) +
+          2 * int64_t(it.bits - sc) * it.p);
+}
+
+// Algorithmic bytes of a binning launch for one signal, by the reference's
+// gather count (BinInTime reads p samples per row, src/binner.cc:394-507):
+// one 32-byte sector per sample of every row's window, the window table and
+// the fold output. (The FP32 kernels gather fewer samples, BinGathers.)
+__host__ __device__ inline int64_t BinBytesOf(const SigIter &it, bool fp64) {
+  return 32 * int64_t(it.trials) * it.p * it.rows +
+         int64_t(fp64 ? 8 : 4) * (it.p2 + 1) +
+         int64_t(it.trials) * (fp64 ? 16 : 8) * it.rows * it.bins;
+}
+
 // Shared-memory keys of k_bucket: half the table (a power of two). The host
 // keeps tables at or below kMaxTableCap so that this fits in shared memory
 // and slots fit the 20 bits of the sort key.

@@ -543,9 +543,13 @@ int CheckWindow(mpsft_ctx *ctx, int32_t bins, double delta, bool fp64) {
 struct BinTimer {
   mpsft_ctx *ctx;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> used;
+  // per timed launch: 0 = the iteration's binning, 1 = its FP64 redo (the
+  // signals an FP32 call runs on the FP64 kernels)
+  std::vector<int> tags;
   size_t next = 0;
-  int Begin() {
+  int Begin(int tag = 0) {
     if (!ctx->profiling) return MPSFT_OK;
+    tags.push_back(tag);
     while (ctx->events.size() < 2 * (next + 1)) {
       cudaEvent_t e;
       MPSFT_CUDA(ctx, cudaEventCreate(&e));
@@ -572,11 +576,7 @@ struct BinTimer {
   }
 };
 
-int64_t BinBytes(const SigIter &it, bool fp64) {
-  const int64_t g = int64_t(it.trials) * it.p * it.rows;
-  return 32 * g + int64_t(fp64 ? 8 : 4) * (it.p2 + 1) +
-         int64_t(it.trials) * (fp64 ? 16 : 8) * it.rows * it.bins;
-}
+int64_t BinBytes(const SigIter &it, bool fp64) { return BinBytesOf(it, fp64); }
 
 // Launch sequence of one iteration for nsig signals whose SigIter array is
 // already on the device.
@@ -712,8 +712,17 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     if (redo) {
       LaunchModePrep(d_its, nsig, mx.cap, s, true);
       LaunchBluesteinSetup(d_its, nsig, mx.m, true, ctx->tw32, ctx->tw64, s, true);
+      if (timer && ctx->profiling) LaunchDelay(20000, s);
+      if (timer) {
+        int rc = timer->Begin(1);
+        if (rc) return rc;
+      }
       LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, true, s,
                     true);
+      if (timer) {
+        int rc = timer->End();
+        if (rc) return rc;
+      }
       LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, true, ctx->tw32,
                    ctx->tw64, s, true);
       LaunchDecide(d_its, nsig, mx.bins, mx.trials, false, false, s, true);
@@ -1373,10 +1382,15 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   int active = host_loop ? nsig : 0;
   if (ctx->profiling) ctx->bin_launches.clear();
+  // per iteration: the binning launch's signals, and those of its FP64 redo
+  std::vector<std::pair<mpsft_bin_launch, mpsft_bin_launch>> iter_recs;
   while (active > 0) {
-    mpsft_bin_launch rec{};
-    rec.iteration = int32_t(ctx->bin_launches.size());
-    rec.min_bins = INT32_MAX;
+    mpsft_bin_launch rec[2] = {};
+    for (int k = 0; k < 2; ++k) {
+      rec[k].iteration = int32_t(iter_recs.size());
+      rec[k].min_bins = INT32_MAX;
+      rec[k].precision = (fp64 || k == 1) ? MPSFT_PREC_FP64 : MPSFT_PREC_FP32;
+    }
     for (int i = 0; i < nsig; ++i) {
       SigIter &it = its[i];
       if (run[i].done) {
@@ -1402,15 +1416,16 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       // (a forced FP64 iteration leaves the FP32 tables unbuilt)
       it.tables_valid = (run[i].last_bins == bins && !it.force_fp64) ? 1 : 0;
       run[i].last_bins = it.force_fp64 ? -1 : bins;
-      run[i].gathers += int64_t(it.trials) * it.p * it.rows;
+      run[i].gathers += BinGathers(it, fp64 || it.force_fp64);
       run[i].bin_bytes += BinBytes(it, fp64 || it.force_fp64);
-      rec.signals += 1;
-      rec.max_bins = std::max(rec.max_bins, bins);
-      rec.min_bins = std::min(rec.min_bins, bins);
-      rec.gathers += int64_t(it.trials) * it.p * it.rows;
-      rec.bytes += BinBytes(it, fp64 || it.force_fp64);
+      mpsft_bin_launch &r = rec[it.force_fp64 ? 1 : 0];
+      r.signals += 1;
+      r.max_bins = std::max(r.max_bins, bins);
+      r.min_bins = std::min(r.min_bins, bins);
+      r.gathers += BinGathers(it, fp64 || it.force_fp64);
+      r.bytes += BinBytes(it, fp64 || it.force_fp64);
     }
-    if (ctx->profiling) ctx->bin_launches.push_back(rec);
+    if (ctx->profiling) iter_recs.emplace_back(rec[0], rec[1]);
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_its, its.data(), sizeof(SigIter) * nsig,
                                     cudaMemcpyHostToDevice, ctx->stream));
     for (int i = 0; i < nsig; ++i) {
@@ -1459,11 +1474,21 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   int first_err = MPSFT_OK;
   const double bin_ms = timer.TotalMs();
   if (ctx->profiling) {
+    // timed launches in order: each iteration's binning (tag 0), then its
+    // FP64 redo when it has one (tag 1); launches that binned no signal
+    // (every signal on the other kind of kernel) are left out
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (size_t j = 0; j < ctx->bin_launches.size() && j < timer.used.size(); ++j) {
+    size_t k = 0;
+    for (size_t j = 0; j < timer.used.size(); ++j) {
+      const bool redo = timer.tags[j] == 1;
+      if (!redo) ++k;
+      if (k == 0 || k > iter_recs.size()) break;
+      mpsft_bin_launch r = redo ? iter_recs[k - 1].second : iter_recs[k - 1].first;
+      if (r.signals == 0) continue;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, timer.used[j].first, timer.used[j].second);
-      ctx->bin_launches[j].ms = ms;
+      r.ms = ms;
+      ctx->bin_launches.push_back(r);
     }
   }
   // the call's own kernels outside the loop: table clearing, phase tables,
@@ -2114,7 +2139,8 @@ int BinInTimeImpl(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
     mpsft_bin_launch rec{};
     rec.signals = 1;
     rec.max_bins = rec.min_bins = bins;
-    rec.gathers = int64_t(it.p) * it.rows;
+    rec.precision = fp64 ? MPSFT_PREC_FP64 : MPSFT_PREC_FP32;
+    rec.gathers = BinGathers(it, fp64);
     rec.bytes = BinBytes(it, fp64);
     rec.ms = timer.TotalMs();
     ctx->bin_launches.assign(1, rec);

@@ -90,7 +90,131 @@ __device__ inline uint32_t StepDown(uint32_t j, uint32_t d, uint32_t n) {
   return j >= d ? j - d : j + (n - d);
 }
 
-// FP32 fold: one CTA per (64 bins, row group, trial, signal); kFoldSplit
+// ---- FP32 fold of the row cluster (row 0 and pair groups 1..sc) --------
+// For bin beta, the cluster's union is u = beta + k B for the span
+// k = -h - Mc .. h + Mc (h = (folds - 1)/2, Mc = 2^(sc-1)): J = folds + 2 Mc
+// samples y_u = x[a (q + u) + c] e^{2 pi i (b u / n - u / (2B))}. Row m B
+// (m = 0, +-1, +-2, ..., +-Mc) folds
+//   F_m[beta] = eps_m sum_{i < folds} y_{beta + (i - h + m) B} wt(beta + (i - h) B)
+// (eps_m = -1 for m = +-1: the row's own phase -t/(2B) differs from -u/(2B)
+// by m/2 turns), i.e. a J-sample correlation with the window. The mirror bin
+// B - beta takes the samples at -u: y_{-u} = x[a (q - u) + c] conj(phase(u)),
+// so one phase serves both (the reference's symmetry of V1/V4), and its
+// window runs backwards.
+//
+// One warp per base bin beta <= (B - 1)/2: its lanes gather the span and the
+// mirrored span into the warp's shared slice (J <= kMaxClusterSpan samples
+// each), then lane r < 16 folds row r of beta and lane 16 + r row r of the
+// mirror bin, the window weights broadcast from the lanes that loaded them.
+// The cluster takes the CTAs of row groups 0..sc of the launch grid (their
+// work would otherwise overlap), so every row of a signal is binned in the
+// same launch and a sample's sector is read from DRAM once for all rows.
+// The shared slices are small (12 KiB per CTA): random gathers need most of
+// the L1 for their misses in flight (a 48 KiB tile per CTA made the binning
+// 1.4x slower on GB300).
+constexpr int kWarpsPerCta = 8;
+constexpr int kSpanSlots = (kMaxClusterSpan + 31) / 32;  // span samples per lane
+constexpr int kMirrorOff = kMaxClusterSpan + 8;  // padded: other shared banks
+
+__device__ inline int ClusterRowOffset(int r) {
+  // row r -> m: 0, then +2^s (r = 2s + 1), -2^s (r = 2s + 2)
+  if (r == 0) return 0;
+  return (r & 1) ? (1 << ((r - 1) >> 1)) : -(1 << ((r >> 1) - 1));
+}
+
+template <typename TX>
+__device__ void FoldClusterWarp(const SigIter &it, int tr, int beta, int sc,
+                                float2 *ys) {
+  const int lane = threadIdx.x & 31;
+  const int B = it.bins, f = it.folds;
+  const int Mc = sc > 0 ? (1 << (sc - 1)) : 0;
+  const int J = f + 2 * Mc;
+  const int h = (f - 1) >> 1;
+  const uint32_t n = uint32_t(it.n);
+  const ModN mod{n, it.n_inv};
+  const int64_t q = it.q[tr];
+  const int64_t a = it.a, c = it.c;
+  const uint64_t phs = it.phi_b - it.psi;  // b/n - 1/(2B) turns
+  const bool mirror = beta != 0;
+  const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
+  // gather: lane l takes span positions l, l + 32, ...; all loads first
+  TX x1[kSpanSlots], x2[kSpanSlots];
+  uint32_t p32[kSpanSlots];
+#pragma unroll
+  for (int s = 0; s < kSpanSlots; ++s) {
+    const int j = lane + 32 * s;
+    if (j < J) {
+      const int64_t u = beta + int64_t(j - h - Mc) * B;
+      x1[s] = __ldg(&x[mod(a * mod(q + u) + c)]);
+      if (mirror) x2[s] = __ldg(&x[mod(a * mod(q - u) + c)]);
+      p32[s] = uint32_t((phs * uint64_t(u) + (uint64_t(1) << 31)) >> 32);
+    }
+  }
+  // window weights W[i] = wt(beta + (i - h) B), lane l holding i = l + 32 s
+  float wreg[kSpanSlots];
+#pragma unroll
+  for (int s = 0; s < kSpanSlots; ++s) {
+    const int i = lane + 32 * s;
+    wreg[s] = 0.f;
+    if (i < f) {
+      const int64_t t = int64_t(beta) + int64_t(i - h) * B;
+      wreg[s] = __ldg(&it.wt32[t < 0 ? -t : t]);
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < kSpanSlots; ++s) {
+    const int j = lane + 32 * s;
+    if (j < J) {
+      const float phi = float(int32_t(p32[s])) * 2.3283064365386963e-10f;
+      float sn, cs;
+      sincospif(2.0f * phi, &sn, &cs);
+      const float2 v1 = to_f2(x1[s]);
+      ys[j] = make_float2(v1.x * cs - v1.y * sn, v1.x * sn + v1.y * cs);
+      if (mirror) {
+        const float2 v2 = to_f2(x2[s]);
+        ys[kMirrorOff + J - 1 - j] =
+            make_float2(v2.x * cs + v2.y * sn, v2.y * cs - v2.x * sn);
+      }
+    }
+  }
+  __syncwarp();
+  // fold: lane r < 16 row r of beta, lane 16 + r row r of B - beta
+  const int sc2 = 1 + 2 * sc;
+  const bool mir = lane >= 16;
+  const int r = lane & 15;
+  const bool live = r < sc2 && (!mir || mirror);
+  const float2 *yb = ys + (mir ? kMirrorOff : 0) + Mc + (live ? ClusterRowOffset(r) : 0);
+  CompF ar, ai;
+  for (int i = 0; i < f; ++i) {
+    // W[i] for the bin, W[f - 1 - i] for its mirror (uniform slot indices)
+    const int i2 = f - 1 - i;
+    float w1 = wreg[0], w2 = wreg[0];
+#pragma unroll
+    for (int s = 1; s < kSpanSlots; ++s) {
+      if ((i >> 5) == s) w1 = wreg[s];
+      if ((i2 >> 5) == s) w2 = wreg[s];
+    }
+    w1 = __shfl_sync(0xffffffffu, w1, i & 31);
+    w2 = __shfl_sync(0xffffffffu, w2, i2 & 31);
+    if (live) {
+      const float w = mir ? w2 : w1;
+      const float2 yv = yb[i];
+      ar.add(yv.x * w);
+      ai.add(yv.y * w);
+    }
+  }
+  if (live) {
+    const float e = (r == 1 || r == 2) ? -1.f : 1.f;
+    float2 *fold = reinterpret_cast<float2 *>(it.fold);
+    const int bin = mir ? B - beta : beta;
+    fold[(size_t(tr) * it.rows + r) * it.bins_cap + bin] =
+        make_float2(e * (ar.s + ar.c), e * (ai.s + ai.c));
+  }
+  __syncwarp();  // the slice is reused by the warp's next bin
+}
+
+// FP32 fold of the pair groups beyond the cluster: one CTA per (64 bins, row
+// group, trial, signal); kFoldSplit
 // threads share a bin and take every kFoldSplit-th fold, kFoldBatch folds of
 // both rows in flight at a time. Setup without divisions: indices by Barrett
 // reduction (or a mask), the phase m/n - t/(2B) as a 64-bit fixed-point
@@ -107,10 +231,24 @@ __global__ void __launch_bounds__(256, 4)
   const SigIter &it = its[blockIdx.z];
   if (!it.active || it.force_fp64) return;
   const int B = it.bins;
-  if (int(blockIdx.x) * kFoldBins >= B) return;
   const int g = blockIdx.y % gmax;
   const int tr = blockIdx.y / gmax;
   if (tr >= it.trials || g > it.bits) return;
+  const int sc = ClusterGroups(it.folds, it.bits);
+  if (g <= sc) {
+    // the row cluster on the CTAs of groups 0..sc: a warp per base bin
+    __shared__ float2 slices[kWarpsPerCta][kMirrorOff + kMaxClusterSpan];
+    const int nb = (B + 1) >> 1;
+    const int ctas = (sc + 1) * int(gridDim.x);
+    const int w = threadIdx.x >> 5;
+    for (int cta = g * int(gridDim.x) + int(blockIdx.x); cta * kWarpsPerCta < nb;
+         cta += ctas) {
+      const int beta = cta * kWarpsPerCta + w;
+      if (beta < nb) FoldClusterWarp<TX>(it, tr, beta, sc, slices[w]);
+    }
+    return;
+  }
+  if (int(blockIdx.x) * kFoldBins >= B) return;
 
   const int lane = threadIdx.x & (kFoldSplit - 1);
   const int beta = blockIdx.x * kFoldBins + threadIdx.x / kFoldSplit;
@@ -294,3 +432,4 @@ void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
 }
 
 }  // namespace mpsft
+

@@ -178,11 +178,9 @@ __global__ void __launch_bounds__(1024)
       c.near_ties += fl[2];
       if (fl[1] & kStatusUnresolved) c.unresolved += 1;
       c.fp64_iters += it.force_fp64;
-      const int64_t g = int64_t(it.trials) * it.p * it.rows;
       const bool f64 = c.fp64_path || it.force_fp64;
-      c.gathers += g;
-      c.bin_bytes += 32 * g + int64_t(f64 ? 8 : 4) * (it.p2 + 1) +
-                     int64_t(it.trials) * (f64 ? 16 : 8) * it.rows * it.bins;
+      c.gathers += BinGathers(it, f64);
+      c.bin_bytes += BinBytesOf(it, f64);
       if (fl[1] & kStatusCapacity) {
         c.status = kSolveCapacity;
       } else if (fl[1] & kStatusNonFinite) {
