@@ -346,6 +346,35 @@ int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                         double *const *out_c, const int32_t *cap,
                         int32_t *count, mpsft_stats *stats);
 
+/* ---- autotuner of the FP32 binning's launch shape ------------------------
+ * No counterpart in the reference (its binning shapes are fixed by the caller,
+ * src/binner_bench.cc:28-33). The FP32 fold has mpsft_fold_shape_count()
+ * launch shapes: threads sharing a bin (2, 4, 8) and folds in flight per
+ * thread (4, 8) of the row pairs, with the row cluster (row 0 and the pairs
+ * whose windows overlap, each sample gathered once) on or off; every shape
+ * computes the same sums up to FP32 rounding, so the frequency sets are the
+ * same. A context keeps a table: key (ceil(log2 bins), ceil(log2 n),
+ * ceil(log2 signals per launch), complex128 input) -> shape, bins being those
+ * a solve sizes its launches for (the batch's largest, or 4 min_bins + 1 once
+ * every signal needs at most that many); launches whose key is not in the
+ * table use shape 0. */
+int32_t mpsft_fold_shape_count(void);
+/* Times every shape on one batched FP32 solve of these signals (each shape
+ * repeats times, the draws from RNGs seeded seed + i, the caller's RNGs
+ * untouched), CUDA events around every binning launch, and records for each
+ * bins class of the solve's launches the shape with the least total time. */
+int mpsft_autotune(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                   const mpsft_solve_options *opts, int32_t nsig, int32_t seed,
+                   int32_t repeats);
+/* The table as text (one line per key: bins_log2 n_log2 signals_log2
+ * complex128 shape microseconds); load replaces the context's table. */
+int mpsft_tuning_save(mpsft_ctx *ctx, const char *path);
+int mpsft_tuning_load(mpsft_ctx *ctx, const char *path);
+int32_t mpsft_tuning_size(const mpsft_ctx *ctx);
+/* Every FP32 binning launch of the context uses shape (-1 = the table's
+ * choice, the default). */
+int mpsft_ctx_set_fold_shape(mpsft_ctx *ctx, int32_t shape);
+
 /* ---- test data and result analysis (Demo1's constructor and PostAnalyze) -- */
 /* GenerateModeMap (src/gen.cc:27-39) on rng: count distinct positions
  * k = RandomInt32() mod n, each with coefficient (RandomNormal(),

@@ -29,6 +29,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmpsft_gb300.so")
+# launch shapes of the FP32 binning chosen by the autotuner on GB300
+# (python -m mpsft_gb300.tune); MPSFT_TUNING_FILE overrides, "none" disables
+TUNING_PATH = os.path.join(_HERE, "tuning", "gb300_fold_shapes.tsv")
 
 OK, ERR_INVALID, ERR_UNSUPPORTED_N, ERR_CUDA, ERR_CAPACITY, ERR_ITER_CAP, \
     ERR_NONFINITE, ERR_NOMEM = range(8)
@@ -126,6 +129,12 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_ctx_set_stream": (I, [P, P]),
         "mpsft_ctx_set_profiling": (I, [P, I]),
         "mpsft_ctx_bin_launches": (I, [P, P, I32, P]),
+        "mpsft_fold_shape_count": (I32, []),
+        "mpsft_ctx_set_fold_shape": (I, [P, I32]),
+        "mpsft_autotune": (I, [P, P, ctypes.POINTER(SolveOptions), I32, I32, I32]),
+        "mpsft_tuning_save": (I, [P, ctypes.c_char_p]),
+        "mpsft_tuning_load": (I, [P, ctypes.c_char_p]),
+        "mpsft_tuning_size": (I32, [P]),
         "mpsft_last_error": (ctypes.c_char_p, [P]),
         "mpsft_status_string": (ctypes.c_char_p, [I]),
         "mpsft_rng_create": (I, [I32, PP]),
@@ -256,6 +265,32 @@ class Context:
         self._out_c = np.empty(0, np.complex128)
         # live signals of this context: freed before the context itself
         self._signals = weakref.WeakSet()
+        tuning = os.environ.get("MPSFT_TUNING_FILE", TUNING_PATH)
+        if tuning != "none" and os.path.exists(tuning):
+            self.tuning_load(tuning)
+
+    # ---- launch shapes of the FP32 binning (autotuner) ----------------------
+    def autotune(self, sigs: list, opts: list, seed: int = 4242, repeats: int = 2) -> None:
+        """Times every launch shape of the FP32 binning on one batched solve of
+        these signals and records the fastest per bins class (mpsft_autotune)."""
+        nsig = len(sigs)
+        sig_arr = (ctypes.c_void_p * nsig)(*[s_._h.value for s_ in sigs])
+        opt_arr = (SolveOptions * nsig)(*opts)
+        _check(self, self._lib.mpsft_autotune(self._h, sig_arr, opt_arr, nsig,
+                                              int(seed), int(repeats)))
+
+    def tuning_save(self, path: str) -> None:
+        _check(self, self._lib.mpsft_tuning_save(self._h, path.encode()))
+
+    def tuning_load(self, path: str) -> None:
+        _check(self, self._lib.mpsft_tuning_load(self._h, path.encode()))
+
+    def tuning_size(self) -> int:
+        return int(self._lib.mpsft_tuning_size(self._h))
+
+    def set_fold_shape(self, shape: int) -> None:
+        """Forces one FP32 binning launch shape (-1: the tuning table's)."""
+        _check(self, self._lib.mpsft_ctx_set_fold_shape(self._h, int(shape)))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -584,7 +584,42 @@ int64_t BinBytes(const SigIter &it, bool fp64) { return BinBytesOf(it, fp64); }
 // Launch maxima of one iteration (grid sizes and shared memory).
 struct Maxima {
   int bins = 0, bits = 0, trials = 0, p2 = 0, m = 0, rows = 0, cap = 0;
+  int64_t n = 0;
+  // bins of the launch-shape lookup (FoldShapeFor): the bins the solve
+  // graph's phase sizes its launches for; 0 = bins
+  int tune_bins = 0;
 };
+
+int CeilLog2(int64_t v) {
+  int l = 0;
+  while ((int64_t(1) << l) < v) ++l;
+  return l;
+}
+
+// The bins a solve graph sizes an iteration's launches for (its phase's
+// largest bins: the batch's largest, or small_bins once every signal needs at
+// most that many, GraphLoop), so that a host-driven loop and the autotuner
+// look up the launch shape the graph uses.
+int32_t PhaseBins(int32_t bins, int32_t bins_cap, int32_t min_bins_max) {
+  const int32_t small_bins = (4 * min_bins_max) | 1;
+  return (bins_cap > small_bins && bins <= small_bins) ? small_bins : bins_cap;
+}
+
+// The FP32 fold's launch shape for a launch of nsig signals (largest bins
+// and length given): the forced shape, else the autotuner's entry for the
+// launch's classes, else the default shape 0.
+int FoldShapeFor(const mpsft_ctx *ctx, int max_bins, int64_t max_n, int nsig,
+                 bool c128) {
+  if (ctx->force_shape >= 0) return ctx->force_shape;
+  const int kb = CeilLog2(max_bins), kn = CeilLog2(max_n), ks = CeilLog2(nsig);
+  for (const auto &e : ctx->tuning) {
+    if (e.bins_log2 == kb && e.n_log2 == kn && e.nsig_log2 == ks &&
+        e.c128 == (c128 ? 1 : 0)) {
+      return e.shape;
+    }
+  }
+  return 0;
+}
 
 Maxima MaximaOf(const std::vector<SigIter> &h_its) {
   Maxima mx;
@@ -597,6 +632,7 @@ Maxima MaximaOf(const std::vector<SigIter> &h_its) {
     mx.m = std::max(mx.m, it.fft_m);
     mx.rows = std::max(mx.rows, it.rows);
     mx.cap = std::max(mx.cap, it.tab_cap);
+    mx.n = std::max<int64_t>(mx.n, it.n);
   }
   return mx;
 }
@@ -657,7 +693,12 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     int rc = timer->Begin();
     if (rc) return rc;
   }
-  if (!ahead) LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, fp64, s);
+  const int shape = FoldShapeFor(ctx, mx.tune_bins > 0 ? mx.tune_bins : mx.bins,
+                                 mx.n, nsig, x_c128);
+  if (!ahead) {
+    LaunchBinFold(d_its, nsig, mx.bins, mx.bits, mx.trials, x_c128, fp64, s, false,
+                  shape);
+  }
   if (timer) {
     int rc = timer->End();
     if (rc) return rc;
@@ -675,7 +716,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_plan_p, ctx->pre));
     LaunchWindow32(ahead->its_ahead, nsig, mx.p2, ctx->pre);
     LaunchBinFold(ahead->its_ahead, nsig, mx.bins, mx.bits, mx.trials, x_c128, false,
-                  ctx->pre);
+                  ctx->pre, false, shape);
     LaunchBluesteinSetup(ahead->its_ahead, nsig, mx.m, false, ctx->tw32, ctx->tw64,
                          ctx->pre);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_p, ctx->pre));
@@ -741,11 +782,14 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
 
 int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
                     const std::vector<SigIter> &h_its, bool x_c128, bool fp64,
-                    BinTimer *timer, int64_t *launched = nullptr) {
+                    BinTimer *timer, int64_t *launched = nullptr,
+                    int32_t tune_bins = 0) {
   bool any_forced = false;
   for (const SigIter &it : h_its) any_forced |= it.active && it.force_fp64;
-  return LaunchIterationKernels(ctx, d_its, nsig, MaximaOf(h_its), x_c128, fp64,
-                                any_forced, timer, launched, ctx->stream);
+  Maxima mx = MaximaOf(h_its);
+  mx.tune_bins = tune_bins;
+  return LaunchIterationKernels(ctx, d_its, nsig, mx, x_c128, fp64, any_forced,
+                                timer, launched, ctx->stream);
 }
 
 struct ModeOut {
@@ -892,6 +936,7 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     mx.p2 = std::max(mx.p2, s.p2_cap);
     mx.m = std::max(mx.m, s.m_cap);
     mx.cap = std::max(mx.cap, s.tab_cap);
+    mx.n = std::max<int64_t>(mx.n, s.n);
   }
   mx.trials = tmax;
   const int stride = dt->stride;
@@ -958,7 +1003,7 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   const std::vector<int64_t> key = {
       int64_t(reinterpret_cast<uintptr_t>(ctx->arena)), nsig, mx.bins, mx.bits,
       mx.rows, mx.p2, mx.m, mx.cap, mx.trials, fp64, x_c128, any_forced,
-      small_bins, mx_small.p2, pipe};
+      small_bins, mx_small.p2, pipe, ctx->tuning_version, ctx->force_shape};
   if (ctx->graph_key != key || ctx->graph_exec == nullptr) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -1016,7 +1061,8 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
           LaunchPlan(ctx->d_solve_ctl, d_its, nsig, ph.plan_max, ctx->cap);
           LaunchWindow32(d_its, nsig, ph.shape.p2, ctx->cap);
           LaunchBinFold(d_its, nsig, ph.shape.bins, ph.shape.bits, ph.shape.trials,
-                        x_c128, false, ctx->cap);
+                        x_c128, false, ctx->cap, false,
+                        FoldShapeFor(ctx, ph.shape.bins, ph.shape.n, nsig, x_c128));
           LaunchBluesteinSetup(d_its, nsig, ph.shape.m, false, ctx->tw32, ctx->tw64,
                                ctx->cap);
           cudaGraph_t captured = nullptr;
@@ -1434,7 +1480,15 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                         ctx->stream));
       }
     }
-    rc = LaunchIteration(ctx, d_its, nsig, its, x_c128, fp64, &timer, &launches);
+    // the launch shape the solve graph would use for this iteration
+    int32_t bins_now = 0, bins_cap = 0, min_bins_max = 1;
+    for (int i = 0; i < nsig; ++i) {
+      bins_cap = std::max(bins_cap, shapes[i].bins_cap);
+      min_bins_max = std::max(min_bins_max, opts[i].min_bins);
+      if (its[i].active) bins_now = std::max(bins_now, its[i].bins);
+    }
+    rc = LaunchIteration(ctx, d_its, nsig, its, x_c128, fp64, &timer, &launches,
+                         PhaseBins(bins_now, bins_cap, min_bins_max));
     if (rc) return rc;
     for (int i = 0; i < nsig; ++i) {
       MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_ctl + kCtlWords * i, ctls[i],
@@ -2122,7 +2176,8 @@ int BinInTimeImpl(mpsft_ctx *ctx, const mpsft_signal *sig, int32_t bins,
   BinTimer timer{ctx};
   rc = timer.Begin();
   if (rc) return rc;
-  LaunchBinFold(d_it, 1, bins, bits, 1, sig->dtype == MPSFT_C128, fp64, st);
+  LaunchBinFold(d_it, 1, bins, bits, 1, sig->dtype == MPSFT_C128, fp64, st, false,
+                FoldShapeFor(ctx, bins, sig->n, 1, sig->dtype == MPSFT_C128));
   rc = timer.End();
   if (rc) return rc;
   LaunchRowFFT(d_it, 1, it.rows, 1, it.fft_m, fp64, ctx->tw32, ctx->tw64, st);
@@ -2653,6 +2708,167 @@ int mpsft_solve(mpsft_ctx *ctx, const mpsft_signal *sig,
   int32_t *ok[1] = {out_k};
   double *oc[1] = {out_c};
   return SolveMany(ctx, sigs, opt, 1, rngs, ok, oc, &cap, count, stats);
+}
+
+int32_t mpsft_fold_shape_count(void) { return kFoldShapes; }
+
+int mpsft_ctx_set_fold_shape(mpsft_ctx *ctx, int32_t shape) {
+  if (!ctx) return MPSFT_ERR_INVALID;
+  if (shape < -1 || shape >= kFoldShapes) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "no such fold shape");
+  }
+  ctx->force_shape = shape;
+  return MPSFT_OK;
+}
+
+int mpsft_autotune(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                   const mpsft_solve_options *opts, int32_t nsig, int32_t seed,
+                   int32_t repeats) {
+  if (!ctx || !sigs || !opts || nsig <= 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  for (int i = 0; i < nsig; ++i) {
+    if (!sigs[i]) return Fail(ctx, MPSFT_ERR_INVALID, "null signal");
+    if (opts[i].precision != MPSFT_PREC_FP32) {
+      return Fail(ctx, MPSFT_ERR_INVALID, "the autotuner times FP32 solves");
+    }
+  }
+  repeats = std::max(1, repeats);
+  const bool prof = ctx->profiling;
+  const int32_t forced = ctx->force_shape;
+  // best[shape][launch]: the shortest of the repeats
+  std::vector<std::vector<double>> best(kFoldShapes);
+  std::vector<mpsft_bin_launch> recs0;
+  std::vector<int32_t> caps(nsig), counts(nsig);
+  std::vector<std::vector<int32_t>> ok(nsig);
+  std::vector<std::vector<double>> oc(nsig);
+  std::vector<int32_t *> okp(nsig);
+  std::vector<double *> ocp(nsig);
+  for (int i = 0; i < nsig; ++i) {
+    caps[i] = 4 * opts[i].k + 4096;
+    ok[i].resize(caps[i]);
+    oc[i].resize(2 * size_t(caps[i]));
+    okp[i] = ok[i].data();
+    ocp[i] = oc[i].data();
+  }
+  int rc = MPSFT_OK;
+  ctx->profiling = true;
+  for (int rep = 0; rep < repeats && rc == MPSFT_OK; ++rep) {
+    for (int shape = 0; shape < kFoldShapes && rc == MPSFT_OK; ++shape) {
+      ctx->force_shape = shape;
+      std::vector<mpsft_rng> rng(nsig);
+      std::vector<mpsft_rng *> rp(nsig);
+      for (int i = 0; i < nsig; ++i) {
+        rng[i].eng.seed(seed + i);
+        rp[i] = &rng[i];
+      }
+      rc = SolveMany(ctx, sigs, opts, nsig, rp.data(), okp.data(), ocp.data(),
+                     caps.data(), counts.data(), nullptr);
+      if (rc) break;
+      std::vector<double> &b = best[shape];
+      const std::vector<mpsft_bin_launch> &r = ctx->bin_launches;
+      if (shape == 0 && rep == 0) recs0 = r;
+      if (b.empty()) b.assign(r.size(), 1e300);
+      for (size_t j = 0; j < r.size() && j < b.size(); ++j) {
+        b[j] = std::min(b[j], r[j].ms);
+      }
+    }
+  }
+  ctx->profiling = prof;
+  ctx->force_shape = forced;
+  if (rc) return rc;
+  // a launch counts for the bins class its solve graph phase looks up
+  int64_t nmax = 0;
+  int32_t bins_cap = 0, min_bins_max = 1;
+  for (int i = 0; i < nsig; ++i) {
+    nmax = std::max<int64_t>(nmax, sigs[i]->n);
+    bins_cap = std::max<int32_t>(bins_cap,
+                                 std::max(2 * opts[i].k + 1, opts[i].min_bins));
+    min_bins_max = std::max(min_bins_max, opts[i].min_bins);
+  }
+  const bool c128 = sigs[0]->dtype == MPSFT_C128;
+  auto key_of = [&](const mpsft_bin_launch &r) {
+    return CeilLog2(PhaseBins(r.max_bins, bins_cap, min_bins_max));
+  };
+  std::vector<int> keys;
+  for (const auto &r : recs0) {
+    if (r.precision != MPSFT_PREC_FP32) continue;
+    const int kb = key_of(r);
+    if (std::find(keys.begin(), keys.end(), kb) == keys.end()) keys.push_back(kb);
+  }
+  // per key: the shape with the least total time over the key's launches
+  for (int kb : keys) {
+    double tbest = 1e300;
+    int sbest = 0;
+    for (int shape = 0; shape < kFoldShapes; ++shape) {
+      double t = 0;
+      for (size_t j = 0; j < recs0.size() && j < best[shape].size(); ++j) {
+        if (recs0[j].precision == MPSFT_PREC_FP32 && key_of(recs0[j]) == kb) {
+          t += best[shape][j];
+        }
+      }
+      if (t < tbest) {
+        tbest = t;
+        sbest = shape;
+      }
+    }
+    mpsft_ctx::TuneEntry e{kb, CeilLog2(nmax), CeilLog2(nsig), c128 ? 1 : 0, sbest,
+                           float(1e3 * tbest)};
+    auto &tab = ctx->tuning;
+    tab.erase(std::remove_if(tab.begin(), tab.end(),
+                             [&](const mpsft_ctx::TuneEntry &o) {
+                               return o.bins_log2 == e.bins_log2 &&
+                                      o.n_log2 == e.n_log2 &&
+                                      o.nsig_log2 == e.nsig_log2 && o.c128 == e.c128;
+                             }),
+              tab.end());
+    tab.push_back(e);
+  }
+  ctx->tuning_version += 1;
+  return MPSFT_OK;
+}
+
+int mpsft_tuning_save(mpsft_ctx *ctx, const char *path) {
+  if (!ctx || !path) return MPSFT_ERR_INVALID;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return Fail(ctx, MPSFT_ERR_INVALID, std::string("cannot write ") + path);
+  std::fprintf(f, "# mpsft-gb300 fold launch shapes: bins_log2 n_log2 "
+                  "signals_log2 complex128 shape us\n");
+  for (const auto &e : ctx->tuning) {
+    std::fprintf(f, "%d %d %d %d %d %.3f\n", e.bins_log2, e.n_log2, e.nsig_log2,
+                 e.c128, e.shape, double(e.us));
+  }
+  std::fclose(f);
+  return MPSFT_OK;
+}
+
+int mpsft_tuning_load(mpsft_ctx *ctx, const char *path) {
+  if (!ctx || !path) return MPSFT_ERR_INVALID;
+  FILE *f = std::fopen(path, "r");
+  if (!f) return Fail(ctx, MPSFT_ERR_INVALID, std::string("cannot read ") + path);
+  std::vector<mpsft_ctx::TuneEntry> tab;
+  char line[256];
+  while (std::fgets(line, sizeof(line), f)) {
+    if (line[0] == '#' || line[0] == '\n') continue;
+    mpsft_ctx::TuneEntry e{};
+    double us = 0;
+    if (std::sscanf(line, "%d %d %d %d %d %lf", &e.bins_log2, &e.n_log2,
+                    &e.nsig_log2, &e.c128, &e.shape, &us) != 6 ||
+        e.shape < 0 || e.shape >= kFoldShapes) {
+      std::fclose(f);
+      return Fail(ctx, MPSFT_ERR_INVALID, std::string("bad tuning line in ") + path);
+    }
+    e.us = float(us);
+    tab.push_back(e);
+  }
+  std::fclose(f);
+  ctx->tuning = tab;
+  ctx->tuning_version += 1;
+  return MPSFT_OK;
+}
+
+int32_t mpsft_tuning_size(const mpsft_ctx *ctx) {
+  return ctx ? int32_t(ctx->tuning.size()) : 0;
 }
 
 int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,

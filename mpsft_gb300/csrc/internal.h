@@ -68,6 +68,16 @@ struct mpsft_ctx {
   std::vector<cudaEvent_t> events;
   // binning launches of the last call made with profiling on
   std::vector<mpsft_bin_launch> bin_launches;
+  // launch shapes of the FP32 fold chosen by the autotuner, per key (bins,
+  // signal length and batch size classes: ceil(log2); complex128 input);
+  // force_shape >= 0 overrides the table (tuning runs, tests)
+  struct TuneEntry {
+    int32_t bins_log2, n_log2, nsig_log2, c128, shape;
+    float us;
+  };
+  std::vector<TuneEntry> tuning;
+  int32_t force_shape = -1;
+  int64_t tuning_version = 0;
   // table cache of FP32 solves: window tables (FP32, FP64, float-float) and
   // FP32 Bluestein tables per odd number of bins for one window delta, built
   // on first use and kept, like FFT plans (win_dev: block offsets, valid and

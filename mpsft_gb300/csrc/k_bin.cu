@@ -213,20 +213,21 @@ __device__ void FoldClusterWarp(const SigIter &it, int tr, int beta, int sc,
   __syncwarp();  // the slice is reused by the warp's next bin
 }
 
-// FP32 fold of the pair groups beyond the cluster: one CTA per (64 bins, row
-// group, trial, signal); kFoldSplit
-// threads share a bin and take every kFoldSplit-th fold, kFoldBatch folds of
-// both rows in flight at a time. Setup without divisions: indices by Barrett
-// reduction (or a mask), the phase m/n - t/(2B) as a 64-bit fixed-point
-// product phi_b (t + off) - psi t (wrap-around = exact reduction mod 1,
-// error < 2^-33 turns), rounded to 32-bit turns for sincospif.
-constexpr int kFoldSplit = 4;
-constexpr int kFoldBatch = 4;
-constexpr int kFoldBins = 256 / kFoldSplit;  // bins per CTA
-
-template <typename TX>
+// FP32 fold of the pair groups beyond the cluster: one CTA per (256/SPLIT
+// bins, row group, trial, signal); SPLIT threads share a bin and take every
+// SPLIT-th fold, BATCH folds of both rows in flight at a time. Setup without
+// divisions: indices by Barrett reduction (or a mask), the phase
+// m/n - t/(2B) as a 64-bit fixed-point product phi_b (t + off) - psi t
+// (wrap-around = exact reduction mod 1, error < 2^-33 turns), rounded to
+// 32-bit turns for sincospif. SPLIT, BATCH and CLUSTER (the row cluster on,
+// or every group folded pairwise) are the launch shape the autotuner picks
+// (FoldShapeOf); every shape computes the same sums up to FP32 rounding.
+template <typename TX, int SPLIT, int BATCH, bool CLUSTER>
 __global__ void __launch_bounds__(256, 4)
     k_bin_fold32(const SigIter *__restrict__ its, int gmax) {
+  constexpr int kFoldSplit = SPLIT;
+  constexpr int kFoldBatch = BATCH;
+  constexpr int kFoldBins = 256 / SPLIT;  // bins per CTA
   PdlEnter();
   const SigIter &it = its[blockIdx.z];
   if (!it.active || it.force_fp64) return;
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(256, 4)
   const int g = blockIdx.y % gmax;
   const int tr = blockIdx.y / gmax;
   if (tr >= it.trials || g > it.bits) return;
-  const int sc = ClusterGroups(it.folds, it.bits);
+  const int sc = CLUSTER ? ClusterGroups(it.folds, it.bits) : -1;
   if (g <= sc) {
     // the row cluster on the CTAs of groups 0..sc: a warp per base bin
     __shared__ float2 slices[kWarpsPerCta][kMirrorOff + kMaxClusterSpan];
@@ -408,11 +409,36 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The FP32 fold's launch shapes (complex64 input; complex128 input uses
+// shape 0): (SPLIT, BATCH, CLUSTER), shape 0 the default.
+using FoldKernel = void (*)(const SigIter *, int);
+const FoldKernel kFoldKernels[kFoldShapes] = {
+    k_bin_fold32<float2, 4, 4, true>,  k_bin_fold32<float2, 2, 4, true>,
+    k_bin_fold32<float2, 8, 4, true>,  k_bin_fold32<float2, 4, 8, true>,
+    k_bin_fold32<float2, 2, 8, true>,  k_bin_fold32<float2, 8, 8, true>,
+    k_bin_fold32<float2, 4, 4, false>, k_bin_fold32<float2, 2, 4, false>,
+    k_bin_fold32<float2, 8, 4, false>, k_bin_fold32<float2, 4, 8, false>,
+    k_bin_fold32<float2, 2, 8, false>, k_bin_fold32<float2, 8, 8, false>,
+};
+
 }  // namespace
+
+FoldShape FoldShapeOf(int shape) {
+  static const int8_t kSplit[kFoldShapes] = {4, 2, 8, 4, 2, 8, 4, 2, 8, 4, 2, 8};
+  static const int8_t kBatch[kFoldShapes] = {4, 4, 4, 8, 8, 8, 4, 4, 4, 8, 8, 8};
+  if (shape < 0 || shape >= kFoldShapes) shape = 0;
+  FoldShape f;
+  f.split = kSplit[shape];
+  f.batch = kBatch[shape];
+  f.cluster = shape < 6;
+  f.bins_per_cta = 256 / f.split;
+  return f;
+}
 
 void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
                    int max_trials, bool x_c128, bool fp64, cudaStream_t s,
-                   bool cond) {
+                   bool cond, int shape) {
+  if (shape < 0 || shape >= kFoldShapes) shape = 0;
   const int gmax = max_bits + 1;
   dim3 grid((max_bins + 31) / 32, gmax * max_trials, nsig);
   if (fp64) {
@@ -422,11 +448,13 @@ void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
       Launch(k_bin_fold64<float2>, grid, 256, 0, s, d_its, gmax, cond ? 1 : 0);
     }
   } else {
-    dim3 grid32((max_bins + kFoldBins - 1) / kFoldBins, gmax * max_trials, nsig);
+    const FoldShape sh = FoldShapeOf(x_c128 ? 0 : shape);
+    dim3 grid32((max_bins + sh.bins_per_cta - 1) / sh.bins_per_cta,
+                gmax * max_trials, nsig);
     if (x_c128) {
-      Launch(k_bin_fold32<double2>, grid32, 256, 0, s, d_its, gmax);
+      Launch(k_bin_fold32<double2, 4, 4, true>, grid32, 256, 0, s, d_its, gmax);
     } else {
-      Launch(k_bin_fold32<float2>, grid32, 256, 0, s, d_its, gmax);
+      Launch(kFoldKernels[shape], grid32, 256, 0, s, d_its, gmax);
     }
   }
 }

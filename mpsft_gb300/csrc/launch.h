@@ -67,11 +67,22 @@ void LaunchBluesteinSetup(const SigIter *d_its, int nsig, int max_m, bool fp64,
                           const float2 *tw32, const double2 *tw64,
                           cudaStream_t s, bool cond = false);
 
+// Launch shapes of the FP32 fold (the autotuner's choices): threads per bin
+// (split) and folds in flight per thread (batch) of the pair groups, the row
+// cluster on or off; shape 0 is the default.
+constexpr int kFoldShapes = 12;
+struct FoldShape {
+  int split, batch, bins_per_cta;
+  bool cluster;
+};
+FoldShape FoldShapeOf(int shape);
+
 // Fold of the windowed, modulated, permuted samples (the time-domain part of
-// BinInTime::Run). x_c128 selects double2 input, fp64 the FP64 arithmetic.
+// BinInTime::Run). x_c128 selects double2 input, fp64 the FP64 arithmetic,
+// shape the FP32 launch shape.
 void LaunchBinFold(const SigIter *d_its, int nsig, int max_bins, int max_bits,
                    int max_trials, bool x_c128, bool fp64, cudaStream_t s,
-                   bool cond = false);
+                   bool cond = false, int shape = 0);
 
 // Size-B FFT of every folded row, times e^{2 pi i b q / n}, into ubuf.
 void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
