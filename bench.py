@@ -417,6 +417,32 @@ def load_peaks() -> dict:
 PHASE_PROFILE = os.path.join(ROOT, "profiles", "bin_fold_phases_config2_batch64.md")
 
 
+def random_gather_ceiling(torch, device, gathers: int = 1 << 25,
+                          span_bytes: int = 2 << 30, reps: int = 5) -> dict:
+    """The GPU's rate of 8-byte reads at uniformly random addresses of a
+    2 GiB buffer (a library gather kernel, torch.take): the ceiling of a
+    binning launch whose samples are too sparse to share DRAM lines (the
+    late iterations). Reported beside the roofline, which stays against the
+    copy bandwidth."""
+    x = torch.empty(span_bytes // 8, dtype=torch.float64, device=device)
+    idx = torch.randint(0, x.numel(), (gathers,), device=device)
+    y = torch.take(x, idx)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        y = torch.take(x, idx)
+    e1.record()
+    torch.cuda.synchronize()
+    rate = gathers * reps / (e0.elapsed_time(e1) / 1e3)
+    del x, idx, y
+    torch.cuda.empty_cache()
+    return {"gathers_per_s": rate, "sector_gb_per_s": 32 * rate / 1e9,
+            "how": f"torch.take of {gathers} float64 at uniform random indices "
+                   f"of a {span_bytes >> 30} GiB buffer"}
+
+
 def profile_traffic() -> dict:
     """Measured DRAM traffic of the binning launches per phase, from the ncu
     summary committed under profiles/: {phase: {"dram_bytes_per_launch",
@@ -871,6 +897,8 @@ def run_gpu(args) -> None:
                  "accuracy": accuracy(sg0, k32, c32, k64, c64),
                  "test_data_pipeline": test_data_pipeline(ctx, m, sg0, k32, c32),
                  "dense_fft": dense_fft(torch, sigs_host, torch.device("cuda", local))}
+        extra["random_gather_ceiling"] = random_gather_ceiling(
+            torch, torch.device("cuda", local))
         if not args.no_extras:
             peak = load_peaks()["hbm_gbs"]
             extra["batched_fp64"] = extra_batched_fp64(torch, ctx, m, stream, sigs,
@@ -884,6 +912,15 @@ def run_gpu(args) -> None:
     if rank == 0:
         peaks = load_peaks()
         phases = binning_roofline(bin_records, 51, peaks["hbm_gbs"], profile_traffic())
+        ceil = extra.get("random_gather_ceiling")
+        if ceil:
+            # each phase's distinct gathered samples per second against the
+            # measured rate of random reads
+            for ph in phases.values():
+                ph["gathers_per_s"] = ph["gathers_per_launch"] / (
+                    ph["kernel_ms"] / ph["launches"] / 1e3)
+                ph["frac_of_random_gather_ceiling"] = (ph["gathers_per_s"] /
+                                                        ceil["gathers_per_s"])
         allp = phases.get("all", {})
         achieved = allp.get("achieved")
         line = {

@@ -95,6 +95,13 @@ typedef struct {
  * *count. */
 int mpsft_ctx_bin_launches(const mpsft_ctx *ctx, mpsft_bin_launch *out,
                            int32_t cap, int32_t *count);
+/* Solve-graph timeline (0 = off, default): with it on, every iteration body
+ * of a solve graph records the device clock at its end; mpsft_ctx_timeline
+ * gives the last solve's records in microseconds after the first (their
+ * differences are the iterations' periods) and their number. */
+int mpsft_ctx_set_timeline(mpsft_ctx *ctx, int enable);
+int mpsft_ctx_timeline(const mpsft_ctx *ctx, double *us, int32_t cap,
+                       int32_t *count);
 const char *mpsft_last_error(const mpsft_ctx *ctx);
 const char *mpsft_status_string(int status);
 

@@ -130,6 +130,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_ctx_set_profiling": (I, [P, I]),
         "mpsft_ctx_bin_launches": (I, [P, P, I32, P]),
         "mpsft_fold_shape_count": (I32, []),
+        "mpsft_ctx_set_timeline": (I, [P, I]),
+        "mpsft_ctx_timeline": (I, [P, P, I32, P]),
         "mpsft_ctx_set_fold_shape": (I, [P, I32]),
         "mpsft_autotune": (I, [P, P, ctypes.POINTER(SolveOptions), I32, I32, I32]),
         "mpsft_tuning_save": (I, [P, ctypes.c_char_p]),
@@ -287,6 +289,19 @@ class Context:
 
     def tuning_size(self) -> int:
         return int(self._lib.mpsft_tuning_size(self._h))
+
+    def set_timeline(self, on: bool) -> None:
+        """Record the device clock at the end of every solve-graph iteration."""
+        _check(self, self._lib.mpsft_ctx_set_timeline(self._h, int(bool(on))))
+
+    def timeline(self) -> np.ndarray:
+        """The last solve's iteration end times, microseconds after the first."""
+        count = np.zeros(1, np.int32)
+        _check(self, self._lib.mpsft_ctx_timeline(self._h, None, 0, _ptr(count)))
+        out = np.zeros(int(count[0]), np.float64)
+        _check(self, self._lib.mpsft_ctx_timeline(self._h, _ptr(out), out.size,
+                                                  _ptr(count)))
+        return out
 
     def set_fold_shape(self, shape: int) -> None:
         """Forces one FP32 binning launch shape (-1: the tuning table's)."""

@@ -206,6 +206,11 @@ struct SolveCtl {
   const int64_t *win_base;
   unsigned char *win_pool;
   int32_t *win_valid, *win_claim;
+  // timeline of a solve graph (signal 0's entry; null = off): k_finish
+  // writes the device clock at the end of every iteration body to
+  // timeline[timeline_count++] (at most timeline_cap entries)
+  unsigned long long *timeline;
+  int32_t timeline_cap, timeline_count;
 };
 
 // Byte offsets of the tables inside a table-cache block.

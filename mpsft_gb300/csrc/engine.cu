@@ -1038,6 +1038,10 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       Phase last = phases.back();
       last.exclude_fixed = false;
       last.pipelined = true;
+      // every signal with work is at its min_bins: the row transforms are no
+      // longer than those of the largest min_bins (small bins take the direct
+      // DFT, LaunchRowFFT)
+      last.shape.m = std::min(last.shape.m, 1 << FFTLog2(min_bins_max));
       phases.push_back(last);
     }
     int rc = MPSFT_OK;
@@ -1273,6 +1277,8 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   bytes += (sizeof(SolveCtl) +
             sizeof(int32_t) * kDrawChunk * (4 + max_trials_all) +
             sizeof(double) * kDrawChunk * max_trials_all * 2) * nsig + 2048;
+  constexpr int kTimelineCap = 4096;
+  bytes += sizeof(unsigned long long) * kTimelineCap + 256;
   int max_cap = 1;
   for (int i = 0; i < nsig; ++i) max_cap = std::max(max_cap, shapes[i].tab_cap);
   // table export staging
@@ -1290,6 +1296,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   const void **d_xs = cv.take<const void *>(nsig);
   int64_t *d_ns = cv.take<int64_t>(nsig);
   ctx->d_solve_ctl = cv.take<SolveCtl>(nsig);
+  unsigned long long *d_timeline = cv.take<unsigned long long>(kTimelineCap);
   ctx->d_draws = cv.take<int32_t>(size_t(nsig) * kDrawChunk * (4 + max_trials_all));
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
   int32_t *d_exp_keys = cv.take<int32_t>(size_t(max_cap) * nsig);
@@ -1393,6 +1400,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       draws.hc[i].win_claim = wc.claim;
     }
   }
+  if (!host_loop && ctx->timeline_on && !draws.hc.empty()) {
+    draws.hc[0].timeline = d_timeline;
+    draws.hc[0].timeline_cap = kTimelineCap;
+    draws.hc[0].timeline_count = 0;
+  }
+  ctx->timeline.clear();
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
   if (!host_loop) {
     rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, d_its_ahead, &its, &draws,
@@ -1413,6 +1426,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                     sizeof(SolveCtl) * nsig,
                                     cudaMemcpyDeviceToHost, ctx->stream));
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_ctl[0].timeline != nullptr && h_ctl[0].timeline_count > 0) {
+      ctx->timeline.resize(h_ctl[0].timeline_count);
+      MPSFT_CUDA(ctx, cudaMemcpy(ctx->timeline.data(), d_timeline,
+                                 sizeof(unsigned long long) * ctx->timeline.size(),
+                                 cudaMemcpyDeviceToHost));
+    }
     for (int i = 0; i < nsig; ++i) {
       Run &r = run[i];
       const SolveCtl &c = h_ctl[i];
@@ -2708,6 +2727,23 @@ int mpsft_solve(mpsft_ctx *ctx, const mpsft_signal *sig,
   int32_t *ok[1] = {out_k};
   double *oc[1] = {out_c};
   return SolveMany(ctx, sigs, opt, 1, rngs, ok, oc, &cap, count, stats);
+}
+
+int mpsft_ctx_set_timeline(mpsft_ctx *ctx, int enable) {
+  if (!ctx) return MPSFT_ERR_INVALID;
+  ctx->timeline_on = enable != 0;
+  return MPSFT_OK;
+}
+
+int mpsft_ctx_timeline(const mpsft_ctx *ctx, double *us, int32_t cap,
+                       int32_t *count) {
+  if (!ctx || !count || (cap > 0 && !us)) return MPSFT_ERR_INVALID;
+  const int32_t total = int32_t(ctx->timeline.size());
+  for (int32_t j = 0; j < total && j < cap; ++j) {
+    us[j] = 1e-3 * double(ctx->timeline[j] - ctx->timeline[0]);
+  }
+  *count = total;
+  return MPSFT_OK;
 }
 
 int32_t mpsft_fold_shape_count(void) { return kFoldShapes; }

@@ -168,6 +168,12 @@ __global__ void __launch_bounds__(1024)
              int32_t cond_lo, int32_t cond_hi, SigIter *__restrict__ its_ahead,
              int exclude_fixed) {
   PdlEnter();
+  if (threadIdx.x == 0 && ctl[0].timeline != nullptr &&
+      ctl[0].timeline_count < ctl[0].timeline_cap) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    ctl[0].timeline[ctl[0].timeline_count++] = t;
+  }
   int any = 0;
   for (int i = threadIdx.x; i < nsig; i += blockDim.x) {
     SolveCtl &c = ctl[i];

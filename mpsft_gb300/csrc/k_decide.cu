@@ -100,19 +100,24 @@ __device__ void BitonicSort(unsigned long long *keys, int m) {
   }
 }
 
-// Sorts the occupied slots by (bin, k0): one 64-bit key per slot,
-// bin << 51 | k0 << 20 | slot (bins < 2^13, k0 < 2^31, slots < 2^20), bitonic
-// sort in shared memory, then per-bin start and count from the run
-// boundaries. The subtraction later walks each bin's modes in increasing k0,
-// an order that does not depend on the table layout. Thread 0 also evaluates
-// this iteration's FP32 error scale eps.
-__global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its) {
+// Sorts the occupied slots by (bin, k0): a counting sort by bin (per-bin
+// counts, their exclusive scan, then each slot's key k0 << 20 | slot placed
+// in its bin's run), then each bin's run sorted by k0 by one thread
+// (insertion sort; a run holds the few modes of one bin). The subtraction
+// later walks each bin's modes in increasing k0, an order that does not
+// depend on the table layout. Thread 0 also evaluates this iteration's FP32
+// error scale eps. Shared memory: the keys (half the table, BucketKeys),
+// then the bins' counts and fill positions.
+__global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its,
+                                                 int max_bins) {
   PdlEnter();
-  extern __shared__ unsigned long long keys[];  // pow2 >= occupied slots
+  extern __shared__ unsigned long long keys[];
   const SigIter &it = its[blockIdx.x];
   if (!it.active) return;
   const int B = it.bins;
   const int occ = *it.tab_count;
+  int *cnt = reinterpret_cast<int *>(keys + BucketKeys(it.tab_cap));
+  int *fill = cnt + max_bins;
   if (threadIdx.x == 0 && it.eps_scale > 0) {
     *it.eps_dev = float(it.eps_scale * sqrt(*it.x_energy));
   }
@@ -122,33 +127,65 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
     if (threadIdx.x == 0) atomicOr(&it.flags[1], kStatusCapacity);
     return;
   }
-  int m = 1;
-  while (m < occ) m <<= 1;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    unsigned long long k = ~0ull;
-    if (i < occ) {
-      const int s = it.occ_list[i];
-      k = (static_cast<unsigned long long>(it.mode_bin[s]) << 51) |
-          (static_cast<unsigned long long>(uint32_t(it.tab_key[s])) << 20) |
-          static_cast<unsigned long long>(s);
-    }
-    keys[i] = k;
-  }
-  for (int i = threadIdx.x; i < B; i += blockDim.x) it.bkt_count[i] = 0;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) cnt[b] = 0;
   __syncthreads();
-  BitonicSort(keys, m);
-  __syncthreads();  // also orders the bkt_count zeroing when occ <= 1
   for (int i = threadIdx.x; i < occ; i += blockDim.x) {
-    const unsigned long long k = keys[i];
-    const int bin = int(k >> 51);
-    it.bkt_list[i] = int32_t(k & 0xFFFFFu);
-    if (i == 0 || int(keys[i - 1] >> 51) != bin) {
-      // first slot of its bin: the run ends at the next bin change
-      int e = i + 1;
-      while (e < occ && int(keys[e] >> 51) == bin) ++e;
-      it.bkt_start[bin] = i;
-      it.bkt_count[bin] = e - i;
+    atomicAdd(&cnt[it.mode_bin[it.occ_list[i]]], 1);
+  }
+  __syncthreads();
+  // exclusive scan of the counts: each thread a contiguous chunk, then the
+  // chunk totals by warp shuffles and one pass over the warps' totals
+  __shared__ int warp_tot[32];
+  const int per = (B + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  int local = 0;
+  for (int b = b0; b < b0 + per && b < B; ++b) local += cnt[b];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+      const int t = warp_tot[w];
+      warp_tot[w] = acc;
+      acc += t;
     }
+  }
+  __syncthreads();
+  int run = warp_tot[warp] + incl - local;
+  for (int b = b0; b < b0 + per && b < B; ++b) {
+    fill[b] = run;
+    it.bkt_start[b] = run;
+    it.bkt_count[b] = cnt[b];
+    run += cnt[b];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < occ; i += blockDim.x) {
+    const int sl = it.occ_list[i];
+    const int pos = atomicAdd(&fill[it.mode_bin[sl]], 1);
+    keys[pos] = (static_cast<unsigned long long>(uint32_t(it.tab_key[sl])) << 20) |
+                static_cast<unsigned long long>(sl);
+  }
+  __syncthreads();
+  // each bin's run in increasing k0 (keys are distinct: one slot per k0)
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    const int st = fill[b] - cnt[b], en = fill[b];
+    for (int i = st + 1; i < en; ++i) {
+      const unsigned long long k = keys[i];
+      int j = i - 1;
+      while (j >= st && keys[j] > k) {
+        keys[j + 1] = keys[j];
+        --j;
+      }
+      keys[j + 1] = k;
+    }
+    for (int i = st; i < en; ++i) it.bkt_list[i] = int32_t(keys[i] & 0xFFFFFu);
   }
 }
 
@@ -546,13 +583,18 @@ void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,
   Launch(k_mode_prep, grid, 256, 0, s, d_its, cond ? 1 : 0);
 }
 
+// Shared memory of k_bucket: the keys, then two ints per bin.
+inline size_t BucketSmem(int max_cap, int max_bins) {
+  return size_t(BucketKeys(max_cap)) * sizeof(unsigned long long) +
+         2 * sizeof(int) * size_t(max_bins);
+}
+
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
                   cudaStream_t s) {
-  (void)max_bins;
-  const size_t sm = size_t(BucketKeys(max_cap)) * sizeof(unsigned long long);
+  const size_t sm = BucketSmem(max_cap, max_bins);
   cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        int(sm));
-  Launch(k_bucket, nsig, 1024, sm, s, d_its);
+  Launch(k_bucket, nsig, 1024, sm, s, d_its, max_bins);
 }
 
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,
@@ -608,9 +650,10 @@ void LaunchPencil(const double2 *u3, int64_t count, double *sigma,
 bool DecideKernelsLaunchable() {
   int a = 0, b = 0, c = 0;
   const size_t smb = size_t(BucketKeys(kMaxTableCap)) * sizeof(unsigned long long);
+  const size_t smk = BucketSmem(kMaxTableCap, kMaxFFT / 2);
   cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       int(smb));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_bucket, 1024, smb);
+                       int(smk));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_bucket, 1024, smk);
   int e = 0;
   cudaFuncSetAttribute(k_export_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        int(smb));

@@ -191,6 +191,86 @@ __global__ void __launch_bounds__(kRowFftThreads)
   }
 }
 
+// Small bins (Bluestein size M <= kDirectMaxM, bins <= 63): the DFT as a
+// direct sum, one warp per row, X[k] = sum_j F[j] e^{-2 pi i j k / B} with
+// the unit roots of the bins grid in shared memory and compensated (TwoSum)
+// sums; then the same epilogue as the Bluestein kernel. At B = 51 a row costs
+// 51 terms per output, against two 128-point transforms and their barriers.
+constexpr int kDirectMaxM = 128;
+constexpr int kDirectRowsPerBlock = 8;
+
+struct CompSum {
+  float s = 0.f, c = 0.f;
+  __device__ void add(float v) {
+    const float t = s + v;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (v - bp);
+    s = t;
+  }
+  __device__ float value() const { return s + c; }
+};
+
+__global__ void __launch_bounds__(32 * kDirectRowsPerBlock)
+    k_row_dft_small(const SigIter *__restrict__ its, int cond) {
+  PdlEnter();
+  __shared__ float2 roots[kDirectMaxM];
+  __shared__ float2 rows[kDirectRowsPerBlock][kDirectMaxM];
+  const SigIter &it = its[blockIdx.z];
+  if (!it.active) return;
+  if (cond ? !RedoFP64(it) : it.force_fp64) return;
+  const int tr = blockIdx.y;
+  const int B = it.bins;
+  if (tr >= it.trials) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kDirectRowsPerBlock + warp;
+  const bool live = row < it.rows;
+  for (int r = threadIdx.x; r < B; r += blockDim.x) {
+    float sn, cs;
+    sincospif(-2.0f * float(r) / float(B), &sn, &cs);
+    roots[r] = make_float2(cs, sn);
+  }
+  if (live) {
+    const float2 *__restrict__ src = reinterpret_cast<const float2 *>(it.fold) +
+                                     (size_t(tr) * it.rows + row) * it.bins_cap;
+    for (int j = lane; j < B; j += 32) rows[warp][j] = src[j];
+  }
+  __syncthreads();
+  if (!live) return;
+  const bool out32 = it.ubuf32 != nullptr;
+  float2 bh = make_float2(0.f, 0.f), bl = bh;
+  if (out32) {
+    const double br = it.bq_re[tr], bi = it.bq_im[tr];
+    bh = make_float2(__double2float_rn(br), __double2float_rn(bi));
+    bl = make_float2(__double2float_rn(br - double(bh.x)),
+                     __double2float_rn(bi - double(bh.y)));
+  }
+  const float2 *f = rows[warp];
+  float mx = 0.f;
+  for (int k = lane; k < B; k += 32) {
+    CompSum xr, xi;
+    int idx = 0;
+    for (int j = 0; j < B; ++j) {
+      const float2 v = f[j], w = roots[idx];
+      xr.add(v.x * w.x - v.y * w.y);
+      xi.add(v.x * w.y + v.y * w.x);
+      idx += k;
+      if (idx >= B) idx -= B;
+    }
+    const float2 y = make_float2(xr.value(), xi.value());
+    if (out32) {
+      it.ubuf32[(size_t(tr) * it.rows + row) * it.bins_cap + k] = MulPhaseFF(y, bh, bl);
+    } else {
+      const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
+      it.ubuf[(size_t(tr) * it.rows + row) * it.bins_cap + k] =
+          cmul(bq, make_double2(y.x, y.y));
+    }
+    mx = fmaxf(mx, sqrtf(y.x * y.x + y.y * y.y));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0 && it.row_max != nullptr) it.row_max[tr * it.rows + row] = mx;
+}
+
 }  // namespace
 
 // Shared memory of a block: one padded row of the largest transform, or the
@@ -208,6 +288,12 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
   // blocks than about two per SM (so that a single signal, or the FP64
   // pipes, still spread over the GPU); every transform of the launch has at
   // most max_m points, so at least rpb rows per block
+  if (!fp64 && max_m <= kDirectMaxM) {
+    dim3 g((max_rows + kDirectRowsPerBlock - 1) / kDirectRowsPerBlock, max_trials,
+           nsig);
+    Launch(k_row_dft_small, g, 32 * kDirectRowsPerBlock, 0, s, d_its, cond ? 1 : 0);
+    return;
+  }
   const int rpb_cap =
       std::max(1, int(int64_t(max_rows) * max_trials * nsig / (2 * 152)));
   const int rpb = std::max(
