@@ -50,6 +50,35 @@ __device__ __forceinline__ V Twiddle(const V *__restrict__ tw, int N, int e,
   return w;
 }
 
+// Twiddles of a fused pass (up to three radix-2 stages, spans 4h, 2h, h):
+// stage S's butterfly m (m < S) takes W_{2Sh}^{k + m h}. Four are read from
+// the table, W_{8h}^k, W_{8h}^{k + h}, W_{4h}^k and W_{2h}^k; the others are
+// these times W_{2S}^{S/2} = -i (+i for the inverse), an exact rotation, so
+// every twiddle is a table value.
+template <typename V>
+__device__ __forceinline__ V RotMinusI(V w, bool inverse) {
+  V r;
+  r.x = inverse ? -w.y : w.y;
+  r.y = inverse ? w.x : -w.x;
+  return r;
+}
+template <typename V>
+__device__ __forceinline__ void PassTwiddles(const V *__restrict__ tw, int h, int k,
+                                             int R, bool inverse, V *wb) {
+  if (R >= 8) {
+    wb[0] = Twiddle(tw, 8 * h, k, inverse);
+    wb[1] = Twiddle(tw, 8 * h, k + h, inverse);
+  }
+  if (R >= 4) wb[2] = Twiddle(tw, 4 * h, k, inverse);
+  wb[3] = Twiddle(tw, 2 * h, k, inverse);
+}
+template <typename V>
+__device__ __forceinline__ V TwStage(const V *wb, int S, int m, bool inverse) {
+  if (S == 4) return m < 2 ? wb[m] : RotMinusI(wb[m - 2], inverse);
+  if (S == 2) return m == 0 ? wb[2] : RotMinusI(wb[2], inverse);
+  return wb[3];
+}
+
 // In-place radix-2 FFTs of a[0..m) (padded layout) in shared memory (m = 2^log2m <=
 // kMaxFFT), unnormalised, with up to three radix-2 stages fused per pass: a
 // thread loads R = 2^r elements spaced h apart, runs the r stages in
@@ -69,6 +98,8 @@ __device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
     const int k = g & (h - 1);
     const int base = (g / h) * (R * h) + k;
     V x[R];
+    V wb[4];  // the pass's table twiddles (loads issued with the data)
+    PassTwiddles(tw, h, k, R, inverse, wb);
 #pragma unroll
     for (int j = 0; j < R; ++j) x[j] = a[Pad(base + j * h)];
     // stages of span S h, S = R/2 .. 1: pairs (j, j + S), twiddle
@@ -80,8 +111,7 @@ __device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
         if ((j & S) == 0) {
           const V u = x[j], v = x[j + S];
           x[j] = vadd(u, v);
-          x[j + S] = vmul(vsub(u, v),
-                          Twiddle(tw, 2 * S * h, k + (j & (S - 1)) * h, inverse));
+          x[j + S] = vmul(vsub(u, v), TwStage(wb, S, j & (S - 1), inverse));
         }
       }
     }
@@ -99,6 +129,8 @@ __device__ __forceinline__ void DitPass(V *a, int m, int h, const V *tw,
     const int k = g & (h - 1);
     const int base = (g / h) * (R * h) + k;
     V x[R];
+    V wb[4];
+    PassTwiddles(tw, h, k, R, inverse, wb);
 #pragma unroll
     for (int j = 0; j < R; ++j) x[j] = a[Pad(base + j * h)];
     // stages of span S h, S = 1 .. R/2: twiddle W_{2Sh}^{k + (j mod S) h}
@@ -109,8 +141,7 @@ __device__ __forceinline__ void DitPass(V *a, int m, int h, const V *tw,
       for (int j = 0; j < R; ++j) {
         if ((j & S) == 0) {
           const V u = x[j];
-          const V v = vmul(x[j + S],
-                           Twiddle(tw, 2 * S * h, k + (j & (S - 1)) * h, inverse));
+          const V v = vmul(x[j + S], TwStage(wb, S, j & (S - 1), inverse));
           x[j] = vadd(u, v);
           x[j + S] = vsub(u, v);
         }
