@@ -95,13 +95,17 @@ typedef struct {
  * *count. */
 int mpsft_ctx_bin_launches(const mpsft_ctx *ctx, mpsft_bin_launch *out,
                            int32_t cap, int32_t *count);
-/* Solve-graph timeline (0 = off, default): with it on, every iteration body
- * of a solve graph records the device clock at its end; mpsft_ctx_timeline
- * gives the last solve's records in microseconds after the first (their
- * differences are the iterations' periods) and their number. */
+/* Solve-graph timeline (0 = off, default): with it on, the iteration kernels
+ * of a solve graph record their kernel id and the device clock when their
+ * first block starts. mpsft_ctx_timeline gives the last solve's records in
+ * start order (kernel[j]: 1 plan, 2 window32, 3 fold, 4 Bluestein tables,
+ * 5 mode preparation, 6 bucketing, 7 row transform, 8 decisions, 9 listed
+ * bins' mode terms, 10 merge, 11 re-binning, 12 listed bins' FP64
+ * decisions, 13 stop rule, 14 FP64 window; us[j] microseconds after the
+ * first) and their number (at most 16384). */
 int mpsft_ctx_set_timeline(mpsft_ctx *ctx, int enable);
-int mpsft_ctx_timeline(const mpsft_ctx *ctx, double *us, int32_t cap,
-                       int32_t *count);
+int mpsft_ctx_timeline(const mpsft_ctx *ctx, int32_t *kernel, double *us,
+                       int32_t cap, int32_t *count);
 const char *mpsft_last_error(const mpsft_ctx *ctx);
 const char *mpsft_status_string(int status);
 

@@ -131,7 +131,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_ctx_bin_launches": (I, [P, P, I32, P]),
         "mpsft_fold_shape_count": (I32, []),
         "mpsft_ctx_set_timeline": (I, [P, I]),
-        "mpsft_ctx_timeline": (I, [P, P, I32, P]),
+        "mpsft_ctx_timeline": (I, [P, P, P, I32, P]),
         "mpsft_ctx_set_fold_shape": (I, [P, I32]),
         "mpsft_autotune": (I, [P, P, ctypes.POINTER(SolveOptions), I32, I32, I32]),
         "mpsft_tuning_save": (I, [P, ctypes.c_char_p]),
@@ -294,14 +294,21 @@ class Context:
         """Record the device clock at the end of every solve-graph iteration."""
         _check(self, self._lib.mpsft_ctx_set_timeline(self._h, int(bool(on))))
 
-    def timeline(self) -> np.ndarray:
-        """The last solve's iteration end times, microseconds after the first."""
+    TIMELINE_KERNELS = {1: "plan", 2: "window32", 3: "fold", 4: "bluestein",
+                        5: "mode_prep", 6: "bucket", 7: "row_fft", 8: "decide",
+                        9: "listed_terms", 10: "merge", 11: "rebin",
+                        12: "decide_listed", 13: "finish", 14: "window64"}
+
+    def timeline(self):
+        """The last solve graph's kernel starts: (kernel ids, microseconds
+        after the first), in start order."""
         count = np.zeros(1, np.int32)
-        _check(self, self._lib.mpsft_ctx_timeline(self._h, None, 0, _ptr(count)))
-        out = np.zeros(int(count[0]), np.float64)
-        _check(self, self._lib.mpsft_ctx_timeline(self._h, _ptr(out), out.size,
-                                                  _ptr(count)))
-        return out
+        _check(self, self._lib.mpsft_ctx_timeline(self._h, None, None, 0, _ptr(count)))
+        ids = np.zeros(int(count[0]), np.int32)
+        us = np.zeros(int(count[0]), np.float64)
+        _check(self, self._lib.mpsft_ctx_timeline(self._h, _ptr(ids), _ptr(us),
+                                                  ids.size, _ptr(count)))
+        return ids, us
 
     def set_fold_shape(self, shape: int) -> None:
         """Forces one FP32 binning launch shape (-1: the tuning table's)."""

@@ -174,6 +174,11 @@ struct SigIter {
   int32_t esc_cap;
   int32_t *flags;       // [0] found, [1] status bits, [2] near-tie bins
                         // flagged this iteration, [3] mode count
+  // solve-graph timeline (signal 0's descriptor; null = off): the iteration
+  // kernels record (kernel id, device clock) at entry, TraceEnter
+  unsigned long long *trace;
+  uint32_t *trace_count;
+  uint32_t trace_cap;
 };
 
 // Per-signal state of a solve run on the device (k_plan / k_finish). The
@@ -206,11 +211,6 @@ struct SolveCtl {
   const int64_t *win_base;
   unsigned char *win_pool;
   int32_t *win_valid, *win_claim;
-  // timeline of a solve graph (signal 0's entry; null = off): k_finish
-  // writes the device clock at the end of every iteration body to
-  // timeline[timeline_count++] (at most timeline_cap entries)
-  unsigned long long *timeline;
-  int32_t timeline_cap, timeline_count;
 };
 
 // Byte offsets of the tables inside a table-cache block.
@@ -298,6 +298,29 @@ __host__ __device__ inline int64_t PhaseTableHi(int64_t n) {
 __device__ __forceinline__ void PdlEnter() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Kernel ids of the timeline (mpsft_ctx_set_timeline).
+enum : int32_t {
+  kTracePlan = 1, kTraceWindow32, kTraceFold, kTraceBluestein, kTraceModePrep,
+  kTraceBucket, kTraceRowFft, kTraceDecide, kTraceListedTerms, kTraceMerge,
+  kTraceRebin, kTraceDecideListed, kTraceFinish, kTraceWindow64,
+};
+
+// PdlEnter, then (timeline on) the kernel's id and the device clock when its
+// first block starts.
+__device__ __forceinline__ void PdlEnter(const SigIter *its, int32_t id) {
+  PdlEnter();
+  if (threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 &&
+      its[0].trace != nullptr) {
+    const uint32_t slot = atomicAdd(its[0].trace_count, 1u);
+    if (slot < its[0].trace_cap) {
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      its[0].trace[2 * slot] = uint64_t(id);
+      its[0].trace[2 * slot + 1] = t;
+    }
+  }
 }
 
 // v mod n (non-negative) for |v| < 2^63 by Barrett reduction with

@@ -661,6 +661,16 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   // iteration's tables were set up with its fold, in the previous body)
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+  if (ahead) {
+    // the next iteration's plan and window (at fixed bins they read nothing
+    // this iteration writes; the stop rule waits for the plan) from the start
+    // of the body on the prefold stream; its gather/fold and Bluestein
+    // tables follow this iteration's row FFT, below
+    MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->pre, ctx->ev_fork, 0));
+    LaunchPlan(ahead->ctl, ahead->its_ahead, nsig, ahead->plan_max, ctx->pre, true);
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_plan_p, ctx->pre));
+    LaunchWindow32(ahead->its_ahead, nsig, mx.p2, ctx->pre);
+  }
   if (!ahead) {
     LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_blue, ctx->side));
@@ -707,14 +717,11 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
   if (ahead) {
-    // the next iteration's plan, window, gather/fold and Bluestein tables
-    // (only this iteration's row FFT, now done, read the fold buffer and
-    // the Bluestein tables)
+    // the next iteration's gather/fold and Bluestein tables (only this
+    // iteration's row FFT, now done, read the fold buffer and the Bluestein
+    // tables)
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_p, s));
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->pre, ctx->ev_fork_p, 0));
-    LaunchPlan(ahead->ctl, ahead->its_ahead, nsig, ahead->plan_max, ctx->pre, true);
-    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_plan_p, ctx->pre));
-    LaunchWindow32(ahead->its_ahead, nsig, mx.p2, ctx->pre);
     LaunchBinFold(ahead->its_ahead, nsig, mx.bins, mx.bits, mx.trials, x_c128, false,
                   ctx->pre, false, shape);
     LaunchBluesteinSetup(ahead->its_ahead, nsig, mx.m, false, ctx->tw32, ctx->tw64,
@@ -838,6 +845,7 @@ int CheckSignal(mpsft_ctx *ctx, const mpsft_signal *sig) {
 }
 
 constexpr int kDrawChunk = 32;  // iterations of draws uploaded at a time
+constexpr int kTimelineCapacity = 1 << 14;  // kernel entries of a timeline
 constexpr int kGraphUnavailable = -100;
 static_assert(int(kSolveCapacity) == int(MPSFT_ERR_CAPACITY) &&
                   int(kSolveIterCap) == int(MPSFT_ERR_ITER_CAP) &&
@@ -953,6 +961,9 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
     it.trials = opts[i].trials;
     it.active = 0;
+    it.trace = i == 0 ? ctx->trace : nullptr;
+    it.trace_count = i == 0 ? ctx->trace_count : nullptr;
+    it.trace_cap = kTimelineCapacity;
   }
   {
     int rc = Upload(ctx, d_its, its->data(), sizeof(SigIter) * nsig, ctx->stream);
@@ -1277,8 +1288,8 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   bytes += (sizeof(SolveCtl) +
             sizeof(int32_t) * kDrawChunk * (4 + max_trials_all) +
             sizeof(double) * kDrawChunk * max_trials_all * 2) * nsig + 2048;
-  constexpr int kTimelineCap = 4096;
-  bytes += sizeof(unsigned long long) * kTimelineCap + 256;
+  constexpr int kTimelineCap = kTimelineCapacity;
+  bytes += 2 * sizeof(unsigned long long) * kTimelineCap + 512;
   int max_cap = 1;
   for (int i = 0; i < nsig; ++i) max_cap = std::max(max_cap, shapes[i].tab_cap);
   // table export staging
@@ -1296,7 +1307,8 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   const void **d_xs = cv.take<const void *>(nsig);
   int64_t *d_ns = cv.take<int64_t>(nsig);
   ctx->d_solve_ctl = cv.take<SolveCtl>(nsig);
-  unsigned long long *d_timeline = cv.take<unsigned long long>(kTimelineCap);
+  unsigned long long *d_trace = cv.take<unsigned long long>(2 * kTimelineCap);
+  uint32_t *d_trace_count = cv.take<uint32_t>(1);
   ctx->d_draws = cv.take<int32_t>(size_t(nsig) * kDrawChunk * (4 + max_trials_all));
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
   int32_t *d_exp_keys = cv.take<int32_t>(size_t(max_cap) * nsig);
@@ -1400,12 +1412,14 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       draws.hc[i].win_claim = wc.claim;
     }
   }
-  if (!host_loop && ctx->timeline_on && !draws.hc.empty()) {
-    draws.hc[0].timeline = d_timeline;
-    draws.hc[0].timeline_cap = kTimelineCap;
-    draws.hc[0].timeline_count = 0;
-  }
   ctx->timeline.clear();
+  ctx->trace = nullptr;
+  ctx->trace_count = nullptr;
+  if (!host_loop && ctx->timeline_on) {
+    MPSFT_CUDA(ctx, cudaMemsetAsync(d_trace_count, 0, sizeof(uint32_t), ctx->stream));
+    ctx->trace = d_trace;
+    ctx->trace_count = d_trace_count;
+  }
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
   if (!host_loop) {
     rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, d_its_ahead, &its, &draws,
@@ -1426,11 +1440,17 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                                     sizeof(SolveCtl) * nsig,
                                     cudaMemcpyDeviceToHost, ctx->stream));
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (h_ctl[0].timeline != nullptr && h_ctl[0].timeline_count > 0) {
-      ctx->timeline.resize(h_ctl[0].timeline_count);
-      MPSFT_CUDA(ctx, cudaMemcpy(ctx->timeline.data(), d_timeline,
-                                 sizeof(unsigned long long) * ctx->timeline.size(),
+    if (ctx->trace != nullptr) {
+      uint32_t cnt = 0;
+      MPSFT_CUDA(ctx, cudaMemcpy(&cnt, d_trace_count, sizeof(cnt),
                                  cudaMemcpyDeviceToHost));
+      cnt = std::min<uint32_t>(cnt, kTimelineCap);
+      ctx->timeline.resize(2 * size_t(cnt));
+      if (cnt > 0) {
+        MPSFT_CUDA(ctx, cudaMemcpy(ctx->timeline.data(), d_trace,
+                                   sizeof(unsigned long long) * ctx->timeline.size(),
+                                   cudaMemcpyDeviceToHost));
+      }
     }
     for (int i = 0; i < nsig; ++i) {
       Run &r = run[i];
@@ -2735,12 +2755,19 @@ int mpsft_ctx_set_timeline(mpsft_ctx *ctx, int enable) {
   return MPSFT_OK;
 }
 
-int mpsft_ctx_timeline(const mpsft_ctx *ctx, double *us, int32_t cap,
-                       int32_t *count) {
-  if (!ctx || !count || (cap > 0 && !us)) return MPSFT_ERR_INVALID;
-  const int32_t total = int32_t(ctx->timeline.size());
+int mpsft_ctx_timeline(const mpsft_ctx *ctx, int32_t *kernel, double *us,
+                       int32_t cap, int32_t *count) {
+  if (!ctx || !count || (cap > 0 && (!us || !kernel))) return MPSFT_ERR_INVALID;
+  const int32_t total = int32_t(ctx->timeline.size() / 2);
+  // in start order (the records' slots are taken in arrival order)
+  std::vector<std::pair<unsigned long long, int32_t>> r(total);
+  for (int32_t j = 0; j < total; ++j) {
+    r[j] = {ctx->timeline[2 * j + 1], int32_t(ctx->timeline[2 * j])};
+  }
+  std::sort(r.begin(), r.end());
   for (int32_t j = 0; j < total && j < cap; ++j) {
-    us[j] = 1e-3 * double(ctx->timeline[j] - ctx->timeline[0]);
+    kernel[j] = r[j].second;
+    us[j] = 1e-3 * double(r[j].first - r[0].first);
   }
   *count = total;
   return MPSFT_OK;

@@ -79,7 +79,9 @@ struct mpsft_ctx {
   // device clock at the end of every iteration body of the last solve graph
   // (mpsft_ctx_set_timeline)
   bool timeline_on = false;
-  std::vector<unsigned long long> timeline;
+  std::vector<unsigned long long> timeline;  // (kernel id, clock) pairs
+  unsigned long long *trace = nullptr;       // the current solve's buffer
+  uint32_t *trace_count = nullptr;
   int32_t force_shape = -1;
   int64_t tuning_version = 0;
   // table cache of FP32 solves: window tables (FP32, FP64, float-float) and

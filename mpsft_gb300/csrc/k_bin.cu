@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256, 4)
   constexpr int kFoldSplit = SPLIT;
   constexpr int kFoldBatch = BATCH;
   constexpr int kFoldBins = 256 / SPLIT;  // bins per CTA
-  PdlEnter();
+  PdlEnter(its, kTraceFold);
   const SigIter &it = its[blockIdx.z];
   if (!it.active || it.force_fp64) return;
   const int B = it.bins;

@@ -55,7 +55,7 @@ __device__ inline int32_t NextBins(const SolveCtl &c, const SigIter &it) {
 // which iteration iter still uses, are cleared by its k_finish instead).
 __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
                        int nsig, int32_t max_bins, int ahead) {
-  PdlEnter();
+  PdlEnter(its, kTracePlan);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nsig) return;
   SolveCtl &c = ctl[i];
@@ -167,13 +167,7 @@ __global__ void __launch_bounds__(1024)
              cudaGraphConditionalHandle handle, int set_condition,
              int32_t cond_lo, int32_t cond_hi, SigIter *__restrict__ its_ahead,
              int exclude_fixed) {
-  PdlEnter();
-  if (threadIdx.x == 0 && ctl[0].timeline != nullptr &&
-      ctl[0].timeline_count < ctl[0].timeline_cap) {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    ctl[0].timeline[ctl[0].timeline_count++] = t;
-  }
+  PdlEnter(its, kTraceFinish);
   int any = 0;
   for (int i = threadIdx.x; i < nsig; i += blockDim.x) {
     SolveCtl &c = ctl[i];

@@ -48,7 +48,7 @@ __device__ inline float WindowInFreq32(const SigIter &it, int64_t k1, int bin) {
 }
 
 __global__ void k_mode_prep(const SigIter *__restrict__ its, int cond) {
-  PdlEnter();
+  PdlEnter(its, kTraceModePrep);
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   if (cond && !RedoFP64(it)) return;
@@ -110,7 +110,7 @@ __device__ void BitonicSort(unsigned long long *keys, int m) {
 // then the bins' counts and fill positions.
 __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its,
                                                  int max_bins) {
-  PdlEnter();
+  PdlEnter(its, kTraceBucket);
   extern __shared__ unsigned long long keys[];
   const SigIter &it = its[blockIdx.x];
   if (!it.active) return;
@@ -173,19 +173,17 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
                 static_cast<unsigned long long>(sl);
   }
   __syncthreads();
-  // each bin's run in increasing k0 (keys are distinct: one slot per k0)
-  for (int b = threadIdx.x; b < B; b += blockDim.x) {
-    const int st = fill[b] - cnt[b], en = fill[b];
-    for (int i = st + 1; i < en; ++i) {
-      const unsigned long long k = keys[i];
-      int j = i - 1;
-      while (j >= st && keys[j] > k) {
-        keys[j + 1] = keys[j];
-        --j;
-      }
-      keys[j + 1] = k;
-    }
-    for (int i = st; i < en; ++i) it.bkt_list[i] = int32_t(keys[i] & 0xFFFFFu);
+  // each bin's run in increasing k0 (keys are distinct: one slot per k0): a
+  // key's place in its run is the number of smaller keys in the run, every
+  // key ranked by its own thread (runs are a bin's few modes)
+  for (int i = threadIdx.x; i < occ; i += blockDim.x) {
+    const unsigned long long k = keys[i];
+    // the run holding position i: the bin whose [start, fill) contains it
+    const int bin = it.mode_bin[int(k & 0xFFFFFu)];
+    const int st = fill[bin] - cnt[bin], en = fill[bin];
+    int rank = 0;
+    for (int j = st; j < en; ++j) rank += keys[j] < k ? 1 : 0;
+    it.bkt_list[st + rank] = int32_t(k & 0xFFFFFu);
   }
 }
 
@@ -194,7 +192,7 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
 template <typename T, int TMAX>
 __global__ void __launch_bounds__(256)
     k_decide(const SigIter *__restrict__ its, int mode, int cond, int mark) {
-  PdlEnter();
+  PdlEnter(its, kTraceDecide);
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
@@ -232,7 +230,7 @@ __device__ void MergeBin(const SigIter &it, int beta);
 template <int TMAX, int W, int G>
 __global__ void __launch_bounds__(32 * W)
     k_decide_listed(const SigIter *__restrict__ its, int redo, int merge) {
-  PdlEnter();
+  PdlEnter(its, kTraceDecideListed);
   __shared__ double2 s_p0[W][TMAX];
   __shared__ double2 s_pp[W][32][TMAX];
   __shared__ double2 s_pm[W][32][TMAX];
@@ -376,7 +374,7 @@ __global__ void __launch_bounds__(32 * W)
 // signal's listed bins, a thread per mode. Runs on the side stream while the
 // listed bins are re-binned.
 __global__ void __launch_bounds__(128) k_listed_terms(const SigIter *__restrict__ its) {
-  PdlEnter();
+  PdlEnter(its, kTraceListedTerms);
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.force_fp64 || it.esc_mask == nullptr) return;
   const int nf = *(volatile int32_t *)&it.flags[2];
@@ -454,7 +452,7 @@ __device__ void MergeBin(const SigIter &it, int beta) {
 // Candidates -> table, one thread per bin; bins held back for their FP64
 // near-tie decision (cand_valid >= kCandListed) are merged by that decision.
 __global__ void k_merge(const SigIter *__restrict__ its) {
-  PdlEnter();
+  PdlEnter(its, kTraceMerge);
   const SigIter &it = its[blockIdx.y];
   if (!it.active) return;
   const int beta = blockIdx.x * blockDim.x + threadIdx.x;

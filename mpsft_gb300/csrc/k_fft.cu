@@ -62,7 +62,7 @@ template <typename V>
 __global__ void __launch_bounds__(kRowFftThreads)
     k_row_fft(const SigIter *__restrict__ its, int max_trials,
               const V *__restrict__ tw, int cond, int rpb_cap) {
-  PdlEnter();
+  PdlEnter(its, kTraceRowFft);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned row_max_bits[kRowsMax];
   const SigIter &it = its[blockIdx.z];
@@ -212,7 +212,7 @@ struct CompSum {
 
 __global__ void __launch_bounds__(32 * kDirectRowsPerBlock)
     k_row_dft_small(const SigIter *__restrict__ its, int cond) {
-  PdlEnter();
+  PdlEnter(its, kTraceRowFft);
   __shared__ float2 roots[kDirectMaxM];
   __shared__ float2 rows[kDirectRowsPerBlock][kDirectMaxM];
   const SigIter &it = its[blockIdx.z];

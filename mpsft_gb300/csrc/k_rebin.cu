@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_rebin_prep(const SigIter *__restrict__ 
 template <typename TX>
 __global__ void __launch_bounds__(256, 2)
     k_rebin_ff(const SigIter *__restrict__ its, int nsig) {
-  PdlEnter();
+  PdlEnter(its, kTraceRebin);
   __shared__ int64_t items_end[kRebinMaxSignals];
   __shared__ float4 pw_s[8][kPowLen];
   for (int s = threadIdx.x; s < nsig; s += blockDim.x) {

@@ -42,7 +42,7 @@ __device__ double SincPi(double x) {
 // FP64 window (the reference's evaluation order) into wt64 and, when
 // present, the float-float copy wtff; with_fp32 also rounds it into wt32.
 __global__ void k_window64(const SigIter *__restrict__ its, int with_fp32) {
-  PdlEnter();
+  PdlEnter(its, kTraceWindow64);
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.tables_valid) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -68,7 +68,7 @@ __global__ void k_window64(const SigIter *__restrict__ its, int with_fp32) {
 // The same window evaluated in FP32 for the FP32 binning (a few ulp; the
 // FP64 tables are built beside it, off the binning's critical path).
 __global__ void k_window32(const SigIter *__restrict__ its) {
-  PdlEnter();
+  PdlEnter(its, kTraceWindow32);
   const SigIter &it = its[blockIdx.y];
   if (!it.active || it.tables_valid || it.force_fp64) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -112,7 +112,7 @@ template <typename V>
 __global__ void __launch_bounds__(512)
     k_bluestein_setup(const SigIter *__restrict__ its, const V *__restrict__ tw,
                       int cond) {
-  PdlEnter();
+  PdlEnter(its, kTraceBluestein);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *a = reinterpret_cast<V *>(smem_raw);
   const SigIter &it = its[blockIdx.x];
