@@ -151,6 +151,8 @@ struct SigIter {
   int32_t *esc_cnt;
   // per listed bin e: s^k, k < 64, with s = e^{2 pi i (b/n - (2 beta + 1)/(2B))}
   // as float-float {re.hi, im.hi, re.lo, im.lo} at [e * 64 + k], and s^64
+  // (the direct evaluation of every bin; null in solves and iterations,
+  // whose re-binning evaluates them per work item)
   float4 *esc_pow;
   double2 *esc_step;
   // per-value part of the FP32 error bound: eps_rel * (kEpsRowMax * max |U|

@@ -290,8 +290,9 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->cand_k0 = cv.take<int32_t>(s.bins_cap);
   it->cand_coef = cv.take<double2>(s.bins_cap);
   it->cand_err = cv.take<double>(s.bins_cap);
-  it->esc_pow = cv.take<float4>(size_t(kMaxListed) * 64);
-  it->esc_step = cv.take<double2>(kMaxListed);
+  // (the re-binning evaluates the listed bins' step powers itself)
+  it->esc_pow = nullptr;
+  it->esc_step = nullptr;
   it->esc_list = cv.take<int32_t>(kMaxListed);
   it->esc_mask = cv.take<uint32_t>(kMaxListed);
   it->esc_cap = kMaxListed;

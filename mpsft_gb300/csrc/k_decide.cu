@@ -204,12 +204,12 @@ __global__ void __launch_bounds__(256)
   } else {
     e = DecideBin<T, TMAX>(it, beta, FromBins{it, beta}, mode);
   }
-  // a listed near tie: its re-binning's tables (after the decision, when few
-  // registers are live); with mark, the bin's candidate is held back from
-  // the merge (cand_valid + kCandListed) until its FP64 decision
+  // a listed near tie: its re-binning's arrival counters cleared; with mark,
+  // the bin's candidate is held back from the merge (cand_valid +
+  // kCandListed) until its FP64 decision
   if (e >= 0) {
     if (mark && (threadIdx.x & 31) == 0) it.cand_valid[beta] += kCandListed;
-    PrepListedBin(it, e, beta, threadIdx.x & 31);
+    ClearListedBin(it, e, threadIdx.x & 31);
   }
 }
 

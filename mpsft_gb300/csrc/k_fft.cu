@@ -192,29 +192,23 @@ __global__ void __launch_bounds__(kRowFftThreads)
 }
 
 // Small bins (Bluestein size M <= kDirectMaxM, bins <= 63): the DFT as a
-// direct sum, one warp per row, X[k] = sum_j F[j] e^{-2 pi i j k / B} with
-// the unit roots of the bins grid in shared memory and compensated (TwoSum)
-// sums; then the same epilogue as the Bluestein kernel. At B = 51 a row costs
-// 51 terms per output, against two 128-point transforms and their barriers.
+// direct sum X[k] = sum_j F[j] e^{-2 pi i j k / B}, two warps per row and one
+// output per lane, with the unit roots of the bins grid in shared memory;
+// then the same epilogue as the Bluestein kernel. Each sum runs as four
+// interleaved FMA chains over j = u mod 4 (each with its own root index
+// j k mod B), added pairwise at the end: a short dependency chain per term,
+// and an FP32 error below that of the Bluestein transform it replaces (two
+// 128-point transforms at B = 51).
 constexpr int kDirectMaxM = 128;
-constexpr int kDirectRowsPerBlock = 8;
+constexpr int kDirectMaxBins = kDirectMaxM / 2;
+constexpr int kDirectRowsPerBlock = 4;  // two warps per row
 
-struct CompSum {
-  float s = 0.f, c = 0.f;
-  __device__ void add(float v) {
-    const float t = s + v;
-    const float bp = t - s;
-    c += (s - (t - bp)) + (v - bp);
-    s = t;
-  }
-  __device__ float value() const { return s + c; }
-};
-
-__global__ void __launch_bounds__(32 * kDirectRowsPerBlock)
+__global__ void __launch_bounds__(64 * kDirectRowsPerBlock)
     k_row_dft_small(const SigIter *__restrict__ its, int cond) {
   PdlEnter(its, kTraceRowFft);
-  __shared__ float2 roots[kDirectMaxM];
-  __shared__ float2 rows[kDirectRowsPerBlock][kDirectMaxM];
+  __shared__ float2 roots[kDirectMaxBins];
+  __shared__ float2 rows[kDirectRowsPerBlock][kDirectMaxBins];
+  __shared__ float wmax[2 * kDirectRowsPerBlock];
   const SigIter &it = its[blockIdx.z];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
@@ -222,7 +216,8 @@ __global__ void __launch_bounds__(32 * kDirectRowsPerBlock)
   const int B = it.bins;
   if (tr >= it.trials) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row = blockIdx.x * kDirectRowsPerBlock + warp;
+  const int lr = warp >> 1;
+  const int row = blockIdx.x * kDirectRowsPerBlock + lr;
   const bool live = row < it.rows;
   for (int r = threadIdx.x; r < B; r += blockDim.x) {
     float sn, cs;
@@ -232,43 +227,66 @@ __global__ void __launch_bounds__(32 * kDirectRowsPerBlock)
   if (live) {
     const float2 *__restrict__ src = reinterpret_cast<const float2 *>(it.fold) +
                                      (size_t(tr) * it.rows + row) * it.bins_cap;
-    for (int j = lane; j < B; j += 32) rows[warp][j] = src[j];
+    for (int j = (warp & 1) * 32 + lane; j < B; j += 64) rows[lr][j] = src[j];
   }
   __syncthreads();
-  if (!live) return;
-  const bool out32 = it.ubuf32 != nullptr;
-  float2 bh = make_float2(0.f, 0.f), bl = bh;
-  if (out32) {
-    const double br = it.bq_re[tr], bi = it.bq_im[tr];
-    bh = make_float2(__double2float_rn(br), __double2float_rn(bi));
-    bl = make_float2(__double2float_rn(br - double(bh.x)),
-                     __double2float_rn(bi - double(bh.y)));
-  }
-  const float2 *f = rows[warp];
+  const int k = (warp & 1) * 32 + lane;
   float mx = 0.f;
-  for (int k = lane; k < B; k += 32) {
-    CompSum xr, xi;
-    int idx = 0;
-    for (int j = 0; j < B; ++j) {
-      const float2 v = f[j], w = roots[idx];
-      xr.add(v.x * w.x - v.y * w.y);
-      xi.add(v.x * w.y + v.y * w.x);
-      idx += k;
-      if (idx >= B) idx -= B;
+  if (live && k < B) {
+    const float2 *f = rows[lr];
+    float xr[4] = {0.f, 0.f, 0.f, 0.f}, xi[4] = {0.f, 0.f, 0.f, 0.f};
+    int id[4];
+    id[0] = 0;
+    id[1] = k;
+    id[2] = (2 * k) % B;
+    id[3] = (3 * k) % B;
+    const int step = (4 * k) % B;
+    int j = 0;
+    for (; j + 4 <= B; j += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float2 v = f[j + u], w = roots[id[u]];
+        xr[u] = fmaf(v.x, w.x, xr[u]);
+        xr[u] = fmaf(-v.y, w.y, xr[u]);
+        xi[u] = fmaf(v.x, w.y, xi[u]);
+        xi[u] = fmaf(v.y, w.x, xi[u]);
+        id[u] += step;
+        if (id[u] >= B) id[u] -= B;
+      }
     }
-    const float2 y = make_float2(xr.value(), xi.value());
-    if (out32) {
-      it.ubuf32[(size_t(tr) * it.rows + row) * it.bins_cap + k] = MulPhaseFF(y, bh, bl);
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      if (j + u < B) {
+        const float2 v = f[j + u], w = roots[id[u]];
+        xr[u] = fmaf(v.x, w.x, xr[u]);
+        xr[u] = fmaf(-v.y, w.y, xr[u]);
+        xi[u] = fmaf(v.x, w.y, xi[u]);
+        xi[u] = fmaf(v.y, w.x, xi[u]);
+      }
+    }
+    const float2 y = make_float2((xr[0] + xr[1]) + (xr[2] + xr[3]),
+                                 (xi[0] + xi[1]) + (xi[2] + xi[3]));
+    const size_t o = (size_t(tr) * it.rows + row) * it.bins_cap + k;
+    if (it.ubuf32 != nullptr) {
+      const double br = it.bq_re[tr], bi = it.bq_im[tr];
+      const float2 bh = make_float2(__double2float_rn(br), __double2float_rn(bi));
+      const float2 bl = make_float2(__double2float_rn(br - double(bh.x)),
+                                    __double2float_rn(bi - double(bh.y)));
+      it.ubuf32[o] = MulPhaseFF(y, bh, bl);
     } else {
       const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
-      it.ubuf[(size_t(tr) * it.rows + row) * it.bins_cap + k] =
-          cmul(bq, make_double2(y.x, y.y));
+      it.ubuf[o] = cmul(bq, make_double2(y.x, y.y));
     }
-    mx = fmaxf(mx, sqrtf(y.x * y.x + y.y * y.y));
+    mx = sqrtf(y.x * y.x + y.y * y.y);
   }
+  // the row's largest magnitude: each warp's, then the row's pair of warps
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0 && it.row_max != nullptr) it.row_max[tr * it.rows + row] = mx;
+  if (lane == 0) wmax[warp] = mx;
+  __syncthreads();
+  if (live && (warp & 1) == 0 && lane == 0 && it.row_max != nullptr) {
+    it.row_max[tr * it.rows + row] = fmaxf(wmax[warp], wmax[warp + 1]);
+  }
 }
 
 }  // namespace
@@ -291,7 +309,7 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
   if (!fp64 && max_m <= kDirectMaxM) {
     dim3 g((max_rows + kDirectRowsPerBlock - 1) / kDirectRowsPerBlock, max_trials,
            nsig);
-    Launch(k_row_dft_small, g, 32 * kDirectRowsPerBlock, 0, s, d_its, cond ? 1 : 0);
+    Launch(k_row_dft_small, g, 64 * kDirectRowsPerBlock, 0, s, d_its, cond ? 1 : 0);
     return;
   }
   const int rpb_cap =

@@ -102,21 +102,31 @@ __global__ void __launch_bounds__(256, 2)
   PdlEnter(its, kTraceRebin);
   __shared__ int64_t items_end[kRebinMaxSignals];
   __shared__ float4 pw_s[8][kPowLen];
-  for (int s = threadIdx.x; s < nsig; s += blockDim.x) {
-    const SigIter &q = its[s];
-    int64_t items = 0;
-    if (q.active && !q.force_fp64) {
-      const int nf = *(volatile int32_t *)&q.flags[2];
-      if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * RebinChunks(q.p);
-    }
-    items_end[s] = items;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int s = 1; s < nsig; ++s) items_end[s] += items_end[s - 1];
-  }
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the signals' work item counts and their inclusive prefix sums, by warp 0
+  // (32 signals per step, a shuffle scan each)
+  if (warp == 0) {
+    int64_t carry = 0;
+    for (int s0 = 0; s0 < nsig; s0 += 32) {
+      const int s = s0 + lane;
+      int64_t items = 0;
+      if (s < nsig) {
+        const SigIter &q = its[s];
+        if (q.active && !q.force_fp64) {
+          const int nf = *(volatile int32_t *)&q.flags[2];
+          if (nf <= q.esc_cap) items = int64_t(nf) * q.trials * q.rows * RebinChunks(q.p);
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t v = __shfl_up_sync(0xffffffffu, items, o);
+        if (lane >= o) items += v;
+      }
+      if (s < nsig) items_end[s] = carry + items;
+      carry += __shfl_sync(0xffffffffu, items, 31);
+    }
+  }
+  __syncthreads();
   float4 *pw = pw_s[warp];
   const int64_t total = items_end[nsig - 1];
   for (int64_t w = int64_t(blockIdx.x) * 8 + warp; w < total;
@@ -140,6 +150,7 @@ __global__ void __launch_bounds__(256, 2)
     const int beta = it.esc_list[e];
     const int64_t n = it.n;
     const int64_t B = it.bins;
+    const ModN mod{uint32_t(n), it.n_inv};
     int64_t off = 0;
     if (r > 0) {
       const int s = (r - 1) / 2;
@@ -152,23 +163,35 @@ __global__ void __launch_bounds__(256, 2)
     const int64_t per = (chunk + 31) / 32;
     const int64_t t0 = c0 + lane * per;
     const int64_t t1 = min(t0 + per, c1);
+    // the bin's phase-step powers s^k (k < 64) into shared memory and s^64
+    // (StepPowers): evaluated here in a solve, from the per-bin tables in the
+    // direct evaluation of every bin
+    const int64_t g = 2 * int64_t(beta) + 1;
+    const uint32_t bm = mod(it.b);
+    float4 p0, p1;
+    double2 S;
+    if (it.esc_pow != nullptr) {
+      p0 = it.esc_pow[size_t(e) * kPowLen + lane];
+      p1 = it.esc_pow[size_t(e) * kPowLen + lane + 32];
+      S = it.esc_step[e];
+    } else {
+      StepPowers(it, beta, lane, &p0, &p1, &S);
+    }
     __syncwarp();
-    pw[lane] = it.esc_pow[size_t(e) * kPowLen + lane];
-    pw[lane + 32] = it.esc_pow[size_t(e) * kPowLen + lane + 32];
+    pw[lane] = p0;
+    pw[lane + 32] = p1;
     __syncwarp();
     double tr = 0.0, ti = 0.0;
     if (t0 < t1) {
       const int64_t twoB = 2 * B;
-      const int64_t g = 2 * int64_t(beta) + 1;
-      const int64_t u0 = PosMod(tau + t0, n);
-      uint32_t j = uint32_t(PosMod(int64_t(it.a) * u0 + it.c, n));
-      const uint32_t astep = uint32_t(PosMod(it.a, n));
+      const int64_t u0 = mod(tau + t0);
+      uint32_t j = mod(int64_t(it.a) * u0 + it.c);
+      const uint32_t astep = mod(it.a);
       const uint32_t nn = uint32_t(n);
-      const int64_t m0 = PosMod(int64_t(it.b) * u0, n);
+      const int64_t m0 = mod(int64_t(bm) * u0);
       const int64_t r0 = PosMod(g * t0, twoB);
       const double2 a0 = StepPhase(it, m0, r0);
       double ar = a0.x, ai = a0.y;
-      const double2 S = it.esc_step[e];
       const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
       const float2 *__restrict__ wff = it.wtff;
       for (int64_t tb = t0; tb < t1; tb += kPowLen) {

@@ -1,8 +1,6 @@
 // Preparation of a near-tie bin's re-binning (the FP32 path lists bins whose
-// decisions lie within their rounding bound of a threshold): the per-bin
-// table of powers of the phase step, its 64th power, cleared arrival
-// counters, and the FP64 row-0 terms of the bin's found modes for its FP64
-// decision.
+// decisions lie within their rounding bound of a threshold): the powers of
+// its phase step and cleared arrival counters.
 #pragma once
 
 #include "common.cuh"
@@ -35,37 +33,53 @@ __device__ inline double2 StepPhase(const SigIter &it, int64_t m, int64_t r) {
 }
 
 // Phase e^{2 pi i k Delta} from exact integer reductions:
-// k Delta = (k b mod n)/n - (k (2 beta + 1) mod 2B)/(2B) (mod 1).
-__device__ inline double2 PowerOfStep(const SigIter &it, int64_t k, int64_t b,
+// k Delta = (k b mod n)/n - (k (2 beta + 1) mod 2B)/(2B) (mod 1), for
+// 0 <= k <= kPowLen and b = it.b mod n.
+__device__ inline double2 PowerOfStep(const SigIter &it, int64_t k, uint32_t b,
                                       int64_t g) {
-  const int64_t n = it.n, twoB = 2 * int64_t(it.bins);
-  return StepPhase(it, PosMod(k * b, n), PosMod(k * g, twoB));
+  const ModN mod{uint32_t(it.n), it.n_inv};
+  const int64_t twoB = 2 * int64_t(it.bins);
+  return StepPhase(it, mod(k * int64_t(b)), (k * g) % twoB);
 }
 
-// Listed bin e (bin beta), one warp: with
-// s = e^{2 pi i (b/n - (2 beta + 1)/(2B))}, s^k for k < 64 as float-float
-// complex {re.hi, im.hi, re.lo, im.lo} and s^64 in FP64; the (trial, row)
-// arrival counters cleared. (A solve's FP64 terms of the bin's found modes
-// come from k_listed_terms, beside the re-binning.) Not inlined: the FP32
-// decide kernel calls it for the few bins it lists, after their decision.
-__device__ __noinline__ void PrepListedBin(const SigIter &it, int e, int beta,
-                                           int lane) {
-  const int64_t b = PosMod(it.b, int64_t(it.n));
-  const int64_t g = 2 * int64_t(beta) + 1;
+// Listed bin e: its (trial, row) arrival counters cleared, by the lanes of
+// one warp. In a solve the re-binning evaluates the bin's phase-step powers
+// itself, beside each work item's own start phase.
+__device__ inline void ClearListedBin(const SigIter &it, int e, int lane) {
   for (int i = lane; i < it.trials * it.rows; i += 32) {
     it.esc_cnt[size_t(e) * it.trials * it.rows + i] = 0;
   }
-  float4 *pw = it.esc_pow + size_t(e) * kPowLen;
-  // lanes 0..31: s^lane and s^(lane + 32); lane 0 also s^64
-  const double2 z0 = PowerOfStep(it, lane, b, g);
-  const double2 z1 = PowerOfStep(it, lane + 32, b, g);
-  const double2 z64 = PowerOfStep(it, kPowLen, b, g);
+}
+
+// s^k of bin beta's phase step s = e^{2 pi i (b/n - (2 beta + 1)/(2B))}, lane
+// k and k + 32, as float-float complex {re.hi, im.hi, re.lo, im.lo}, and
+// s^64 in FP64.
+__device__ inline void StepPowers(const SigIter &it, int beta, int lane, float4 *p0,
+                                  float4 *p1, double2 *s64) {
+  const ModN mod{uint32_t(it.n), it.n_inv};
+  const uint32_t bm = mod(it.b);
+  const int64_t g = 2 * int64_t(beta) + 1;
+  const double2 z0 = PowerOfStep(it, lane, bm, g);
+  const double2 z1 = PowerOfStep(it, lane + 32, bm, g);
+  *s64 = PowerOfStep(it, kPowLen, bm, g);
   FF zr = FFOf(z0.x), zi = FFOf(z0.y);
-  pw[lane] = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
+  *p0 = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
   zr = FFOf(z1.x);
   zi = FFOf(z1.y);
-  pw[lane + 32] = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
-  if (lane == 0) it.esc_step[e] = z64;
+  *p1 = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
+}
+
+// The direct evaluation of every bin (no solve tables, FP64 sincospi per
+// power): the powers once per bin into esc_pow / esc_step, and the counters.
+__device__ __noinline__ void PrepListedBin(const SigIter &it, int e, int beta,
+                                           int lane) {
+  ClearListedBin(it, e, lane);
+  float4 p0, p1;
+  double2 s64;
+  StepPowers(it, beta, lane, &p0, &p1, &s64);
+  it.esc_pow[size_t(e) * kPowLen + lane] = p0;
+  it.esc_pow[size_t(e) * kPowLen + lane + 32] = p1;
+  if (lane == 0) it.esc_step[e] = s64;
 }
 
 }  // namespace
