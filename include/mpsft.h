@@ -22,6 +22,7 @@
  *   mpsft_iterate       Iterate                src/iterate.h:65, src/iterate.cc:80-176
  *   mpsft_solve         Demo1::Run             src/demo1.h:39, src/demo1.cc:36-59
  *   mpsft_solve_batched (no counterpart: many Demo1::Run solves in one launch sequence)
+ *   mpsft_solve_batched_packed  the same, results of all signals in one pair of arrays
  *   mpsft_window_*      Window                 src/window.h:25-55, src/window.cc:28-81
  *   mpsft_rng_*         RandomSeed/RandomInt32 src/base.h:61-62, src/base.cc:52-53
  *   mpsft_num_bits      NumBits                src/iterate.cc:30-42
@@ -356,6 +357,17 @@ int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
                         mpsft_rng *const *rngs, int32_t *const *out_k,
                         double *const *out_c, const int32_t *cap,
                         int32_t *count, mpsft_stats *stats);
+
+/* mpsft_solve_batched with every signal's results in one pair of arrays:
+ * signal i's modes (sorted by k) at [offsets[i], offsets[i + 1]) of out_k
+ * and out_c (out_cap entries in all; offsets has nsig + 1 entries). A signal
+ * whose modes do not fit in what is left gets MPSFT_ERR_CAPACITY, its
+ * stored prefix and its full count in count[i]. */
+int mpsft_solve_batched_packed(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                               const mpsft_solve_options *opts, int32_t nsig,
+                               mpsft_rng *const *rngs, int32_t *out_k, double *out_c,
+                               int64_t out_cap, int64_t *offsets, int32_t *count,
+                               mpsft_stats *stats);
 
 /* ---- autotuner of the FP32 binning's launch shape ------------------------
  * No counterpart in the reference (its binning shapes are fixed by the caller,

@@ -172,6 +172,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                             ctypes.POINTER(Stats)]),
         "mpsft_solve_batched": (I, [P, P, ctypes.POINTER(SolveOptions), I32, P, P,
                                     P, P, P, ctypes.POINTER(Stats)]),
+        "mpsft_solve_batched_packed": (I, [P, P, ctypes.POINTER(SolveOptions), I32, P,
+                                           P, P, I64, P, P, ctypes.POINTER(Stats)]),
         "mpsft_generate_mode_map": (I, [P, I32, I32, P, P]),
         "mpsft_signal_generate": (I, [P, I64, P, P, I64, D, ctypes.c_uint64, I, PP]),
         "mpsft_signal_spectrum": (I, [P, P, P]),
@@ -603,28 +605,26 @@ class Context:
         """Many Demo1::Run solves advanced together. Returns
         (list of (k, coef) arrays, list of Stats dicts)."""
         nsig = len(sigs)
-        caps = np.array([cap or (4 * o.k + 4096) for o in opts], np.int32)
-        offs = np.zeros(nsig + 1, np.int64)
-        np.cumsum(caps, out=offs[1:])
-        total = int(offs[-1])
+        total = sum(cap or (4 * o.k + 4096) for o in opts)
         if self._out_k.size < total:
             self._out_k = np.empty(total, np.int32)
             self._out_c = np.empty(total, np.complex128)
         count = np.zeros(nsig, np.int32)
+        offs = np.zeros(nsig + 1, np.int64)
         stats = (Stats * nsig)()
         opt_arr = (SolveOptions * nsig)(*opts)
         sig_arr = (ctypes.c_void_p * nsig)(*[s._h.value for s in sigs])
         rng_arr = (ctypes.c_void_p * nsig)(*[r._h.value for r in rngs])
-        kb, cb = self._out_k.ctypes.data, self._out_c.ctypes.data
-        k_arr = (ctypes.c_void_p * nsig)(*(kb + 4 * offs[:-1]).tolist())
-        c_arr = (ctypes.c_void_p * nsig)(*(cb + 16 * offs[:-1]).tolist())
-        rc = self._lib.mpsft_solve_batched(
-            self._h, sig_arr, opt_arr, nsig, rng_arr, k_arr, c_arr, _ptr(caps),
-            _ptr(count), stats)
+        rc = self._lib.mpsft_solve_batched_packed(
+            self._h, sig_arr, opt_arr, nsig, rng_arr, _ptr(self._out_k),
+            _ptr(self._out_c), total, _ptr(offs), _ptr(count), stats)
         if raise_on_error:
             _check(self, rc)
-        out = [(self._out_k[o:o + c].copy(), self._out_c[o:o + c].copy())
-               for o, c in zip(offs[:-1].tolist(), count.tolist())]
+        # one copy of the packed results, handed out as one view per signal
+        used = int(offs[-1])
+        ks, cs = self._out_k[:used].copy(), self._out_c[:used].copy()
+        bounds = offs.tolist()
+        out = [(ks[a:b], cs[a:b]) for a, b in zip(bounds[:-1], bounds[1:])]
         return out, [stats[i].as_dict() for i in range(nsig)]
 
 

@@ -36,7 +36,11 @@ __host__ __device__ inline int RebinChunks(int p) {
 constexpr int kMaxListed = 256;    // near-tie bins listed per signal/iteration
 constexpr int kRebinMaxSignals = 256;  // signals per FP64 re-binning launch
 
-constexpr int kCtlWords = 4;  // found flag, status bits, near ties, mode count
+// found flag, status bits, near ties, mode count, spilled candidates
+constexpr int kCtlWords = 5;
+// candidates per signal and iteration whose k1 rounded into a neighbouring
+// bin's range (inserted after the others, in bin order: InsertSpills)
+constexpr int kSpillCap = 16;
 // cand_valid of a listed near-tie bin held back from the merge until its FP64
 // decision (added to the FP32 pass's 0 or 2)
 constexpr int32_t kCandListed = 3;
@@ -148,6 +152,9 @@ struct SigIter {
   // [(e * trials + t) * rows + r]: the chunk partials summed in chunk order
   // (by the warp that finishes the row's last chunk) and the arrival counter
   double2 *esc_sum;
+  // [(e * trials + t) * rows + r]: the FP64 sum of the listed bin's found
+  // modes in row r (k_listed_terms), subtracted by its FP64 decision
+  double2 *esc_msub;
   int32_t *esc_cnt;
   // per listed bin e: s^k, k < 64, with s = e^{2 pi i (b/n - (2 beta + 1)/(2B))}
   // as float-float {re.hi, im.hi, re.lo, im.lo} at [e * 64 + k], and s^64
@@ -175,9 +182,15 @@ struct SigIter {
   uint32_t *esc_mask;   // per listed bin: bit s set = rows 2s+1, 2s+2 near
   int32_t esc_cap;
   int32_t *flags;       // [0] found, [1] status bits, [2] near-tie bins
-                        // flagged this iteration, [3] mode count
+                        // flagged this iteration, [3] mode count, [4] spills
+  // spilled candidates of this iteration (kSpillCap): bin, k0, coefficient,
+  // error bound
+  int32_t *spill_beta;
+  int32_t *spill_k0;
+  double2 *spill_coef;
+  double *spill_err;
   // solve-graph timeline (signal 0's descriptor; null = off): the iteration
-  // kernels record (kernel id, device clock) at entry, TraceEnter
+  // kernels record (kernel id, device clock) at entry, PdlEnter
   unsigned long long *trace;
   uint32_t *trace_count;
   uint32_t trace_cap;
@@ -575,6 +588,50 @@ __host__ __device__ inline int BucketKeys(int tab_cap) { return tab_cap / 2; }
 // Hash slot of a mode key (Fibonacci hashing into a power-of-two table).
 __device__ inline uint32_t KeySlot(int32_t k, int32_t cap) {
   return (uint32_t(k) * 2654435769u) & uint32_t(cap - 1);
+}
+
+// mm[k0] += coef (and its error bound) in the signal's open-addressing table
+// (linear probing; a new key takes the next entry of the insertion list).
+__device__ inline void InsertMode(const SigIter &it, int32_t k0, double2 coef,
+                                  double err) {
+  const int cap = it.tab_cap;
+  uint32_t slot = KeySlot(k0, cap);
+  for (int probe = 0; probe < cap; ++probe) {
+    const int32_t prev = atomicCAS(&it.tab_key[slot], kEmptyKey, k0);
+    if (prev == kEmptyKey) {
+      it.occ_list[atomicAdd(it.tab_count, 1)] = int32_t(slot);
+    }
+    if (prev == kEmptyKey || prev == k0) {
+      atomicAdd(&it.tab_coef[slot].x, coef.x);
+      atomicAdd(&it.tab_coef[slot].y, coef.y);
+      if (err != 0.0) atomicAdd(&it.tab_err[slot], err);
+      return;
+    }
+    slot = (slot + 1) & uint32_t(cap - 1);
+  }
+  atomicOr(&it.flags[1], kStatusCapacity);
+}
+
+// The iteration's spilled candidates into the table, in increasing bin
+// order, after every other candidate (one thread per signal). A candidate's
+// k1 lies in its own bin's range except when it rounds across the bin's edge
+// (a mode at the edge, seen by both bins); only then can two candidates of
+// one iteration meet in one table entry. The others are added by atomics,
+// at most one per entry, and the spills in this fixed order, so the
+// coefficients do not depend on the order in which blocks run.
+__device__ inline void InsertSpills(const SigIter &it) {
+  const int ns = min(it.flags[4], kSpillCap);
+  uint32_t left = ns >= 32 ? 0xffffffffu : ((1u << ns) - 1u);
+  while (left) {
+    int best = __ffs(left) - 1;
+    for (uint32_t m = left & (left - 1); m; m &= m - 1) {
+      const int j = __ffs(m) - 1;
+      if (it.spill_beta[j] < it.spill_beta[best]) best = j;
+    }
+    InsertMode(it, it.spill_k0[best], it.spill_coef[best], it.spill_err[best]);
+    left &= ~(1u << best);
+  }
+  it.flags[4] = 0;
 }
 
 }  // namespace mpsft

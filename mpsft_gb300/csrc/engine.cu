@@ -265,6 +265,7 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->esc_part =
       cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap * kRebinChunks);
   it->esc_sum = cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap);
+  it->esc_msub = cv.take<double2>(size_t(kMaxListed) * s.trials * s.rows_cap);
   it->esc_cnt = cv.take<int32_t>(size_t(kMaxListed) * s.trials * s.rows_cap);
   it->tab_key = cv.take<int32_t>(s.tab_cap);
   it->tab_coef = cv.take<double2>(s.tab_cap);
@@ -296,6 +297,10 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->esc_list = cv.take<int32_t>(kMaxListed);
   it->esc_mask = cv.take<uint32_t>(kMaxListed);
   it->esc_cap = kMaxListed;
+  it->spill_beta = cv.take<int32_t>(kSpillCap);
+  it->spill_k0 = cv.take<int32_t>(kSpillCap);
+  it->spill_coef = cv.take<double2>(kSpillCap);
+  it->spill_err = cv.take<double>(kSpillCap);
   *ctl = cv.take<int32_t>(kCtlWords);
   it->flags = *ctl;
   it->tab_count = *ctl + 3;
@@ -333,14 +338,52 @@ int EnsureHostCtl(mpsft_ctx *ctx, size_t words) {
   return MPSFT_OK;
 }
 
+// Pinned, device-mapped host staging for a call's results: the device writes
+// the solve state and the tables' entries straight into it, so that the call
+// waits once for the graph and its export together.
 int EnsureHostStage(mpsft_ctx *ctx, size_t bytes) {
   if (ctx->h_stage_n >= bytes) return MPSFT_OK;
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   ctx->h_stage = nullptr;
+  ctx->d_stage = nullptr;
   ctx->h_stage_n = 0;
-  MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_stage, bytes));
+  MPSFT_CUDA(ctx, cudaHostAlloc(&ctx->h_stage, bytes, cudaHostAllocMapped));
+  void *dp = nullptr;
+  MPSFT_CUDA(ctx, cudaHostGetDevicePointer(&dp, ctx->h_stage, 0));
+  ctx->d_stage = static_cast<unsigned char *>(dp);
   ctx->h_stage_n = bytes;
   return MPSFT_OK;
+}
+
+// A solve call's results in the mapped staging: the solve state, then the
+// tables' entry counts, sorted flags, keys and coefficients (max_cap per
+// signal). Offsets from the staging's start, the same for both views.
+struct ResultStage {
+  size_t ctl = 0, counts = 0, sorted = 0, keys = 0, coefs = 0, bytes = 0;
+  int max_cap = 0;
+  ResultStage(int nsig, int cap) : max_cap(cap) {
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    counts = up(ctl + sizeof(SolveCtl) * size_t(nsig));
+    sorted = up(counts + sizeof(int32_t) * size_t(nsig));
+    keys = up(sorted + sizeof(int32_t) * size_t(nsig));
+    coefs = up(keys + sizeof(int32_t) * size_t(cap) * nsig);
+    bytes = up(coefs + sizeof(double2) * size_t(cap) * nsig);
+  }
+  template <typename T> T *at(unsigned char *base, size_t off) const {
+    return reinterpret_cast<T *>(base + off);
+  }
+};
+
+// The solve state and every table's entries (k_export_tables) into the
+// staging, on the context's stream.
+void LaunchResults(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
+                   const ResultStage &rs) {
+  unsigned char *d = ctx->d_stage;
+  LaunchCopyMapped(ctx->d_solve_ctl, rs.at<SolveCtl>(d, rs.ctl), sizeof(SolveCtl) * nsig,
+                   ctx->stream);
+  LaunchExportTables(d_its, nsig, rs.max_cap, rs.at<int32_t>(d, rs.keys),
+                     rs.at<double2>(d, rs.coefs), rs.at<int32_t>(d, rs.counts),
+                     rs.at<int32_t>(d, rs.sorted), ctx->stream);
 }
 
 // A solve's small host -> device transfers (iteration descriptors, draw
@@ -747,7 +790,7 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     // re-binning
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_l, s));
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork_l, 0));
-    LaunchListedTerms(d_its, nsig, ctx->side);
+    LaunchListedTerms(d_its, nsig, mx.trials, ctx->side);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_l, ctx->side));
     if (side_merge) {
       LaunchMerge(d_its, nsig, mx.bins, ctx->side);
@@ -796,8 +839,14 @@ int LaunchIteration(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   for (const SigIter &it : h_its) any_forced |= it.active && it.force_fp64;
   Maxima mx = MaximaOf(h_its);
   mx.tune_bins = tune_bins;
-  return LaunchIterationKernels(ctx, d_its, nsig, mx, x_c128, fp64, any_forced,
-                                timer, launched, ctx->stream);
+  const int rc = LaunchIterationKernels(ctx, d_its, nsig, mx, x_c128, fp64, any_forced,
+                                        timer, launched, ctx->stream);
+  if (rc != MPSFT_OK) return rc;
+  // (in the solve graph, k_finish inserts the spilled candidates)
+  LaunchInsertSpills(d_its, nsig, ctx->stream);
+  if (launched) *launched += 1;
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  return MPSFT_OK;
 }
 
 struct ModeOut {
@@ -934,7 +983,8 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
               SigIter *d_its, SigIter *d_its_ahead, std::vector<SigIter> *its,
               DrawTables *dt,
               const std::vector<int32_t> &force, bool any_forced, bool fp64,
-              bool x_c128, int64_t *launches) {
+              bool x_c128, int64_t *launches, const ResultStage &rs,
+              std::vector<SolveCtl> *ctl_out) {
   const int tmax = dt->tmax;
   Maxima mx;
   for (int i = 0; i < nsig; ++i) {
@@ -1164,10 +1214,14 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       return Fail(ctx, MPSFT_ERR_ITER_CAP, "solve graph did not converge");
     }
     MPSFT_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-    MPSFT_CUDA(ctx, cudaMemcpyAsync(hc.data(), ctx->d_solve_ctl,
-                                    sizeof(SolveCtl) * nsig,
-                                    cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
+    // the solve state and, for the usual case that every signal has
+    // stopped, the results with it: one wait per graph launch
+    LaunchResults(ctx, d_its, nsig, rs);
+    *launches += 2;
+    MPSFT_CUDA(ctx, cudaGetLastError());
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::memcpy(hc.data(), rs.at<SolveCtl>(ctx->h_stage, rs.ctl), sizeof(SolveCtl) * nsig);
     ctx->up_off = 0;  // every upload so far has been consumed
     int32_t most = 0;
     bool all_done = true, refilled = false;
@@ -1204,6 +1258,7 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
   }
   *launches += body_runs * ctx->graph_body_kernels;
+  *ctl_out = hc;
   // leave each RNG as if exactly the used draws had been taken
   for (int i = 0; i < nsig; ++i) {
     *rngs[i] = saved[i];
@@ -1215,12 +1270,22 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   return MPSFT_OK;
 }
 
-// One batched solve; the core of mpsft_solve and mpsft_solve_batched.
+// Results of every signal one after another in two arrays (signal i at
+// [offsets[i], offsets[i + 1])), for mpsft_solve_batched_packed.
+struct PackedOut {
+  int32_t *k;
+  double *c;
+  int64_t cap;
+  int64_t *offsets;
+};
+
+// One batched solve; the core of mpsft_solve, mpsft_solve_batched and
+// mpsft_solve_batched_packed (packed: out_k, out_c, cap are unused).
 int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
               const mpsft_solve_options *opts, int32_t nsig,
               mpsft_rng *const *rngs, int32_t *const *out_k,
               double *const *out_c, const int32_t *cap, int32_t *count,
-              mpsft_stats *stats) {
+              mpsft_stats *stats, const PackedOut *packed = nullptr) {
   if (nsig <= 0) return Fail(ctx, MPSFT_ERR_INVALID, "no signals");
   const bool fp64 = opts[0].precision == MPSFT_PREC_FP64;
   const bool x_c128 = sigs[0]->dtype == MPSFT_C128;
@@ -1293,10 +1358,11 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   bytes += 2 * sizeof(unsigned long long) * kTimelineCap + 512;
   int max_cap = 1;
   for (int i = 0; i < nsig; ++i) max_cap = std::max(max_cap, shapes[i].tab_cap);
-  // table export staging
-  bytes += (sizeof(int32_t) + sizeof(double2)) * size_t(max_cap) * nsig +
-           2 * sizeof(int32_t) * nsig + 1024;
   int rc = EnsureArena(ctx, bytes);
+  if (rc) return rc;
+  // the results' mapped staging (solve state, tables' entries)
+  const ResultStage rs(nsig, max_cap);
+  rc = EnsureHostStage(ctx, rs.bytes);
   if (rc) return rc;
   rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
   if (rc) return rc;
@@ -1312,9 +1378,6 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   uint32_t *d_trace_count = cv.take<uint32_t>(1);
   ctx->d_draws = cv.take<int32_t>(size_t(nsig) * kDrawChunk * (4 + max_trials_all));
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
-  int32_t *d_exp_keys = cv.take<int32_t>(size_t(max_cap) * nsig);
-  double2 *d_exp_coefs = cv.take<double2>(size_t(max_cap) * nsig);
-  int32_t *d_exp_counts = cv.take<int32_t>(2 * size_t(nsig));  // counts, sorted
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
   int64_t phase_entries = 1;
@@ -1422,9 +1485,10 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     ctx->trace_count = d_trace_count;
   }
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop0, ctx->stream));
+  std::vector<SolveCtl> h_ctl;
   if (!host_loop) {
     rc = GraphLoop(ctx, sigs, opts, nsig, rngs, shapes, d_its, d_its_ahead, &its, &draws,
-                   force, any_forced, fp64, x_c128, &launches);
+                   force, any_forced, fp64, x_c128, &launches, rs, &h_ctl);
     if (rc == kGraphUnavailable) {
       // no iteration ran and the tables are untouched; the RNGs are back
       // where they were
@@ -1434,13 +1498,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
   }
   if (!host_loop) {
-    std::vector<SolveCtl> h_ctl(nsig);
-    // on the context's stream (a legacy-stream copy would also wait for
-    // unrelated work, such as a caller's uploads on another stream)
-    MPSFT_CUDA(ctx, cudaMemcpyAsync(h_ctl.data(), ctx->d_solve_ctl,
-                                    sizeof(SolveCtl) * nsig,
-                                    cudaMemcpyDeviceToHost, ctx->stream));
-    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // (the graph's solve state and results are in the staging already)
     if (ctx->trace != nullptr) {
       uint32_t cnt = 0;
       MPSFT_CUDA(ctx, cudaMemcpy(&cnt, d_trace_count, sizeof(cnt),
@@ -1564,7 +1622,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       }
     }
   }
-  MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
+  if (host_loop) {
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
+    LaunchResults(ctx, d_its, nsig, rs);
+    launches += 2;
+    MPSFT_CUDA(ctx, cudaGetLastError());
+  }
   int first_err = MPSFT_OK;
   const double bin_ms = timer.TotalMs();
   if (ctx->profiling) {
@@ -1586,42 +1649,18 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
   }
   // the call's own kernels outside the loop: table clearing, phase tables,
-  // the energy pair (FP32), the export and the upload copies
-  launches += 2 + (fp64 ? 0 : 2) + 1 + ctx->up_launches;
-  // every table's entries in two copies: counts first, then the
-  // (signals x largest count) block of keys and coefficients
-  LaunchExportTables(d_its, nsig, max_cap, d_exp_keys, d_exp_coefs,
-                     d_exp_counts, d_exp_counts + nsig, ctx->stream);
-  MPSFT_CUDA(ctx, cudaGetLastError());
-  rc = EnsureHostStage(ctx, 2 * sizeof(int32_t) * nsig);
-  if (rc) return rc;
-  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, d_exp_counts,
-                                  2 * sizeof(int32_t) * nsig,
-                                  cudaMemcpyDeviceToHost, ctx->stream));
+  // the energy pair (FP32) and the upload copies
+  launches += 2 + (fp64 ? 0 : 2) + ctx->up_launches;
+  // every table's entries (k_export_tables, with the solve state) in the
+  // mapped staging: counts and sorted flags, then max_cap keys and
+  // coefficients per signal
   MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  std::vector<int32_t> counts(nsig), sorted(nsig);
-  std::memcpy(counts.data(), ctx->h_stage, sizeof(int32_t) * nsig);
-  std::memcpy(sorted.data(), ctx->h_stage + sizeof(int32_t) * nsig,
-              sizeof(int32_t) * nsig);
-  int32_t maxc = 0;
-  for (int i = 0; i < nsig; ++i) maxc = std::max(maxc, counts[i]);
-  const size_t kbytes = sizeof(int32_t) * size_t(maxc) * nsig;
-  rc = EnsureHostStage(ctx, kbytes + sizeof(double2) * size_t(maxc) * nsig + 64);
-  if (rc) return rc;
-  int32_t *h_keys = reinterpret_cast<int32_t *>(ctx->h_stage);
-  double2 *h_coefs =
-      reinterpret_cast<double2 *>(ctx->h_stage + ((kbytes + 15) & ~size_t(15)));
-  if (maxc > 0) {
-    MPSFT_CUDA(ctx, cudaMemcpy2DAsync(h_keys, sizeof(int32_t) * maxc, d_exp_keys,
-                                      sizeof(int32_t) * max_cap,
-                                      sizeof(int32_t) * maxc, nsig,
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-    MPSFT_CUDA(ctx, cudaMemcpy2DAsync(h_coefs, sizeof(double2) * maxc,
-                                      d_exp_coefs, sizeof(double2) * max_cap,
-                                      sizeof(double2) * maxc, nsig,
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  }
+  const int32_t *counts = rs.at<int32_t>(ctx->h_stage, rs.counts);
+  const int32_t *sorted = rs.at<int32_t>(ctx->h_stage, rs.sorted);
+  const int32_t *h_keys = rs.at<int32_t>(ctx->h_stage, rs.keys);
+  const double2 *h_coefs = rs.at<double2>(ctx->h_stage, rs.coefs);
+  const size_t maxc = size_t(max_cap);
+  int64_t packed_off = 0;
   float loop_ms = 0.f;
   MPSFT_CUDA(ctx, cudaEventElapsedTime(&loop_ms, ctx->ev_loop0, ctx->ev_loop1));
   for (int i = 0; i < nsig; ++i) {
@@ -1636,13 +1675,30 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
     int st = run[i].status;
     const int32_t m = counts[i];
-    if (m > cap[i]) st = st ? st : MPSFT_ERR_CAPACITY;
-    const int32_t w = std::min(m, cap[i]);
+    int32_t room = 0;
+    int32_t *dk = nullptr;
+    double *dc = nullptr;
+    if (packed) {
+      room = int32_t(std::min<int64_t>(packed->cap - packed_off, INT32_MAX));
+      dk = packed->k + packed_off;
+      dc = packed->c + 2 * packed_off;
+      packed->offsets[i] = packed_off;
+    } else {
+      room = cap[i];
+      dk = out_k[i];
+      dc = out_c[i];
+    }
+    if (m > room) st = st ? st : MPSFT_ERR_CAPACITY;
+    const int32_t w = std::min(m, room);
     for (int32_t j = 0; j < w; ++j) {
       const int32_t s = sorted[i] ? j : order[j];
-      out_k[i][j] = ki[s];
-      out_c[i][2 * j] = ci[s].x;
-      out_c[i][2 * j + 1] = ci[s].y;
+      dk[j] = ki[s];
+      dc[2 * j] = ci[s].x;
+      dc[2 * j + 1] = ci[s].y;
+    }
+    if (packed) {
+      packed_off += w;
+      packed->offsets[i + 1] = packed_off;
     }
     count[i] = m;
     if (stats) {
@@ -2945,6 +3001,20 @@ int mpsft_solve_batched(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   return SolveMany(ctx, sigs, opts, nsig, rngs, out_k, out_c, cap, count,
                    stats);
+}
+
+int mpsft_solve_batched_packed(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
+                               const mpsft_solve_options *opts, int32_t nsig,
+                               mpsft_rng *const *rngs, int32_t *out_k, double *out_c,
+                               int64_t out_cap, int64_t *offsets, int32_t *count,
+                               mpsft_stats *stats) {
+  if (!ctx || !sigs || !opts || !rngs || !out_k || !out_c || !offsets || !count ||
+      out_cap < 0) {
+    return Fail(ctx, MPSFT_ERR_INVALID, "null argument");
+  }
+  const PackedOut packed{out_k, out_c, out_cap, offsets};
+  return SolveMany(ctx, sigs, opts, nsig, rngs, nullptr, nullptr, nullptr, count,
+                   stats, &packed);
 }
 
 }  // extern "C"

@@ -58,7 +58,7 @@ struct mpsft_ctx {
   int32_t *h_ctl = nullptr;
   size_t h_ctl_n = 0;
   // pinned staging of exported mode tables
-  unsigned char *h_stage = nullptr;
+  unsigned char *h_stage = nullptr, *d_stage = nullptr;  // mapped pinned
   // pinned, device-mapped staging of a solve's small uploads (copied by a
   // kernel, see Upload), its device address and the bump offset
   unsigned char *h_up = nullptr, *d_up = nullptr;

@@ -173,6 +173,8 @@ __global__ void __launch_bounds__(1024)
     SolveCtl &c = ctl[i];
     SigIter &it = its[i];
     if (it.active) {
+      // this iteration's spilled candidates, after all others (InsertSpills)
+      if (it.flags[4] > 0) InsertSpills(it);
       const int32_t *fl = it.flags;
       c.iter += 1;
       c.near_ties += fl[2];

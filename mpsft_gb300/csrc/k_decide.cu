@@ -213,45 +213,36 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// FP64 decisions on the re-binned values of the listed near-tie bins: one
-// block of W warps per listed bin, kListedBlocks blocks per signal taking
-// every kListedBlocks-th bin. The subtraction of the bin's found modes from
-// row 0 and from each bit's two rows (a long chain of FP64 operations per
-// mode; GB300 has few FP64 pipes, with long latencies) is split over the
-// warps: warp w takes the groups of G consecutive modes w, w + W, ..., loads
-// their terms and row-factor table entries together, and keeps per-lane
-// partial sums; the partials meet in shared memory in warp order, and warp 0
-// decides (energy threshold, then DecideTail). Signals whose list overflowed
-// are redone whole instead (redo), or marked unresolved.
+// The listed near-tie bins of the FP32 pass, decided in FP64 on their
+// re-binned rows. kListedBlocks blocks per signal take every
+// kListedBlocks-th listed bin (k_listed_terms) or group of 8 listed bins
+// (k_decide_listed).
 constexpr int kListedBlocks = 8;
 
 __device__ void MergeBin(const SigIter &it, int beta);
 
+// FP64 mode subtraction of the listed bins, beside their re-binning: one
+// block of W warps per listed bin. The bin's found modes get their FP64
+// row-0 terms (ModeTerms64: two FP64 erf each, long on this part; a thread
+// per mode), then their sum over the bin in every row: row 0 takes the terms
+// themselves, the rows 2s+1, 2s+2 of bit s the terms times the row factor
+// e^{+-2 pi i (B 2^s k1 mod n)/n} (src/binner.cc:584-589), lane s of every
+// warp. Warp w takes the groups of G consecutive modes w, w + W, ..., loads
+// their terms and row-factor table entries together and keeps per-lane
+// partial sums (a long chain of FP64 operations per mode; GB300 has few FP64
+// pipes, with long latencies); the partials meet in shared memory in warp
+// order, into esc_msub. Signals whose list overflowed are redone whole or
+// marked unresolved (k_decide_listed).
 template <int TMAX, int W, int G>
-__global__ void __launch_bounds__(32 * W)
-    k_decide_listed(const SigIter *__restrict__ its, int redo, int merge) {
-  PdlEnter(its, kTraceDecideListed);
+__global__ void __launch_bounds__(32 * W) k_listed_terms(const SigIter *__restrict__ its) {
+  PdlEnter(its, kTraceListedTerms);
   __shared__ double2 s_p0[W][TMAX];
   __shared__ double2 s_pp[W][32][TMAX];
   __shared__ double2 s_pm[W][32][TMAX];
   const SigIter &it = its[blockIdx.y];
-  if (!it.active) return;
-  if (it.force_fp64) return;
+  if (!it.active || it.force_fp64 || it.esc_mask == nullptr) return;
   const int nf = *(volatile int32_t *)&it.flags[2];
-  if (nf > it.esc_cap) {
-    if (!redo && blockIdx.x == 0 && threadIdx.x == 0) {
-      atomicOr(&it.flags[1], kStatusUnresolved);
-    }
-    // unresolved: the held-back bins keep their FP32 candidates
-    if (merge && threadIdx.x == 0) {
-      for (int e = blockIdx.x; e < it.esc_cap; e += kListedBlocks) {
-        const int beta = it.esc_list[e];
-        it.cand_valid[beta] -= kCandListed;
-        MergeBin(it, beta);
-      }
-    }
-    return;
-  }
+  if (nf > it.esc_cap) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int TR = it.trials;
   const bool has_bit = lane < it.bits;
@@ -261,6 +252,11 @@ __global__ void __launch_bounds__(32 * W)
   for (int e = blockIdx.x; e < nf; e += kListedBlocks) {
     const int beta = it.esc_list[e];
     const int nm = it.bkt_count[beta], st = it.bkt_start[beta];
+    for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+      const int sl = it.bkt_list[st + i];
+      ModeTerms64(it, sl, it.mode_k1[sl], it.mode_bin[sl]);
+    }
+    __syncthreads();  // the block's terms are visible to the whole block
     double2 p0[TMAX], pp[TMAX], pm[TMAX];
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
@@ -315,101 +311,106 @@ __global__ void __launch_bounds__(32 * W)
     }
     __syncthreads();
     if (warp == 0) {
-      const FromRebin src{it, e, beta, it.esc_mask[e]};
-      double2 u0[TMAX], up[TMAX], um[TMAX];
-      double en = 0.0;
+      double2 *out = it.esc_msub + size_t(e) * TR * it.rows;
 #pragma unroll
       for (int t = 0; t < TMAX; ++t) {
         if (t < TR) {
-          double2 sum = s_p0[0][t];
+          if (lane == 0) {
+            double2 sum = s_p0[0][t];
 #pragma unroll
-          for (int w = 1; w < W; ++w) sum = cadd(sum, s_p0[w][t]);
-          u0[t] = csub(src.get(t, 0), sum);
-          en += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
-        }
-      }
-      en /= double(TR);
-      // energy threshold on row 0 (src/iterate.cc:114-124)
-      bool go = true;
-      if (!isfinite(en)) {
-        if (lane == 0) {
-          atomicOr(&it.flags[1], kStatusNonFinite);
-          it.cand_valid[beta] = 0;
-        }
-        go = false;
-      } else if (it.bin_thr > 0 && en < it.bin_thr * it.bin_thr) {
-        NoCandidate(it, beta, lane);
-        go = false;
-      }
-      if (go) {
+            for (int w = 1; w < W; ++w) sum = cadd(sum, s_p0[w][t]);
+            out[size_t(t) * it.rows] = sum;
+          }
+          if (has_bit) {
+            double2 sp = s_pp[0][lane][t], sm = s_pm[0][lane][t];
 #pragma unroll
-        for (int t = 0; t < TMAX; ++t) {
-          if (t < TR) {
-            if (has_bit) {
-              double2 sp = s_pp[0][lane][t], sm = s_pm[0][lane][t];
-#pragma unroll
-              for (int w = 1; w < W; ++w) {
-                sp = cadd(sp, s_pp[w][lane][t]);
-                sm = cadd(sm, s_pm[w][lane][t]);
-              }
-              up[t] = csub(src.get(t, 2 * lane + 1), sp);
-              um[t] = csub(src.get(t, 2 * lane + 2), sm);
-            } else {
-              up[t] = um[t] = make_double2(0.0, 0.0);
+            for (int w = 1; w < W; ++w) {
+              sp = cadd(sp, s_pp[w][lane][t]);
+              sm = cadd(sm, s_pm[w][lane][t]);
             }
+            out[size_t(t) * it.rows + 2 * lane + 1] = sp;
+            out[size_t(t) * it.rows + 2 * lane + 2] = sm;
           }
         }
-        DecideTail<double, TMAX>(it, beta, kDecideExact, u0, up, um, 0.f, 0.f,
-                                 false, -1);
       }
-      // the bin's candidate (written by lane 0 above) into the table
-      if (merge && lane == 0) MergeBin(it, beta);
     }
     __syncthreads();  // the partials are rewritten for the next listed bin
   }
 }
 
-// FP64 row-0 terms (ModeTerms64: two FP64 erf, long on this part) of the
-// found modes in the listed bins, for their FP64 decisions: blocks over a
-// signal's listed bins, a thread per mode. Runs on the side stream while the
-// listed bins are re-binned.
-__global__ void __launch_bounds__(128) k_listed_terms(const SigIter *__restrict__ its) {
-  PdlEnter(its, kTraceListedTerms);
+// FP64 decisions of the listed near-tie bins: one warp per listed bin (lane s
+// holds bit s), on the re-binned rows (FromRebin) minus the bin's found modes
+// (esc_msub): energy threshold, then DecideTail, and the bin's candidate into
+// the table. Signals whose list overflowed are redone whole instead (redo),
+// or marked unresolved, their held-back bins keeping their FP32 candidates.
+template <int TMAX>
+__global__ void __launch_bounds__(256)
+    k_decide_listed(const SigIter *__restrict__ its, int redo, int merge) {
+  PdlEnter(its, kTraceDecideListed);
   const SigIter &it = its[blockIdx.y];
-  if (!it.active || it.force_fp64 || it.esc_mask == nullptr) return;
+  if (!it.active) return;
+  if (it.force_fp64) return;
   const int nf = *(volatile int32_t *)&it.flags[2];
-  if (nf > it.esc_cap) return;
-  for (int e = blockIdx.x; e < nf; e += gridDim.x) {
-    const int beta = it.esc_list[e];
-    const int nm = it.bkt_count[beta], st = it.bkt_start[beta];
-    for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-      const int sl = it.bkt_list[st + i];
-      ModeTerms64(it, sl, it.mode_k1[sl], it.mode_bin[sl]);
+  if (nf > it.esc_cap) {
+    if (!redo && blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicOr(&it.flags[1], kStatusUnresolved);
     }
+    if (merge && threadIdx.x == 0) {
+      for (int e = blockIdx.x; e < it.esc_cap; e += kListedBlocks) {
+        const int beta = it.esc_list[e];
+        it.cand_valid[beta] -= kCandListed;
+        MergeBin(it, beta);
+      }
+    }
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const int TR = it.trials;
+  const bool has_bit = lane < it.bits;
+  for (int e = blockIdx.x * 8 + (threadIdx.x >> 5); e < nf; e += kListedBlocks * 8) {
+    const int beta = it.esc_list[e];
+    const FromRebin src{it, e, beta, it.esc_mask[e]};
+    const double2 *ms = it.esc_msub + size_t(e) * TR * it.rows;
+    double2 u0[TMAX], up[TMAX], um[TMAX];
+    double en = 0.0;
+#pragma unroll
+    for (int t = 0; t < TMAX; ++t) {
+      if (t < TR) {
+        u0[t] = csub(src.get(t, 0), __ldcg(&ms[size_t(t) * it.rows]));
+        en += u0[t].x * u0[t].x + u0[t].y * u0[t].y;
+        if (has_bit) {
+          up[t] = csub(src.get(t, 2 * lane + 1),
+                       __ldcg(&ms[size_t(t) * it.rows + 2 * lane + 1]));
+          um[t] = csub(src.get(t, 2 * lane + 2),
+                       __ldcg(&ms[size_t(t) * it.rows + 2 * lane + 2]));
+        } else {
+          up[t] = um[t] = make_double2(0.0, 0.0);
+        }
+      }
+    }
+    en /= double(TR);
+    // energy threshold on row 0 (src/iterate.cc:114-124)
+    bool go = true;
+    if (!isfinite(en)) {
+      if (lane == 0) {
+        atomicOr(&it.flags[1], kStatusNonFinite);
+        it.cand_valid[beta] = 0;
+      }
+      go = false;
+    } else if (it.bin_thr > 0 && en < it.bin_thr * it.bin_thr) {
+      NoCandidate(it, beta, lane);
+      go = false;
+    }
+    if (go) {
+      DecideTail<double, TMAX>(it, beta, kDecideExact, u0, up, um, 0.f, 0.f, false,
+                               -1);
+    }
+    // the bin's candidate (written by lane 0 above) into the table
+    if (merge && lane == 0) MergeBin(it, beta);
   }
 }
 
 // ---------------------------------------------------------------- merge
-__device__ void InsertMode(const SigIter &it, int32_t k0, double2 coef,
-                           double err) {
-  const int cap = it.tab_cap;
-  uint32_t slot = KeySlot(k0, cap);
-  for (int probe = 0; probe < cap; ++probe) {
-    const int32_t prev = atomicCAS(&it.tab_key[slot], kEmptyKey, k0);
-    if (prev == kEmptyKey) {
-      it.occ_list[atomicAdd(it.tab_count, 1)] = int32_t(slot);
-    }
-    if (prev == kEmptyKey || prev == k0) {
-      atomicAdd(&it.tab_coef[slot].x, coef.x);
-      atomicAdd(&it.tab_coef[slot].y, coef.y);
-      if (err != 0.0) atomicAdd(&it.tab_err[slot], err);
-      return;
-    }
-    slot = (slot + 1) & uint32_t(cap - 1);
-  }
-  atomicOr(&it.flags[1], kStatusCapacity);
-}
-
 // Candidate of bin beta -> table. A pending FP32 candidate is finished here
 // in FP64 (src/iterate.cc:139-171): the window response at
 // xi0 = k1/n - (beta + 1/2)/B and its threshold, the average over the
@@ -421,8 +422,13 @@ __device__ void MergeBin(const SigIter &it, int beta) {
   int32_t k0 = it.cand_k0[beta];
   double2 coef = it.cand_coef[beta];
   double err = it.cand_err[beta];
+  const ModN mod{uint32_t(it.n), it.n_inv};
+  // k1 of the candidate (pending: cand_k0 holds it), and whether it lies in
+  // this bin's range
+  const int64_t k1 = v == 2 ? int64_t(k0) : int64_t(mod(int64_t(it.a) * k0 + it.b));
+  const bool own = int64_t(mod.quot(k1 * int64_t(it.bins))) == beta;
   if (v == 2) {
-    const int64_t n = it.n, k1 = k0;
+    const int64_t n = it.n;
     const int B = it.bins;
     // xi0 = k1/n - (beta + 1/2)/B from its exact integer numerator
     // (|num| < 2^53) and 1/(2nB); one FP64 division per candidate (each is a
@@ -435,7 +441,6 @@ __device__ void MergeBin(const SigIter &it, int beta) {
     }
     const double m = double(it.trials * (1 + 2 * it.bits));
     const double scale = 1.0 / (m * wf);  // the average and the window
-    const ModN mod{uint32_t(n), it.n_inv};
     k0 = int32_t(mod(int64_t(it.a_inv) * mod(k1 - it.b)));
     coef = cmul(coef, Phase64(it, -int64_t(it.c) * k0));
     coef = make_double2(coef.x * scale, coef.y * scale);
@@ -446,7 +451,29 @@ __device__ void MergeBin(const SigIter &it, int beta) {
     it.cand_valid[beta] = 1;
   }
   it.flags[0] = 1;
+  if (!own) {
+    const int j = atomicAdd(&it.flags[4], 1);
+    if (j < kSpillCap) {
+      it.spill_beta[j] = beta;
+      it.spill_k0[j] = k0;
+      it.spill_coef[j] = coef;
+      it.spill_err[j] = err;
+      return;
+    }
+    // (a full spill list: added at once, the order of these few additions
+    // then follows the blocks)
+  }
   InsertMode(it, k0, coef, err);
+}
+
+// The spilled candidates of every signal (InsertSpills), after the merges of
+// an iteration that no stop-rule kernel follows.
+__global__ void k_insert_spills(const SigIter *__restrict__ its, int nsig) {
+  PdlEnter();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsig) return;
+  const SigIter &it = its[i];
+  if (it.active && it.flags[4] > 0) InsertSpills(it);
 }
 
 // Candidates -> table, one thread per bin; bins held back for their FP64
@@ -613,23 +640,33 @@ void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
   dim3 grid(kListedBlocks, nsig);
   const int r = redo ? 1 : 0, mg = merge ? 1 : 0;
   if (max_trials <= 1) {
-    Launch(k_decide_listed<1, 8, 4>, grid, 32 * 8, 0, s, d_its, r, mg);
+    Launch(k_decide_listed<1>, grid, 256, 0, s, d_its, r, mg);
   } else if (max_trials <= 5) {
-    Launch(k_decide_listed<5, 4, 2>, grid, 32 * 4, 0, s, d_its, r, mg);
+    Launch(k_decide_listed<5>, grid, 256, 0, s, d_its, r, mg);
   } else {
-    Launch(k_decide_listed<kMaxTrials, 2, 1>, grid, 32 * 2, 0, s, d_its, r, mg);
+    Launch(k_decide_listed<kMaxTrials>, grid, 256, 0, s, d_its, r, mg);
   }
 }
 
-void LaunchListedTerms(const SigIter *d_its, int nsig, cudaStream_t s) {
+void LaunchListedTerms(const SigIter *d_its, int nsig, int max_trials, cudaStream_t s) {
   dim3 grid(kListedBlocks, nsig);
-  Launch(k_listed_terms, grid, 128, 0, s, d_its);
+  if (max_trials <= 1) {
+    Launch(k_listed_terms<1, 8, 4>, grid, 32 * 8, 0, s, d_its);
+  } else if (max_trials <= 5) {
+    Launch(k_listed_terms<5, 4, 2>, grid, 32 * 4, 0, s, d_its);
+  } else {
+    Launch(k_listed_terms<kMaxTrials, 2, 1>, grid, 32 * 2, 0, s, d_its);
+  }
 }
 
 void LaunchMerge(const SigIter *d_its, int nsig, int max_bins,
                  cudaStream_t s) {
   dim3 grid((max_bins + 255) / 256, nsig);
   Launch(k_merge, grid, 256, 0, s, d_its);
+}
+
+void LaunchInsertSpills(const SigIter *d_its, int nsig, cudaStream_t s) {
+  Launch(k_insert_spills, (nsig + 127) / 128, 128, 0, s, d_its, nsig);
 }
 
 void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,
@@ -659,12 +696,12 @@ bool DecideKernelsLaunchable() {
   a = a < e ? a : e;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_decide<double, kMaxTrials>, 256, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_decide<float, kMaxTrials>, 256, 0);
-  int l = 0;
-  int l1 = 0, l5 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, k_decide_listed<kMaxTrials, 2, 1>, 64, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l1, k_decide_listed<1, 8, 4>, 256, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l5, k_decide_listed<5, 4, 2>, 128, 0);
-  l = (l1 > 0 && l5 > 0) ? l : 0;
+  int l = 0, l1 = 0, l5 = 0, d = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, k_listed_terms<kMaxTrials, 2, 1>, 64, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l1, k_listed_terms<1, 8, 4>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l5, k_listed_terms<5, 4, 2>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_decide_listed<kMaxTrials>, 256, 0);
+  l = (l1 > 0 && l5 > 0 && d > 0) ? l : 0;
   return a > 0 && b > 0 && c > 0 && l > 0;
 }
 

@@ -142,9 +142,14 @@ void LaunchDecideListed(const SigIter *d_its, int nsig, int max_trials,
 
 // Candidates -> mode table (mm[k0] += coef).
 void LaunchMerge(const SigIter *d_its, int nsig, int max_bins, cudaStream_t s);
-// FP64 row-0 terms of the listed near-tie bins' found modes (for their FP64
-// decisions), beside the re-binning.
-void LaunchListedTerms(const SigIter *d_its, int nsig, cudaStream_t s);
+// FP64 row-0 terms of the listed near-tie bins' found modes and their sums
+// in every row of the bin (esc_msub, for the FP64 decisions), beside the
+// re-binning.
+void LaunchListedTerms(const SigIter *d_its, int nsig, int max_trials, cudaStream_t s);
+
+// The spilled candidates of each signal into its table (InsertSpills), for
+// iterations that no k_finish follows.
+void LaunchInsertSpills(const SigIter *d_its, int nsig, cudaStream_t s);
 
 // Inserts / accumulates explicit (k0, coef) pairs into one signal's table.
 void LaunchTableInsert(const SigIter *d_it, const int32_t *k0,
