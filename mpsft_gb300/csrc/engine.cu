@@ -1053,9 +1053,14 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     mx_small.bins = small_bins;
     mx_small.m = 1 << FFTLog2(small_bins);
     mx_small.p2 = 0;
+    // (once per distinct window delta; a batch usually shares one)
+    std::vector<double> deltas;
     for (int i = 0; i < nsig; ++i) {
+      const double d = opts[i].window_delta;
+      if (std::find(deltas.begin(), deltas.end(), d) != deltas.end()) continue;
+      deltas.push_back(d);
       for (int32_t bb = min_bins_min | 1; bb <= small_bins; bb += 2) {
-        mx_small.p2 = std::max(mx_small.p2, MakeWindow(bb, opts[i].window_delta).p2);
+        mx_small.p2 = std::max(mx_small.p2, MakeWindow(bb, d).p2);
       }
     }
   }
@@ -1259,13 +1264,12 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   *launches += body_runs * ctx->graph_body_kernels;
   *ctl_out = hc;
-  // leave each RNG as if exactly the used draws had been taken
+  // leave each RNG as if exactly the used draws had been taken: 3 + trials
+  // draws per iteration (DrawTransform's a, b, c, then the q's)
   for (int i = 0; i < nsig; ++i) {
     *rngs[i] = saved[i];
-    for (int32_t j = 0; j < hc[i].iter; ++j) {
-      DrawTransform(rngs[i], int32_t(sigs[i]->n));
-      for (int t = 0; t < opts[i].trials; ++t) rngs[i]->Draw();
-    }
+    const int64_t draws = int64_t(hc[i].iter) * (3 + opts[i].trials);
+    for (int64_t j = 0; j < draws; ++j) rngs[i]->Draw();
   }
   return MPSFT_OK;
 }
@@ -1690,11 +1694,17 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
     if (m > room) st = st ? st : MPSFT_ERR_CAPACITY;
     const int32_t w = std::min(m, room);
-    for (int32_t j = 0; j < w; ++j) {
-      const int32_t s = sorted[i] ? j : order[j];
-      dk[j] = ki[s];
-      dc[2 * j] = ci[s].x;
-      dc[2 * j + 1] = ci[s].y;
+    if (sorted[i]) {
+      // (re, im) pairs of doubles: the staging's layout is the caller's
+      std::memcpy(dk, ki, sizeof(int32_t) * size_t(w));
+      std::memcpy(dc, ci, sizeof(double2) * size_t(w));
+    } else {
+      for (int32_t j = 0; j < w; ++j) {
+        const int32_t s = order[j];
+        dk[j] = ki[s];
+        dc[2 * j] = ci[s].x;
+        dc[2 * j + 1] = ci[s].y;
+      }
     }
     if (packed) {
       packed_off += w;

@@ -519,10 +519,14 @@ __global__ void k_clear_tables(const SigIter *__restrict__ its) {
 }
 
 // The occupied entries of every table into a staging area, signal s at
-// [s * stride, s * stride + count_s), sorted by k0 (one block per signal,
-// bitonic sort of (k0, slot) in shared memory); a table with more entries
-// than the sort holds (only after a capacity status) is written in insertion
-// order and sorted[s] = 0.
+// [s * stride, s * stride + count_s), sorted by k0 (one block per signal).
+// Up to kRankSortMax entries each key's place is its rank, the number of
+// smaller keys (the keys are distinct: one slot per k0), counted by its own
+// thread over the keys in shared memory; larger tables take a bitonic sort of
+// (k0, slot). A table with more entries than the sort holds (only after a
+// capacity status) is written in insertion order and sorted[s] = 0.
+constexpr int kRankSortMax = 4096;
+
 __global__ void __launch_bounds__(1024)
     k_export_tables(const SigIter *__restrict__ its, int32_t *keys,
                     double2 *coefs, int32_t *counts, int32_t *sorted, int stride) {
@@ -540,6 +544,21 @@ __global__ void __launch_bounds__(1024)
       const int sl = it.occ_list[i];
       keys[base + i] = it.tab_key[sl];
       coefs[base + i] = it.tab_coef[sl];
+    }
+    return;
+  }
+  if (cnt <= kRankSortMax) {
+    int32_t *sk32 = reinterpret_cast<int32_t *>(sk);
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      sk32[i] = it.tab_key[it.occ_list[i]];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const int32_t k = sk32[i];
+      int rank = 0;
+      for (int j = 0; j < cnt; ++j) rank += sk32[j] < k ? 1 : 0;
+      keys[base + rank] = k;
+      coefs[base + rank] = it.tab_coef[it.occ_list[i]];
     }
     return;
   }
