@@ -338,30 +338,27 @@ int EnsureHostCtl(mpsft_ctx *ctx, size_t words) {
   return MPSFT_OK;
 }
 
-// Pinned, device-mapped host staging for a call's results: the device writes
-// the solve state and the tables' entries straight into it, so that the call
-// waits once for the graph and its export together.
+// Pinned host staging for a call's results (the solve state and the
+// tables' entries, copied from the device after the graph with one wait).
 int EnsureHostStage(mpsft_ctx *ctx, size_t bytes) {
   if (ctx->h_stage_n >= bytes) return MPSFT_OK;
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   ctx->h_stage = nullptr;
-  ctx->d_stage = nullptr;
   ctx->h_stage_n = 0;
-  MPSFT_CUDA(ctx, cudaHostAlloc(&ctx->h_stage, bytes, cudaHostAllocMapped));
-  void *dp = nullptr;
-  MPSFT_CUDA(ctx, cudaHostGetDevicePointer(&dp, ctx->h_stage, 0));
-  ctx->d_stage = static_cast<unsigned char *>(dp);
+  MPSFT_CUDA(ctx, cudaMallocHost(&ctx->h_stage, bytes));
   ctx->h_stage_n = bytes;
   return MPSFT_OK;
 }
 
-// A solve call's results in the mapped staging: the solve state, then the
-// tables' entry counts, sorted flags, keys and coefficients (max_cap per
-// signal). Offsets from the staging's start, the same for both views.
+// A solve call's results, the same layout on the device (arena) and in the
+// host staging: the solve state, the tables' entry counts and sorted flags,
+// then the packed keys and coefficients (room for max_cap per signal).
 struct ResultStage {
   size_t ctl = 0, counts = 0, sorted = 0, keys = 0, coefs = 0, bytes = 0;
-  int max_cap = 0;
-  ResultStage(int nsig, int cap) : max_cap(cap) {
+  int nsig = 0, max_cap = 0;
+  unsigned char *dev = nullptr;
+  mutable size_t est = 0;  // entries copied with the header (LaunchResults)
+  ResultStage(int n, int cap) : nsig(n), max_cap(cap) {
     auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
     counts = up(ctl + sizeof(SolveCtl) * size_t(nsig));
     sorted = up(counts + sizeof(int32_t) * size_t(nsig));
@@ -369,21 +366,58 @@ struct ResultStage {
     coefs = up(keys + sizeof(int32_t) * size_t(cap) * nsig);
     bytes = up(coefs + sizeof(double2) * size_t(cap) * nsig);
   }
+  size_t entries() const { return size_t(max_cap) * nsig; }
   template <typename T> T *at(unsigned char *base, size_t off) const {
     return reinterpret_cast<T *>(base + off);
   }
 };
 
 // The solve state and every table's entries (k_export_tables) into the
-// staging, on the context's stream.
-void LaunchResults(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
-                   const ResultStage &rs) {
-  unsigned char *d = ctx->d_stage;
-  LaunchCopyMapped(ctx->d_solve_ctl, rs.at<SolveCtl>(d, rs.ctl), sizeof(SolveCtl) * nsig,
-                   ctx->stream);
-  LaunchExportTables(d_its, nsig, rs.max_cap, rs.at<int32_t>(d, rs.keys),
+// device staging, then their copies to the host: the header and the first
+// `est` entries (the last call's count and a quarter more), so that one wait
+// usually covers the results (FinishResults copies any rest).
+int LaunchResults(mpsft_ctx *ctx, const SigIter *d_its, const ResultStage &rs) {
+  size_t *est = &rs.est;
+  unsigned char *d = rs.dev;
+  LaunchCopyMapped(ctx->d_solve_ctl, rs.at<SolveCtl>(d, rs.ctl),
+                   sizeof(SolveCtl) * rs.nsig, ctx->stream);
+  LaunchExportTables(d_its, rs.nsig, rs.max_cap, rs.at<int32_t>(d, rs.keys),
                      rs.at<double2>(d, rs.coefs), rs.at<int32_t>(d, rs.counts),
                      rs.at<int32_t>(d, rs.sorted), ctx->stream);
+  *est = std::min(rs.entries(), std::max<size_t>(ctx->res_est, 256 * size_t(rs.nsig)));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, d, rs.keys, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage + rs.keys, d + rs.keys,
+                                  sizeof(int32_t) * *est, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage + rs.coefs, d + rs.coefs,
+                                  sizeof(double2) * *est, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  return MPSFT_OK;
+}
+
+// After the wait: the entries past the first `est` when the tables grew past
+// the estimate (one more wait), and the next call's estimate.
+int FinishResults(mpsft_ctx *ctx, const ResultStage &rs) {
+  const size_t est = rs.est;
+  const int32_t *counts = rs.at<int32_t>(ctx->h_stage, rs.counts);
+  size_t total = 0;
+  for (int i = 0; i < rs.nsig; ++i) total += size_t(counts[i]);
+  total = std::min(total, rs.entries());
+  if (total > est) {
+    unsigned char *d = rs.dev;
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage + rs.keys + sizeof(int32_t) * est,
+                                    d + rs.keys + sizeof(int32_t) * est,
+                                    sizeof(int32_t) * (total - est),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage + rs.coefs + sizeof(double2) * est,
+                                    d + rs.coefs + sizeof(double2) * est,
+                                    sizeof(double2) * (total - est),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->res_est = total + total / 4 + 256;
+  return MPSFT_OK;
 }
 
 // A solve's small host -> device transfers (iteration descriptors, draw
@@ -1222,7 +1256,8 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
     // the solve state and, for the usual case that every signal has
     // stopped, the results with it: one wait per graph launch
-    LaunchResults(ctx, d_its, nsig, rs);
+    int rc = LaunchResults(ctx, d_its, rs);
+    if (rc) return rc;
     *launches += 2;
     MPSFT_CUDA(ctx, cudaGetLastError());
     MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1362,10 +1397,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   bytes += 2 * sizeof(unsigned long long) * kTimelineCap + 512;
   int max_cap = 1;
   for (int i = 0; i < nsig; ++i) max_cap = std::max(max_cap, shapes[i].tab_cap);
+  // the results' staging (solve state, tables' entries), on the device and
+  // in pinned host memory
+  ResultStage rs(nsig, max_cap);
+  bytes += rs.bytes + 256;
   int rc = EnsureArena(ctx, bytes);
   if (rc) return rc;
-  // the results' mapped staging (solve state, tables' entries)
-  const ResultStage rs(nsig, max_cap);
   rc = EnsureHostStage(ctx, rs.bytes);
   if (rc) return rc;
   rc = EnsureHostCtl(ctx, size_t(kCtlWords) * nsig);
@@ -1382,6 +1419,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   uint32_t *d_trace_count = cv.take<uint32_t>(1);
   ctx->d_draws = cv.take<int32_t>(size_t(nsig) * kDrawChunk * (4 + max_trials_all));
   ctx->d_draw_bq = cv.take<double>(size_t(nsig) * kDrawChunk * max_trials_all * 2);
+  rs.dev = cv.take<unsigned char>(rs.bytes);
   std::vector<SigIter> its(nsig);
   std::vector<int32_t *> ctls(nsig);
   int64_t phase_entries = 1;
@@ -1628,7 +1666,8 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   if (host_loop) {
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_loop1, ctx->stream));
-    LaunchResults(ctx, d_its, nsig, rs);
+    rc = LaunchResults(ctx, d_its, rs);
+    if (rc) return rc;
     launches += 2;
     MPSFT_CUDA(ctx, cudaGetLastError());
   }
@@ -1656,20 +1695,23 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   // the energy pair (FP32) and the upload copies
   launches += 2 + (fp64 ? 0 : 2) + ctx->up_launches;
   // every table's entries (k_export_tables, with the solve state) in the
-  // mapped staging: counts and sorted flags, then max_cap keys and
-  // coefficients per signal
+  // host staging: counts and sorted flags, then the packed keys and
+  // coefficients, signal after signal
   MPSFT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  rc = FinishResults(ctx, rs);
+  if (rc) return rc;
   const int32_t *counts = rs.at<int32_t>(ctx->h_stage, rs.counts);
   const int32_t *sorted = rs.at<int32_t>(ctx->h_stage, rs.sorted);
   const int32_t *h_keys = rs.at<int32_t>(ctx->h_stage, rs.keys);
   const double2 *h_coefs = rs.at<double2>(ctx->h_stage, rs.coefs);
-  const size_t maxc = size_t(max_cap);
+  size_t res_off = 0;  // signal i's entries in the staging
   int64_t packed_off = 0;
   float loop_ms = 0.f;
   MPSFT_CUDA(ctx, cudaEventElapsedTime(&loop_ms, ctx->ev_loop0, ctx->ev_loop1));
   for (int i = 0; i < nsig; ++i) {
-    const int32_t *ki = h_keys + size_t(i) * maxc;
-    const double2 *ci = h_coefs + size_t(i) * maxc;
+    const int32_t *ki = h_keys + res_off;
+    const double2 *ci = h_coefs + res_off;
+    res_off += size_t(counts[i]);
     std::vector<int32_t> order;
     if (!sorted[i]) {
       order.resize(counts[i]);

@@ -58,7 +58,8 @@ struct mpsft_ctx {
   int32_t *h_ctl = nullptr;
   size_t h_ctl_n = 0;
   // pinned staging of exported mode tables
-  unsigned char *h_stage = nullptr, *d_stage = nullptr;  // mapped pinned
+  unsigned char *h_stage = nullptr;  // pinned: a call's results
+  size_t res_est = 0;  // table entries the last solve call exported
   // pinned, device-mapped staging of a solve's small uploads (copied by a
   // kernel, see Upload), its device address and the bump offset
   unsigned char *h_up = nullptr, *d_up = nullptr;

@@ -518,22 +518,36 @@ __global__ void k_clear_tables(const SigIter *__restrict__ its) {
   if (i < kCtlWords) it.flags[i] = 0;
 }
 
-// The occupied entries of every table into a staging area, signal s at
-// [s * stride, s * stride + count_s), sorted by k0 (one block per signal).
-// Up to kRankSortMax entries each key's place is its rank, the number of
-// smaller keys (the keys are distinct: one slot per k0), counted by its own
-// thread over the keys in shared memory; larger tables take a bitonic sort of
-// (k0, slot). A table with more entries than the sort holds (only after a
+// The occupied entries of every table into one packed staging area, signal
+// s at [o_s, o_s + count_s) with o_s the sum of the counts before it (each
+// block adds them up itself), sorted by k0 (one block per signal, bitonic
+// sort of (k0, slot) in shared memory: ranking every key by counting the
+// smaller ones, O(count^2), took 16x longer at the tables of 64 config-2
+// solves); a table with more entries than the sort holds (only after a
 // capacity status) is written in insertion order and sorted[s] = 0.
-constexpr int kRankSortMax = 4096;
-
 __global__ void __launch_bounds__(1024)
-    k_export_tables(const SigIter *__restrict__ its, int32_t *keys,
-                    double2 *coefs, int32_t *counts, int32_t *sorted, int stride) {
+    k_export_tables(const SigIter *__restrict__ its, int nsig, int32_t *keys,
+                    double2 *coefs, int32_t *counts, int32_t *sorted) {
   extern __shared__ unsigned long long sk[];
+  __shared__ long long s_base;
   const SigIter &it = its[blockIdx.x];
   const int cnt = *it.tab_count;
-  const size_t base = size_t(blockIdx.x) * stride;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  {
+    long long part = 0;
+    for (int j = threadIdx.x; j < int(blockIdx.x); j += blockDim.x) {
+      part += *its[j].tab_count;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0 && part != 0) {
+      atomicAdd(reinterpret_cast<unsigned long long *>(&s_base),
+                static_cast<unsigned long long>(part));
+    }
+  }
+  __syncthreads();
+  const size_t base = size_t(s_base);
   const bool fits = cnt <= BucketKeys(it.tab_cap);
   if (threadIdx.x == 0) {
     counts[blockIdx.x] = cnt;
@@ -544,21 +558,6 @@ __global__ void __launch_bounds__(1024)
       const int sl = it.occ_list[i];
       keys[base + i] = it.tab_key[sl];
       coefs[base + i] = it.tab_coef[sl];
-    }
-    return;
-  }
-  if (cnt <= kRankSortMax) {
-    int32_t *sk32 = reinterpret_cast<int32_t *>(sk);
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      sk32[i] = it.tab_key[it.occ_list[i]];
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const int32_t k = sk32[i];
-      int rank = 0;
-      for (int j = 0; j < cnt; ++j) rank += sk32[j] < k ? 1 : 0;
-      keys[base + rank] = k;
-      coefs[base + rank] = it.tab_coef[it.occ_list[i]];
     }
     return;
   }
@@ -615,8 +614,7 @@ void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
   const size_t sm = size_t(BucketKeys(max_cap)) * sizeof(unsigned long long);
   cudaFuncSetAttribute(k_export_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        int(sm));
-  k_export_tables<<<nsig, 1024, sm, s>>>(d_its, keys, coefs, counts, sorted,
-                                         max_cap);
+  k_export_tables<<<nsig, 1024, sm, s>>>(d_its, nsig, keys, coefs, counts, sorted);
 }
 
 void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,

@@ -98,9 +98,10 @@ void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,
 // Empty mode tables and control words of every signal.
 void LaunchClearTables(const SigIter *d_its, int nsig, int max_cap,
                        cudaStream_t s);
-// Occupied table entries of signal s to keys / coefs [s * max_cap, ...),
-// sorted by k0 (sorted[s] = 1; 0: insertion order, the table exceeded half
-// its capacity), their number to counts[s].
+// Occupied table entries of every signal, packed: signal s to keys / coefs
+// [o_s, o_s + counts[s]) with o_s = counts[0] + ... + counts[s - 1], sorted by
+// k0 (sorted[s] = 1; 0: insertion order, the table exceeded half its
+// capacity). max_cap: the largest table capacity.
 void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
                         int32_t *keys, double2 *coefs, int32_t *counts,
                         int32_t *sorted, cudaStream_t s);
