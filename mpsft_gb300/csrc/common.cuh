@@ -100,6 +100,10 @@ struct SigIter {
   double *wt64;
   float2 *wtff;         // wt64 as float-float (hi, lo); may be null
   void *fold;           // FP32: float2, FP64: double2
+  // a second fold buffer of the same size: in the fixed-bins phase the next
+  // iteration (planned ahead) folds into it while this iteration's row
+  // transforms read fold (k_plan swaps the two)
+  void *fold_alt;
   double2 *ubuf;
   // solves and iterations on the FP32 path: the FP32 pass's bins (the row
   // FFT writes here instead of ubuf, which then holds only FP64 bins)

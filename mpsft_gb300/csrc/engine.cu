@@ -254,6 +254,7 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   const size_t cells = size_t(s.trials) * s.rows_cap * s.bins_cap;
   // 16-byte cells: the FP32 path may redo an iteration in FP64
   it->fold = cv.take<double2>(cells);
+  it->fold_alt = s.fp32_bins ? cv.take<double2>(cells) : nullptr;
   it->ubuf = cv.take<double2>(cells);
   it->ubuf32 = s.fp32_bins ? cv.take<float2>(cells) : nullptr;
   it->row_max = cv.take<float>(size_t(s.trials) * s.rows_cap);
@@ -748,6 +749,12 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     LaunchPlan(ahead->ctl, ahead->its_ahead, nsig, ahead->plan_max, ctx->pre, true);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_plan_p, ctx->pre));
     LaunchWindow32(ahead->its_ahead, nsig, mx.p2, ctx->pre);
+    // the next iteration's gather/fold goes into the other fold buffer
+    // (k_plan swapped them), beside all of this iteration
+    LaunchBinFold(ahead->its_ahead, nsig, mx.bins, mx.bits, mx.trials, x_c128, false,
+                  ctx->pre, false,
+                  FoldShapeFor(ctx, mx.tune_bins > 0 ? mx.tune_bins : mx.bins, mx.n,
+                               nsig, x_c128));
   }
   if (!ahead) {
     LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
@@ -795,13 +802,11 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
   if (ahead) {
-    // the next iteration's gather/fold and Bluestein tables (only this
-    // iteration's row FFT, now done, read the fold buffer and the Bluestein
-    // tables)
+    // the next iteration's Bluestein tables once this iteration's row
+    // transforms have read theirs (its gather/fold, into the other fold
+    // buffer, was queued on the prefold stream at the start of the body)
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_p, s));
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->pre, ctx->ev_fork_p, 0));
-    LaunchBinFold(ahead->its_ahead, nsig, mx.bins, mx.bits, mx.trials, x_c128, false,
-                  ctx->pre, false, shape);
     LaunchBluesteinSetup(ahead->its_ahead, nsig, mx.m, false, ctx->tw32, ctx->tw64,
                          ctx->pre);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_p, ctx->pre));

@@ -70,6 +70,13 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     it.active = 0;
     return;
   }
+  if (ahead && it.fold_alt != nullptr) {
+    // the planned iteration folds into the buffer this one's row transforms
+    // do not read
+    void *f = it.fold;
+    it.fold = it.fold_alt;
+    it.fold_alt = f;
+  }
   // Everything that depends on the bins only (and on the signal's constants)
   // stays from the previous iteration when the bins repeat (most late
   // iterations): the window scalars, fixed-point constants and thresholds

@@ -6,8 +6,9 @@
 // Iterate (src/iterate.cc:113-175), IdentifyFreq (src/iterate.cc:44-76) and
 // MatPencil (src/freqid.cc:27-48).
 //
-// k_mode_prep (one thread per table slot) evaluates, once per mode and
-// iteration, what BinInFreq needs from a mode: k1 = (a k0 + b) mod n, its bin,
+// k_mode_prep (threads striding over the occupied slots) evaluates, once per
+// mode and iteration, what BinInFreq needs from a mode: k1 = (a k0 + b) mod n,
+// its bin,
 // the window response wf (two FP64 erf) and, per trial, the row-0 term
 // wf * coef * e^{2 pi i (q k1 + c k0)/n}. k_bucket (one CTA per signal) sorts
 // the slots by bin. k_decide then works with one warp per (bin, signal):
@@ -31,7 +32,7 @@ namespace mpsft {
 namespace {
 
 // ---------------------------------------------------------------- prep
-// One thread per occupied slot (the table's insertion list): k1 = (a k0 + b)
+// Per occupied slot (the table's insertion list): k1 = (a k0 + b)
 // mod n and the mode's bin for the bucketing, and the row-0 term
 // wf c e^{2 pi i (q_t k1 + c k0)/n} of every trial (BinInFreqV1::Run,
 // src/binner.cc:565-591) in FP64 (unit phases from the FP64 tables). The
@@ -47,14 +48,8 @@ __device__ inline float WindowInFreq32(const SigIter &it, int64_t k1, int bin) {
   return 0.5f * (erff(float(np) * it.wf_scale) - erff(float(nm) * it.wf_scale));
 }
 
-__global__ void k_mode_prep(const SigIter *__restrict__ its, int cond) {
-  PdlEnter(its, kTraceModePrep);
-  const SigIter &it = its[blockIdx.y];
-  if (!it.active) return;
-  if (cond && !RedoFP64(it)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *it.tab_count) return;
-  const int s = it.occ_list[i];
+// One occupied slot s of k_mode_prep.
+__device__ void ModePrepSlot(const SigIter &it, int s, int cond) {
   const int32_t key = it.tab_key[s];
   const int64_t n = it.n;
   const int B = it.bins;
@@ -76,6 +71,21 @@ __global__ void k_mode_prep(const SigIter *__restrict__ its, int cond) {
                       8.f * it.eps_rel * sqrtf(wc.x * wc.x + wc.y * wc.y);
   } else {
     ModeTerms64(it, s, k1, bin);
+  }
+}
+
+__global__ void k_mode_prep(const SigIter *__restrict__ its, int cond) {
+  PdlEnter(its, kTraceModePrep);
+  const SigIter &it = its[blockIdx.y];
+  if (!it.active) return;
+  if (cond && !RedoFP64(it)) return;
+  // a few blocks per signal striding over the occupied slots (a grid over
+  // the whole table would flood the SMs with empty blocks at the start of
+  // every iteration, ahead of the other streams' kernels)
+  const int count = *it.tab_count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += gridDim.x * blockDim.x) {
+    ModePrepSlot(it, it.occ_list[i], cond);
   }
 }
 
@@ -619,9 +629,9 @@ void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
 
 void LaunchModePrep(const SigIter *d_its, int nsig, int max_cap, cudaStream_t s,
                     bool cond) {
-  // the occupied count is only known on the device: cover the whole table,
-  // blocks past the count exit at once
-  dim3 grid((max_cap + 255) / 256, nsig);
+  // the occupied count is only known on the device: up to 8 blocks per
+  // signal stride over it (a table holds at most max_cap / 2 entries)
+  dim3 grid(std::min(8, std::max(1, max_cap / 2 / 256)), nsig);
   Launch(k_mode_prep, grid, 256, 0, s, d_its, cond ? 1 : 0);
 }
 

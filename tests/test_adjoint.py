@@ -75,6 +75,26 @@ def test_estimate_matches_oracle(ctx, port):
     assert np.abs(got - want).max() <= 1e-10 * np.abs(want).max()
 
 
+def test_estimate_complex64_config4(ctx, port):
+    """Config 4's input type: the estimate of a complex64 signal (FP64
+    arithmetic on the exactly widened samples) equals that of the same
+    samples in complex128 bit for bit, and the oracle's to FP64 rounding."""
+    n, S = 1 << 20, 200
+    rng = np.random.default_rng(11)
+    k = rng.choice(n, S, replace=False)
+    x64 = _tone_signal(n, k, np.exp(2j * np.pi * rng.random(S)), 1e-6,
+                       rng).astype(np.complex64)
+    su = _setup(ctx, n, 2 * S + 1, 1e-5, 3, 21)
+    s64 = ctx.upload(x64)
+    s128 = ctx.upload(x64.astype(np.complex128))
+    got = ctx.estimate(s64, su, k)
+    assert np.array_equal(got, ctx.estimate(s128, su, k))
+    want = _reference_estimate(port, x64.astype(np.complex128), su, k)
+    assert np.abs(got - want).max() <= 1e-10 * np.abs(want).max()
+    s64.free()
+    s128.free()
+
+
 @pytest.mark.parametrize("n", [1 << 16, 65537])
 def test_adjoint_identity(ctx, n):
     rng = np.random.default_rng(7)
