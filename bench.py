@@ -763,9 +763,10 @@ def run_gpu(args) -> None:
 
     rngs = [m.Rng(SEED_RNG + i) for i in range(G)]
 
+    seeds = np.arange(SEED_RNG, SEED_RNG + G, dtype=np.int32)
+
     def step(profile=False):
-        for i, r in enumerate(rngs):  # every step draws the same transforms
-            r.seed(SEED_RNG + i)
+        m.Rng.seed_many(rngs, seeds)  # every step draws the same transforms
         return ctx.solve_batched(sigs, rngs, opts)
 
     if args.profile_case:
@@ -836,8 +837,7 @@ def run_gpu(args) -> None:
         ready[j].record(copy_stream)
 
     def solve_set(j):
-        for i, r in enumerate(rngs):
-            r.seed(SEED_RNG + i)
+        m.Rng.seed_many(rngs, seeds)
         return ctx.solve_batched(sets[j], rngs, opts)
 
     torch.cuda.synchronize()

@@ -118,6 +118,8 @@ int mpsft_rng_destroy(mpsft_rng *rng);
 /* Reseeds the engine only, as RandomSeed does: a normal draw held back by
  * the normal distribution (the second of a pair) survives the reseed. */
 int mpsft_rng_seed(mpsft_rng *rng, int32_t seed);
+/* rngs[i] reseeded with seeds[i], i < count (mpsft_rng_seed each). */
+int mpsft_rng_seed_many(mpsft_rng *const *rngs, const int32_t *seeds, int32_t count);
 int32_t mpsft_rng_int32(mpsft_rng *rng);
 /* count draws of std::normal_distribution<double> on the same engine (the
  * reference's RandomNormal, src/base.cc:55), into out or discarded (out =

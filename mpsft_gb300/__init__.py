@@ -142,6 +142,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         "mpsft_rng_create": (I, [I32, PP]),
         "mpsft_rng_destroy": (I, [P]),
         "mpsft_rng_seed": (I, [P, I32]),
+        "mpsft_rng_seed_many": (I, [P, P, I32]),
         "mpsft_rng_int32": (I32, [P]),
         "mpsft_rng_normals": (I, [P, I64, P]),
         "mpsft_num_bits": (I32, [I32, I32]),
@@ -219,6 +220,15 @@ class Rng:
 
     def seed(self, s: int) -> None:
         self._lib.mpsft_rng_seed(self._h, int(s))
+
+    @staticmethod
+    def seed_many(rngs: list, seeds) -> None:
+        """Reseeds rngs[i] with seeds[i] in one call."""
+        seeds = np.ascontiguousarray(seeds, np.int32)
+        if seeds.size != len(rngs):
+            raise ValueError("one seed per generator")
+        arr = (ctypes.c_void_p * len(rngs))(*[r._h.value for r in rngs])
+        _check(None, load_library().mpsft_rng_seed_many(arr, _ptr(seeds), len(rngs)))
 
     def int32(self) -> int:
         return int(self._lib.mpsft_rng_int32(self._h))

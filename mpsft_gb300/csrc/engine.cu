@@ -971,7 +971,10 @@ struct DrawTables {
   std::vector<SolveCtl> hc;
   std::vector<int32_t> hd;
   std::vector<double> hb;
-  std::vector<mpsft_rng> saved;
+  // working copies of the callers' generators: the draws come from these,
+  // and the callers' own generators take the used draws afterwards
+  // (mpsft_rng::pending), so that an error leaves them untouched
+  std::vector<mpsft_rng> work;
 };
 
 void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
@@ -984,7 +987,7 @@ void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   dt->hc.assign(nsig, SolveCtl{});
   dt->hd.assign(size_t(nsig) * kDrawChunk * stride, 0);
   dt->hb.assign(nsig * dt->bq_per, 0.0);
-  dt->saved.resize(nsig);
+  dt->work.resize(nsig);
   for (int i = 0; i < nsig; ++i) {
     const mpsft_solve_options &o = opts[i];
     SolveCtl &c = dt->hc[i];
@@ -1005,8 +1008,8 @@ void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     c.draw_base = 0;
     c.draws_avail = kDrawChunk;
     c.last_bins = -1;
-    dt->saved[i] = *rngs[i];
-    FillDraws(rngs[i], int32_t(sigs[i]->n), o.trials, stride,
+    dt->work[i] = *rngs[i];
+    FillDraws(&dt->work[i], int32_t(sigs[i]->n), o.trials, stride,
               dt->hd.data() + size_t(i) * kDrawChunk * stride,
               dt->hb.data() + i * dt->bq_per);
   }
@@ -1065,7 +1068,6 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   std::vector<SolveCtl> &hc = dt->hc;
   std::vector<int32_t> &hd = dt->hd;
   std::vector<double> &hb = dt->hb;
-  const std::vector<mpsft_rng> &saved = dt->saved;
   const size_t bq_per = dt->bq_per;
   for (int i = 0; i < nsig; ++i) hc[i].force_fp64 = force[i];
   {
@@ -1242,7 +1244,6 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       cudaGraphDestroy(g);
       ctx->graph = nullptr;
       ctx->graph_unavailable = true;
-      for (int i = 0; i < nsig; ++i) *rngs[i] = saved[i];
       return kGraphUnavailable;
     }
     ctx->graph_exec = exec;
@@ -1277,7 +1278,7 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       all_done = false;
       if (hc[i].iter - hc[i].draw_base >= hc[i].draws_avail) {
         // the next kDrawChunk iterations continue this signal's RNG stream
-        FillDraws(rngs[i], int32_t(sigs[i]->n), opts[i].trials, stride,
+        FillDraws(&dt->work[i], int32_t(sigs[i]->n), opts[i].trials, stride,
                   hd.data() + size_t(i) * kDrawChunk * stride,
                   hb.data() + i * bq_per);
         const int32_t window[2] = {hc[i].iter, kDrawChunk};
@@ -1304,12 +1305,10 @@ int GraphLoop(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   *launches += body_runs * ctx->graph_body_kernels;
   *ctl_out = hc;
-  // leave each RNG as if exactly the used draws had been taken: 3 + trials
-  // draws per iteration (DrawTransform's a, b, c, then the q's)
+  // each caller's generator takes exactly the used draws, 3 + trials per
+  // iteration (DrawTransform's a, b, c, then the q's), before its next draw
   for (int i = 0; i < nsig; ++i) {
-    *rngs[i] = saved[i];
-    const int64_t draws = int64_t(hc[i].iter) * (3 + opts[i].trials);
-    for (int64_t j = 0; j < draws; ++j) rngs[i]->Draw();
+    rngs[i]->pending += int64_t(hc[i].iter) * (3 + opts[i].trials);
   }
   return MPSFT_OK;
 }
@@ -1470,10 +1469,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     // the host's share of the solve graph runs while the GPU reads x
     if (!host_loop) PrepareDraws(ctx, sigs, opts, nsig, rngs, fp64, &draws);
     rc = ReadEnergy(ctx, d_energy, nsig, &energy);
-    if (rc) {
-      for (int i = 0; i < int(draws.saved.size()); ++i) *rngs[i] = draws.saved[i];
-      return rc;
-    }
+    if (rc) return rc;
   } else if (!host_loop) {
     PrepareDraws(ctx, sigs, opts, nsig, rngs, fp64, &draws);
   }
@@ -1511,10 +1507,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     WinCacheRefs wc;
     if (one_delta) {
       rc = EnsureWinCache(ctx, opts[0].window_delta, bmin, bmax, &wc);
-      if (rc) {
-        for (int i = 0; i < nsig; ++i) *rngs[i] = draws.saved[i];
-        return rc;
-      }
+      if (rc) return rc;
     }
     for (int i = 0; i < nsig; ++i) {
       draws.hc[i].win_base = wc.base;
@@ -1936,7 +1929,7 @@ const char *mpsft_last_error(const mpsft_ctx *ctx) {
 int mpsft_rng_create(int32_t seed, mpsft_rng **out) {
   if (!out) return MPSFT_ERR_INVALID;
   *out = new mpsft_rng;
-  (*out)->eng.seed(seed);
+  (*out)->Seed(seed);
   return MPSFT_OK;
 }
 int mpsft_rng_destroy(mpsft_rng *rng) {
@@ -1947,7 +1940,16 @@ int mpsft_rng_seed(mpsft_rng *rng, int32_t seed) {
   if (!rng) return MPSFT_ERR_INVALID;
   // RandomSeed (src/base.cc:52) reseeds the engine only: a normal draw the
   // distribution holds back (the second of a pair) survives the reseed
-  rng->eng.seed(seed);
+  rng->Seed(seed);
+  return MPSFT_OK;
+}
+int mpsft_rng_seed_many(mpsft_rng *const *rngs, const int32_t *seeds,
+                        int32_t count) {
+  if (count < 0 || (count > 0 && (!rngs || !seeds))) return MPSFT_ERR_INVALID;
+  for (int32_t i = 0; i < count; ++i) {
+    if (!rngs[i]) return MPSFT_ERR_INVALID;
+  }
+  for (int32_t i = 0; i < count; ++i) rngs[i]->Seed(seeds[i]);
   return MPSFT_OK;
 }
 int32_t mpsft_rng_int32(mpsft_rng *rng) { return rng ? rng->Draw() : -1; }
@@ -2936,7 +2938,7 @@ int mpsft_autotune(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
       std::vector<mpsft_rng> rng(nsig);
       std::vector<mpsft_rng *> rp(nsig);
       for (int i = 0; i < nsig; ++i) {
-        rng[i].eng.seed(seed + i);
+        rng[i].Seed(seed + i);
         rp[i] = &rng[i];
       }
       rc = SolveMany(ctx, sigs, opts, nsig, rp.data(), okp.data(), ocp.data(),

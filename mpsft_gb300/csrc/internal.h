@@ -109,8 +109,25 @@ struct mpsft_rng {
   std::mt19937 eng;
   std::uniform_int_distribution<int32_t> uid;
   std::normal_distribution<double> nd;
-  int32_t Draw() { return uid(eng); }
-  double Normal() { return nd(eng); }
+  // integer draws that a batched solve took from a copy of this generator
+  // and that it has not taken itself yet: taken before its next draw (a
+  // reseed drops them)
+  int64_t pending = 0;
+  void CatchUp() {
+    for (; pending > 0; --pending) uid(eng);
+  }
+  int32_t Draw() {
+    CatchUp();
+    return uid(eng);
+  }
+  double Normal() {
+    CatchUp();
+    return nd(eng);
+  }
+  void Seed(int32_t seed) {
+    eng.seed(seed);
+    pending = 0;
+  }
 };
 
 namespace mpsft {

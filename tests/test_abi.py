@@ -31,6 +31,18 @@ def test_rng_matches_reference(lib, golden):
     assert r.int32() == int(golden["rng_123534"][0])
 
 
+def test_rng_seed_many(lib):
+    rngs = [m.Rng(5) for _ in range(3)]
+    for r in rngs:
+        r.int32()
+    m.Rng.seed_many(rngs, [7, 8, 9])
+    for r, s in zip(rngs, [7, 8, 9]):
+        want = m.Rng(s)
+        assert [r.int32() for _ in range(4)] == [want.int32() for _ in range(4)]
+    with pytest.raises(ValueError):
+        m.Rng.seed_many(rngs, [1, 2])
+
+
 @pytest.mark.parametrize("kind", ["port", "ref"])
 def test_rng_reseed_keeps_the_held_normal(lib, kind):
     """RandomSeed (src/base.cc:52) reseeds the engine only: after an odd
