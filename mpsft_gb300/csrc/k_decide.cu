@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
 // One warp per bin. cond: only signals whose iteration is redone in FP64
 // (more near-tie bins than their list holds) take part.
 template <typename T, int TMAX>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && TMAX == 1) ? 6 : 1)
     k_decide(const SigIter *__restrict__ its, int mode, int cond, int mark) {
   PdlEnter(its, kTraceDecide);
   const SigIter &it = its[blockIdx.y];
