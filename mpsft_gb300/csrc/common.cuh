@@ -54,9 +54,13 @@ enum : int32_t {
 
 // FP32 near-tie bound, in units of eps_rel = margin * 2^-24: the bins of a
 // row carry at most kEpsRms * rms + kEpsRowMax * (largest |U| of the row) +
-// kEpsValue * |U| of rounding error (measured on GB300: about 3, 1 and 3.6 at
-// the maximum over 10^6 bins; the margin multiplies these).
-constexpr float kEpsRms = 8.0f;
+// kEpsValue * |U| of rounding error, rms the row's own sqrt(mean |U|^2 / 2)
+// over its bins (the row transform measures it). Measured on GB300 over 240
+// random binnings (n up to 2^22, prime and power of two, 51 to 2001 bins,
+// 20 to 80 dB): the largest error is 1.04 of this sum without the margin
+// (the same as 8 times the signal-wide rms sqrt(mean |x|^2 / (2 bins)), which
+// the rows' own rms is 0.43 to 0.91 of); the margin multiplies it.
+constexpr float kEpsRms = 12.0f;
 constexpr float kEpsRowMax = 1.0f;
 constexpr float kEpsValue = 4.0f;
 
@@ -143,13 +147,12 @@ struct SigIter {
   double *cand_err;
   // FP32 near-tie detection: bins whose decisions lie within eps_u (the
   // a-priori bound on an FP32 bin's rounding error) plus the error carried by
-  // the subtracted modes are listed for FP64 treatment.
-  //   eps = eps_scale * sqrt(*x_energy) with x_energy = mean |x|^2, so that
-  //   eps tracks the bins' rms sqrt(mean|x|^2 / (2 bins)).
-  double eps_scale;     // 0 on the FP64 path
-  const double *x_energy;
-  float *eps_dev;       // eps_scale * sqrt(*x_energy), set by k_bucket
-  float *row_max;       // [t * rows + r]: max |U| of the row (k_row_fft)
+  // the subtracted modes are listed for FP64 treatment. The bound's rms term
+  // of row r is eps_ms * sqrt(row_ms[r]), eps_ms = eps_rel kEpsRms / sqrt(2)
+  // (0 on the FP64 path).
+  float eps_ms;
+  float *row_max;       // [t * rows + r]: max |U| of the row (row transforms)
+  float *row_ms;        // [t * rows + r]: mean |U|^2 over the row's bins
   // re-binning of listed bins: [((e * trials + t) * rows + r) * chunks + c]
   // partial sums over chunk c of the window support
   double2 *esc_part;

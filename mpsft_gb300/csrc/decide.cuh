@@ -340,21 +340,25 @@ __device__ __forceinline__ int DecideTail(const SigIter &it, int beta, int mode,
   // the FP32 binning bound into the coefficient
   double err = 0.0;
   if (!fp32 && mode == kDecideExact) {
-    float rm = 0.f, am = 0.f;
+    float rm = 0.f, am = 0.f, msx = 0.f;
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) {
         const float *r = it.row_max + size_t(t) * rows;
+        const float *ms = it.row_ms + size_t(t) * rows;
         rm = fmaxf(rm, r[0]);
+        msx = fmaxf(msx, ms[0]);
         // magnitudes in FP32 (an error bound needs no more)
         am = fmaxf(am, Abs32(u0[t]));
         if (has_bit) {
           rm = fmaxf(rm, fmaxf(r[2 * lane + 1], r[2 * lane + 2]));
+          msx = fmaxf(msx, fmaxf(ms[2 * lane + 1], ms[2 * lane + 2]));
           am = fmaxf(am, fmaxf(Abs32(up[t]), Abs32(um[t])));
         }
       }
     }
-    float e = *it.eps_dev + it.eps_rel * (kEpsRowMax * rm + kEpsValue * am);
+    float e = it.eps_ms * sqrtf(msx) +
+              it.eps_rel * (kEpsRowMax * rm + kEpsValue * am);
     for (int o = 16; o > 0; o >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
     err = double(e);
   }
@@ -446,19 +450,28 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mode_err += __shfl_xor_sync(0xffffffffu, mode_err, o);
   }
-  // FP32 error bound of this lane's values (see kEpsRms and friends)
-  float eps_base = 0.f, rm0 = 0.f, rml = 0.f;
+  // FP32 error bound of this lane's values (see kEpsRms and friends): the
+  // rows' rms terms (row 0 alone for the energy test, warp-uniform; with the
+  // lane's two rows for its votes and the coefficient), the carried errors
+  float eps_base = 0.f, eps_base0 = 0.f, rm0 = 0.f, rml = 0.f;
   if (fp32) {
-    eps_base = *it.eps_dev + mode_err;
+    float ms0 = 0.f, msl = 0.f;
 #pragma unroll
     for (int t = 0; t < TMAX; ++t) {
       if (t < TR) {
         const float *rm = it.row_max + size_t(t) * rows;
+        const float *ms = it.row_ms + size_t(t) * rows;
         rm0 = fmaxf(rm0, rm[0]);
-        if (has_bit) rml = fmaxf(rml, fmaxf(rm[2 * lane + 1], rm[2 * lane + 2]));
+        ms0 = fmaxf(ms0, ms[0]);
+        if (has_bit) {
+          rml = fmaxf(rml, fmaxf(rm[2 * lane + 1], rm[2 * lane + 2]));
+          msl = fmaxf(msl, fmaxf(ms[2 * lane + 1], ms[2 * lane + 2]));
+        }
       }
     }
     rml = fmaxf(rml, rm0);
+    eps_base0 = it.eps_ms * sqrtf(ms0) + mode_err;
+    eps_base = it.eps_ms * sqrtf(fmaxf(ms0, msl)) + mode_err;
   }
   bool e_near = false;  // energy decision near its threshold (warp-uniform)
 
@@ -485,8 +498,8 @@ __device__ int DecideBin(const SigIter &it, int beta, const Src &src,
       T thr2;
       if (fp32) {
         thr2 = it.bin_thr2_f;
-        const T eps0 = T(eps_base + it.eps_rel * (kEpsRowMax * rm0 +
-                                                  kEpsValue * float(amax)));
+        const T eps0 = T(eps_base0 + it.eps_rel * (kEpsRowMax * rm0 +
+                                                   kEpsValue * float(amax)));
         // |d e| <= 2 max|u0| eps + eps^2, plus the threshold's FP32 rounding
         e_near = fabs(e - thr2) <= T(2) * amax * eps0 + eps0 * eps0 +
                                        thr2 * T(1.2e-7);

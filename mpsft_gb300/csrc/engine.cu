@@ -184,6 +184,10 @@ int CheckN(mpsft_ctx *ctx, int64_t n) {
 // eps / threshold does not depend on the number of bins: it is an SNR test
 // (about 90 dB with the reference's thresholds 3 sigma/sqrt(B), sigma/sqrt(B)).
 constexpr double kPrecisionRatio = 0.01;
+// The policy's mean |x|^2, estimated from 256 evenly spread runs of this
+// many samples (the near-tie bound itself takes each row's own rms, measured
+// by the row transforms, so the policy needs no exact energy)
+constexpr int kPolicySample = 256;
 
 // Precision-policy decision for one signal (FP32 calls): true when its FP32
 // rounding is not small against its noise thresholds. The ratio does not
@@ -191,8 +195,10 @@ constexpr double kPrecisionRatio = 0.01;
 bool PolicyForcesFP64(double margin, int32_t bins, double energy,
                       double bin_thr, double sv_thr) {
   const double m = margin > 0 ? margin : kDefaultNearTieMargin;
-  const double eps =
-      m * kEpsRms * std::ldexp(1.0, -24) / std::sqrt(2.0 * bins) * std::sqrt(energy);
+  // the bound's rms term for a typical row: a row's own rms is about 2/3 of
+  // the signal-wide sqrt(energy / (2 bins))
+  const double eps = m * kEpsRms * (2.0 / 3.0) * std::ldexp(1.0, -24) /
+                     std::sqrt(2.0 * bins) * std::sqrt(energy);
   double scale = 0;
   if (bin_thr > 0) scale = bin_thr;
   if (sv_thr > 0) scale = scale > 0 ? std::min(scale, sv_thr) : sv_thr;
@@ -206,13 +212,13 @@ void SetNearTie(SigIter *it, bool fp64, double margin, int32_t bins,
   it->force_fp64 = force ? 1 : 0;
   if (fp64) {
     it->force_fp64 = 0;
-    it->eps_scale = 0;
+    it->eps_ms = 0;
     it->eps_rel = 0;
     return;
   }
   const double m = margin > 0 ? margin : kDefaultNearTieMargin;
   it->eps_rel = float(m * std::ldexp(1.0, -24));
-  it->eps_scale = m * kEpsRms * std::ldexp(1.0, -24) / std::sqrt(2.0 * bins);
+  it->eps_ms = float(m * kEpsRms * std::ldexp(1.0, -24) / std::sqrt(2.0));
 }
 
 // mean |x|^2 of the signals (device values, one synchronisation)
@@ -258,6 +264,7 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->ubuf = cv.take<double2>(cells);
   it->ubuf32 = s.fp32_bins ? cv.take<float2>(cells) : nullptr;
   it->row_max = cv.take<float>(size_t(s.trials) * s.rows_cap);
+  it->row_ms = cv.take<float>(size_t(s.trials) * s.rows_cap);
   it->chirp32 = cv.take<float2>(s.bins_cap);
   it->chat32 = cv.take<float2>(s.m_cap);
   it->chirp64 = cv.take<double2>(s.bins_cap);
@@ -273,7 +280,6 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->tab_err = cv.take<double>(s.tab_cap);
   it->tab_cap = s.tab_cap;
   it->occ_list = cv.take<int32_t>(s.tab_cap);
-  it->eps_dev = cv.take<float>(1);
   it->mode_bin = cv.take<int32_t>(s.tab_cap);
   it->mode_k1 = cv.take<int32_t>(s.tab_cap);
 
@@ -1430,7 +1436,6 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   for (int i = 0; i < nsig; ++i) {
     std::memset(&its[i], 0, sizeof(SigIter));
     CarveSignal(cv, shapes[i], &its[i], &ctls[i]);
-    its[i].x_energy = d_energy + size_t(kEnergyStride) * i;
     its[i].n = int32_t(sigs[i]->n);
     phase_entries = std::max(phase_entries, PhaseTableEntries(sigs[i]->n));
   }
@@ -1454,7 +1459,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   std::vector<double> energy(nsig, 0.0);
   DrawTables draws;
   if (!fp64) {
-    // mean |x|^2 of every signal scales the FP32 near-tie margin
+    // an estimate of every signal's mean |x|^2 for the precision policy
     std::vector<const void *> h_xs(nsig);
     std::vector<int64_t> h_ns(nsig);
     for (int i = 0; i < nsig; ++i) {
@@ -1465,7 +1470,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     if (rc) return rc;
     rc = Upload(ctx, d_ns, h_ns.data(), sizeof(int64_t) * nsig, ctx->stream);
     if (rc) return rc;
-    LaunchEnergy(d_xs, d_ns, nsig, x_c128, d_energy, ctx->stream);
+    LaunchEnergy(d_xs, d_ns, nsig, x_c128, d_energy, ctx->stream, kPolicySample);
     // the host's share of the solve graph runs while the GPU reads x
     if (!host_loop) PrepareDraws(ctx, sigs, opts, nsig, rngs, fp64, &draws);
     rc = ReadEnergy(ctx, d_energy, nsig, &energy);
@@ -2755,7 +2760,6 @@ int IterateImpl(mpsft_ctx *ctx, const mpsft_signal *sig,
   it.sv_thr = opt->sv_threshold;
   SetThresholdCopies(&it);
   it.win_thr = opt->window_threshold;
-  it.x_energy = d_energy;
   cudaStream_t st = ctx->stream;
   std::vector<double> energy(1, 0.0);
   if (!fp64) {
@@ -2765,7 +2769,7 @@ int IterateImpl(mpsft_ctx *ctx, const mpsft_signal *sig,
                                     cudaMemcpyHostToDevice, st));
     MPSFT_CUDA(ctx, cudaMemcpyAsync(d_ns, &h_n, sizeof(h_n),
                                     cudaMemcpyHostToDevice, st));
-    LaunchEnergy(d_xs, d_ns, 1, sig->dtype == MPSFT_C128, d_energy, st);
+    LaunchEnergy(d_xs, d_ns, 1, sig->dtype == MPSFT_C128, d_energy, st, kPolicySample);
     rc = ReadEnergy(ctx, d_energy, 1, &energy);
     if (rc) return rc;
   }

@@ -116,11 +116,11 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     it.fft_m = 1 << l;
     if (!c.fp64_path) {
       it.eps_rel = float(c.margin * 5.9604644775390625e-08);  // margin * 2^-24
-      it.eps_scale =
-          c.margin * double(kEpsRms) * 5.9604644775390625e-08 / sqrt(2.0 * B);
+      it.eps_ms = float(c.margin * double(kEpsRms) * 5.9604644775390625e-08 *
+                        0.70710678118654752);  // / sqrt(2)
     } else {
       it.eps_rel = 0.f;
-      it.eps_scale = 0.0;
+      it.eps_ms = 0.f;
     }
   }
   const int32_t *d = c.draws + size_t(local) * c.draw_stride;

@@ -128,9 +128,6 @@ __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its
   const int occ = *it.tab_count;
   int *cnt = reinterpret_cast<int *>(keys + BucketKeys(it.tab_cap));
   int *fill = cnt + max_bins;
-  if (threadIdx.x == 0 && it.eps_scale > 0) {
-    *it.eps_dev = float(it.eps_scale * sqrt(*it.x_energy));
-  }
   // shared keys were sized for half the table (BucketKeys); more occupied
   // slots end the solve with a capacity status instead of overflowing
   if (occ > BucketKeys(it.tab_cap)) {

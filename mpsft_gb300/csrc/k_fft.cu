@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(kRowFftThreads)
   }
   __syncthreads();
   BlockFFTDit(a, live ? M : 0, it.fft_log2m, tw, true, tid, nth);
+  float ss = 0.f;  // this thread's share of the row's sum of |U|^2
   if (live && out32) {
     // FP32 bins: exact power-of-two scale, float-float row factor
     const float inv_mf = 1.0f / float(M);
@@ -155,7 +156,9 @@ __global__ void __launch_bounds__(kRowFftThreads)
           const V z = vmul(a[Pad(k)], w[u]);
           const float2 y = make_float2(float(z.x) * inv_mf, float(z.y) * inv_mf);
           dst[k] = MulPhaseFF(y, bh, bl);
-          mx = fmaxf(mx, sqrtf(y.x * y.x + y.y * y.y));
+          const float y2 = y.x * y.x + y.y * y.y;
+          ss += y2;
+          mx = fmaxf(mx, sqrtf(y2));
         }
       }
     }
@@ -178,16 +181,29 @@ __global__ void __launch_bounds__(kRowFftThreads)
         if (k < B) {
           const double2 y = cscale(to_d2(vmul(a[Pad(k)], w[u])), inv_m);
           dst[k] = cmul(bq, y);
-          mx = fmaxf(mx, float(sqrt(y.x * y.x + y.y * y.y)));
+          const double y2 = y.x * y.x + y.y * y.y;
+          ss += float(y2);
+          mx = fmaxf(mx, float(sqrt(y2)));
         }
       }
     }
     // non-negative floats order like their bit patterns
     atomicMax(&row_max_bits[lr], __float_as_uint(mx));
   }
+  // the row's sum of |U|^2 in a fixed order: a shuffle tree over segments of
+  // min(nth, 32) threads (a row's threads are consecutive, nth a power of
+  // two), then the row's segments in order
+  __shared__ float seg_ss[kRowFftThreads / 8];
+  const int seg = nth < 32 ? nth : 32;
+  for (int o = seg >> 1; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & (seg - 1)) == 0) seg_ss[threadIdx.x / seg] = ss;
   __syncthreads();  // (rows past the last only reach the barriers)
   if (live && tid == 0 && it.row_max != nullptr) {
     it.row_max[tr * it.rows + row] = __uint_as_float(row_max_bits[lr]);
+    const int nseg = nth / seg;
+    float t = 0.f;
+    for (int j = 0; j < nseg; ++j) t += seg_ss[lr * nseg + j];
+    it.row_ms[tr * it.rows + row] = t / float(B);
   }
 }
 
@@ -209,6 +225,7 @@ __global__ void __launch_bounds__(64 * kDirectRowsPerBlock)
   __shared__ float2 roots[kDirectMaxBins];
   __shared__ float2 rows[kDirectRowsPerBlock][kDirectMaxBins];
   __shared__ float wmax[2 * kDirectRowsPerBlock];
+  __shared__ float wss[2 * kDirectRowsPerBlock];
   const SigIter &it = its[blockIdx.z];
   if (!it.active) return;
   if (cond ? !RedoFP64(it) : it.force_fp64) return;
@@ -231,7 +248,7 @@ __global__ void __launch_bounds__(64 * kDirectRowsPerBlock)
   }
   __syncthreads();
   const int k = (warp & 1) * 32 + lane;
-  float mx = 0.f;
+  float mx = 0.f, ss = 0.f;
   if (live && k < B) {
     const float2 *f = rows[lr];
     float xr[4] = {0.f, 0.f, 0.f, 0.f}, xi[4] = {0.f, 0.f, 0.f, 0.f};
@@ -277,15 +294,24 @@ __global__ void __launch_bounds__(64 * kDirectRowsPerBlock)
       const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
       it.ubuf[o] = cmul(bq, make_double2(y.x, y.y));
     }
-    mx = sqrtf(y.x * y.x + y.y * y.y);
+    ss = y.x * y.x + y.y * y.y;
+    mx = sqrtf(ss);
   }
-  // the row's largest magnitude: each warp's, then the row's pair of warps
+  // the row's largest magnitude and mean |U|^2: each warp's (a fixed shuffle
+  // tree), then the row's pair of warps
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0) wmax[warp] = mx;
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  }
+  if (lane == 0) {
+    wmax[warp] = mx;
+    wss[warp] = ss;
+  }
   __syncthreads();
   if (live && (warp & 1) == 0 && lane == 0 && it.row_max != nullptr) {
     it.row_max[tr * it.rows + row] = fmaxf(wmax[warp], wmax[warp + 1]);
+    it.row_ms[tr * it.rows + row] = (wss[warp] + wss[warp + 1]) / float(B);
   }
 }
 
@@ -312,8 +338,11 @@ void LaunchRowFFT(const SigIter *d_its, int nsig, int max_rows,
     Launch(k_row_dft_small, g, 64 * kDirectRowsPerBlock, 0, s, d_its, cond ? 1 : 0);
     return;
   }
-  const int rpb_cap =
-      std::max(1, int(int64_t(max_rows) * max_trials * nsig / (2 * 152)));
+  // (a power of two, so that a row's threads are whole shuffle segments)
+  int rpb_cap = 1;
+  while (int64_t(rpb_cap) * 2 <= int64_t(max_rows) * max_trials * nsig / (2 * 152)) {
+    rpb_cap *= 2;
+  }
   const int rpb = std::max(
       1, std::min({kRowsMax, kRowFftThreads * 8 / std::max(1, max_m), rpb_cap}));
   dim3 grid((max_rows + rpb - 1) / rpb, max_trials, nsig);

@@ -199,23 +199,36 @@ namespace mpsft {
 
 namespace {
 
-// Deterministic mean |x|^2: block b of signal s sums a fixed grid-stride
-// share in a fixed tree order, then one block adds the partials in order.
+// Deterministic mean |x|^2: block b of signal s sums a fixed share in a
+// fixed tree order, then one block adds the partials in order. per_block = 0:
+// every sample (grid stride); otherwise block b sums the per_block samples
+// from n b / kEnergyBlocks on (an estimate from kEnergyBlocks evenly spread
+// runs).
 template <typename TX>
 __global__ void k_energy_partial(const void *const *__restrict__ xs,
                                  const int64_t *__restrict__ ns,
-                                 double *__restrict__ energy) {
+                                 double *__restrict__ energy, int per_block) {
   __shared__ double red[256];
   const int sig = blockIdx.y;
   const TX *x = reinterpret_cast<const TX *>(xs[sig]);
   const int64_t n = ns[sig];
   // per-thread sums in FP32 (a few thousand terms), combined in FP64
   float acc = 0.f;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x) {
-    const TX v = x[i];
-    const float re = float(v.x), im = float(v.y);
-    acc = fmaf(re, re, fmaf(im, im, acc));
+  const int64_t run = per_block > 0 ? min(int64_t(per_block), n / kEnergyBlocks) : 0;
+  if (run > 0) {
+    const int64_t start = n * blockIdx.x / kEnergyBlocks;
+    for (int64_t i = threadIdx.x; i < run; i += blockDim.x) {
+      const TX v = x[start + i];
+      const float re = float(v.x), im = float(v.y);
+      acc = fmaf(re, re, fmaf(im, im, acc));
+    }
+  } else {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += int64_t(gridDim.x) * blockDim.x) {
+      const TX v = x[i];
+      const float re = float(v.x), im = float(v.y);
+      acc = fmaf(re, re, fmaf(im, im, acc));
+    }
   }
   red[threadIdx.x] = double(acc);
   __syncthreads();
@@ -227,7 +240,7 @@ __global__ void k_energy_partial(const void *const *__restrict__ xs,
 }
 
 __global__ void k_energy_final(const int64_t *__restrict__ ns,
-                               double *__restrict__ energy) {
+                               double *__restrict__ energy, int per_block) {
   __shared__ double red[kEnergyBlocks];
   const int sig = blockIdx.x;
   double *e = energy + size_t(sig) * kEnergyStride;
@@ -237,20 +250,22 @@ __global__ void k_energy_final(const int64_t *__restrict__ ns,
     if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) e[0] = red[0] / double(ns[sig]);
+  const int64_t n = ns[sig];
+  const int64_t run = per_block > 0 ? min(int64_t(per_block), n / kEnergyBlocks) : 0;
+  if (threadIdx.x == 0) e[0] = red[0] / double(run > 0 ? run * kEnergyBlocks : n);
 }
 
 }  // namespace
 
 void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
-                  double *energy, cudaStream_t s) {
+                  double *energy, cudaStream_t s, int per_block) {
   dim3 grid(kEnergyBlocks, nsig);
   if (c128) {
-    k_energy_partial<double2><<<grid, 256, 0, s>>>(x, n, energy);
+    k_energy_partial<double2><<<grid, 256, 0, s>>>(x, n, energy, per_block);
   } else {
-    k_energy_partial<float2><<<grid, 256, 0, s>>>(x, n, energy);
+    k_energy_partial<float2><<<grid, 256, 0, s>>>(x, n, energy, per_block);
   }
-  k_energy_final<<<nsig, kEnergyBlocks, 0, s>>>(n, energy);
+  k_energy_final<<<nsig, kEnergyBlocks, 0, s>>>(n, energy, per_block);
 }
 
 bool WindowKernelsLaunchable() {

@@ -107,11 +107,12 @@ void LaunchExportTables(const SigIter *d_its, int nsig, int max_cap,
                         int32_t *sorted, cudaStream_t s);
 
 // mean |x|^2 of each signal into energy[sig * kEnergyStride] (two
-// deterministic passes).
+// deterministic passes): over every sample (per_block = 0), or estimated
+// from kEnergyBlocks evenly spread runs of per_block samples.
 constexpr int kEnergyBlocks = 256;
 constexpr int kEnergyStride = kEnergyBlocks + 1;
 void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
-                  double *energy, cudaStream_t s);
+                  double *energy, cudaStream_t s, int per_block = 0);
 
 // Lists of table slots per bin (counting sort by bin).
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
