@@ -80,7 +80,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         list(ex.map(run, cmds))
     if cmds or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+        link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)

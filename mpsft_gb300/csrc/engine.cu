@@ -994,7 +994,7 @@ void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   dt->hd.assign(size_t(nsig) * kDrawChunk * stride, 0);
   dt->hb.assign(nsig * dt->bq_per, 0.0);
   dt->work.resize(nsig);
-  for (int i = 0; i < nsig; ++i) {
+  auto fill = [&](int i) {
     const mpsft_solve_options &o = opts[i];
     SolveCtl &c = dt->hc[i];
     std::memset(&c, 0, sizeof(c));
@@ -1018,7 +1018,19 @@ void PrepareDraws(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     FillDraws(&dt->work[i], int32_t(sigs[i]->n), o.trials, stride,
               dt->hd.data() + size_t(i) * kDrawChunk * stride,
               dt->hb.data() + i * dt->bq_per);
+  };
+  // each signal's draws come from its own generator: the signals are filled
+  // side by side, in chunks, by the context's host threads and this one
+  constexpr int kPoolMin = 16, kPoolWorkers = 3, kChunk = 8;
+  if (nsig < kPoolMin) {
+    for (int i = 0; i < nsig; ++i) fill(i);
+    return;
   }
+  if (!ctx->pool) ctx->pool = std::make_unique<HostPool>(kPoolWorkers);
+  const int chunks = (nsig + kChunk - 1) / kChunk;
+  ctx->pool->Run(chunks, [&](int ch) {
+    for (int i = ch * kChunk; i < std::min(nsig, (ch + 1) * kChunk); ++i) fill(i);
+  });
 }
 
 // The solve as a CUDA graph: a while node whose body is one iteration of

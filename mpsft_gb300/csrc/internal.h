@@ -5,16 +5,92 @@
 
 #include <cuda_runtime.h>
 
+#include <condition_variable>
 #include <cstdint>
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mpsft.h"
 #include "common.cuh"
 
+// A few host threads that run the parts of a call's host work that are
+// independent per signal (the solve graph's draw tables) beside the calling
+// thread. Run(n, fn) calls fn(0) .. fn(n - 1), each once, on the workers and
+// the caller, and returns when all are done.
+class HostPool {
+ public:
+  explicit HostPool(int workers) {
+    for (int w = 0; w < workers; ++w) threads_.emplace_back([this] { Work(); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      stop_ = true;
+    }
+    wake_.notify_all();
+    for (std::thread &t : threads_) t.join();
+  }
+  void Run(int n, const std::function<void(int)> &fn) {
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      fn_ = &fn;
+      n_ = n;
+      next_ = 0;
+      left_ = n;
+      ++gen_;
+    }
+    wake_.notify_all();
+    Drain();
+    std::unique_lock<std::mutex> lock(mu_);
+    done_.wait(lock, [this] { return left_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  void Drain() {
+    for (;;) {
+      int i;
+      const std::function<void(int)> *fn;
+      {
+        std::lock_guard<std::mutex> lock(mu_);
+        if (fn_ == nullptr || next_ >= n_) return;
+        i = next_++;
+        fn = fn_;
+      }
+      (*fn)(i);
+      std::lock_guard<std::mutex> lock(mu_);
+      if (--left_ == 0) done_.notify_all();
+    }
+  }
+  void Work() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lock(mu_);
+        wake_.wait(lock, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+      }
+      Drain();
+    }
+  }
+  std::vector<std::thread> threads_;
+  std::mutex mu_;
+  std::condition_variable wake_, done_;
+  const std::function<void(int)> *fn_ = nullptr;
+  int n_ = 0, next_ = 0, left_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
 struct mpsft_ctx {
   int device = 0;
+  std::unique_ptr<HostPool> pool;  // made at the first large batched solve
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   // second stream, at the highest priority, for the kernels of an iteration
