@@ -491,3 +491,69 @@ def test_iterate_statistics_match_reference(ctx, port, golden, name, prec):
     assert sorted(mm) == sorted(mm_o)
     kk = sorted(mm_o)
     assert coef_err(mm, kk, [mm_o[q] for q in kk]) < (1e-6 if prec == m.FP64 else 1e-2)
+
+
+def test_batched_result_layouts(ctx):
+    """mpsft_solve_batched (one output pair per signal) and
+    mpsft_solve_batched_packed (all signals in one pair, at offsets) give the
+    same modes; a packed output too small for the last signal reports
+    MPSFT_ERR_CAPACITY for it with its full count and a stored prefix, and
+    the signals before it intact."""
+    import ctypes
+    from mpsft_gb300 import SolveOptions, Stats, _ptr
+    from mpsft_gb300.signals import make_signal
+
+    spec = [(1 << 16, 20, 3), (1 << 16, 35, 4), (65537, 15, 5)]
+    sigs, opts = [], []
+    for n, S, seed in spec:
+        sg = make_signal(n, S, 900 + seed, sigma=1e-5)
+        sigs.append(ctx.upload(sg.x))
+        opts.append(ctx.solve_options(S, sg.sigma, min_bins=51, window_delta=1e-5))
+    nsig = len(spec)
+    lib = ctx._lib
+    opt_arr = (SolveOptions * nsig)(*opts)
+    sig_arr = (ctypes.c_void_p * nsig)(*[s._h.value for s in sigs])
+
+    def rng_arr():
+        rngs = [m.Rng(40 + i) for i in range(nsig)]
+        return rngs, (ctypes.c_void_p * nsig)(*[r._h.value for r in rngs])
+
+    cap = 4096
+    ks = [np.zeros(cap, np.int32) for _ in range(nsig)]
+    cs = [np.zeros(cap, np.complex128) for _ in range(nsig)]
+    count = np.zeros(nsig, np.int32)
+    rngs, ra = rng_arr()
+    rc = lib.mpsft_solve_batched(
+        ctx._h, sig_arr, opt_arr, nsig, ra,
+        (ctypes.c_void_p * nsig)(*[k.ctypes.data for k in ks]),
+        (ctypes.c_void_p * nsig)(*[c.ctypes.data for c in cs]),
+        _ptr(np.full(nsig, cap, np.int32)), _ptr(count), (Stats * nsig)())
+    assert rc == m.OK
+    # packed, with room for all
+    total = 3 * cap
+    pk, pc = np.zeros(total, np.int32), np.zeros(total, np.complex128)
+    offs, count2 = np.zeros(nsig + 1, np.int64), np.zeros(nsig, np.int32)
+    rngs, ra = rng_arr()
+    rc = lib.mpsft_solve_batched_packed(ctx._h, sig_arr, opt_arr, nsig, ra, _ptr(pk),
+                                        _ptr(pc), total, _ptr(offs), _ptr(count2),
+                                        (Stats * nsig)())
+    assert rc == m.OK
+    assert np.array_equal(count, count2)
+    for i in range(nsig):
+        a, b = int(offs[i]), int(offs[i + 1])
+        assert b - a == count[i]
+        assert np.array_equal(pk[a:b], ks[i][:count[i]])
+        assert np.array_equal(pc[a:b].view(np.uint64), cs[i][:count[i]].view(np.uint64))
+    # packed, one entry short of the last signal
+    short = int(count[:-1].sum() + count[-1] - 1)
+    offs3, count3 = np.zeros(nsig + 1, np.int64), np.zeros(nsig, np.int32)
+    st3 = (Stats * nsig)()
+    rngs, ra = rng_arr()
+    rc = lib.mpsft_solve_batched_packed(ctx._h, sig_arr, opt_arr, nsig, ra, _ptr(pk),
+                                        _ptr(pc), short, _ptr(offs3), _ptr(count3), st3)
+    assert rc == m.ERR_CAPACITY
+    assert np.array_equal(count3, count)
+    assert [st3[i].status for i in range(nsig)] == [0, 0, m.ERR_CAPACITY]
+    assert offs3[-1] == short and np.array_equal(offs3[:-1], offs[:-1])
+    for s in sigs:
+        s.free()
