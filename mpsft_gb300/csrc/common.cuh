@@ -85,6 +85,7 @@ struct SigIter {
   // (built once per call, see PhaseTableK)
   double2 *ph_lo, *ph_hi;
   int32_t ph_k;
+  int32_t ph_build;  // 1: k_phase_tables fills ph_lo / ph_hi of this signal
   // FP32 copies of the thresholds (the near-tie windows include their rounding)
   float bin_thr2_f, sv_thr_f;
   int32_t trials;

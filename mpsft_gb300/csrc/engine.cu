@@ -291,6 +291,7 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->ph_k = PhaseTableK(s.n);
   it->ph_lo = cv.take<double2>(size_t(1) << it->ph_k);
   it->ph_hi = cv.take<double2>(size_t(PhaseTableHi(s.n)));
+  it->ph_build = 1;
   it->bkt_count = cv.take<int32_t>(s.bins_cap);
   it->bkt_start = cv.take<int32_t>(s.bins_cap);
   it->bkt_list = cv.take<int32_t>(s.tab_cap);
@@ -1451,6 +1452,28 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     its[i].n = int32_t(sigs[i]->n);
     phase_entries = std::max(phase_entries, PhaseTableEntries(sigs[i]->n));
   }
+  // the signals of the first one's length share the context's phase tables
+  // of that length (built once, by the first of them, when the length is
+  // new); other lengths build their own
+  {
+    const int64_t n0 = sigs[0]->n;
+    const size_t lo = size_t(1) << PhaseTableK(n0), hi = size_t(PhaseTableHi(n0));
+    const bool fresh = ctx->ph_cache_n != n0;
+    if (fresh) {
+      if (ctx->ph_cache) cudaFree(ctx->ph_cache);
+      ctx->ph_cache = nullptr;
+      ctx->ph_cache_n = 0;
+      MPSFT_CUDA(ctx, cudaMalloc(&ctx->ph_cache, sizeof(double2) * (lo + hi)));
+    }
+    bool first = true;
+    for (int i = 0; i < nsig; ++i) {
+      if (sigs[i]->n != n0) continue;
+      its[i].ph_lo = ctx->ph_cache;
+      its[i].ph_hi = ctx->ph_cache + lo;
+      its[i].ph_build = fresh && first ? 1 : 0;
+      first = false;
+    }
+  }
   // the call's small uploads (descriptors three times, signal pointers and
   // lengths, draw tables, solve state) fit the staging without a wait
   rc = EnsureUploadStage(
@@ -1466,7 +1489,11 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   rc = Upload(ctx, d_its, its.data(), sizeof(SigIter) * nsig, ctx->stream);
   if (rc) return rc;
   LaunchClearTables(d_its, nsig, max_cap, ctx->stream);
-  LaunchPhaseTables(d_its, nsig, phase_entries, ctx->stream);
+  bool any_phase = false;
+  for (int i = 0; i < nsig; ++i) any_phase |= its[i].ph_build != 0;
+  if (any_phase) LaunchPhaseTables(d_its, nsig, phase_entries, ctx->stream);
+  MPSFT_CUDA(ctx, cudaGetLastError());
+  ctx->ph_cache_n = sigs[0]->n;  // the shared tables are built (or were)
   bool host_loop = ctx->profiling || ctx->graph_unavailable;
   std::vector<double> energy(nsig, 0.0);
   DrawTables draws;
@@ -1708,7 +1735,7 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
   }
   // the call's own kernels outside the loop: table clearing, phase tables,
   // the energy pair (FP32) and the upload copies
-  launches += 2 + (fp64 ? 0 : 2) + ctx->up_launches;
+  launches += 1 + (any_phase ? 1 : 0) + (fp64 ? 0 : 2) + ctx->up_launches;
   // every table's entries (k_export_tables, with the solve state) in the
   // host staging: counts and sorted flags, then the packed keys and
   // coefficients, signal after signal
@@ -1886,6 +1913,7 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->tw32) cudaFree(ctx->tw32);
   if (ctx->tw64) cudaFree(ctx->tw64);
   if (ctx->win_dev) cudaFree(ctx->win_dev);
+  if (ctx->ph_cache) cudaFree(ctx->ph_cache);
   if (ctx->side64) {
     cudaStreamSynchronize(ctx->side64);
     cudaStreamDestroy(ctx->side64);

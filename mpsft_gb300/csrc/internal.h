@@ -166,6 +166,10 @@ struct mpsft_ctx {
   // on first use and kept, like FFT plans (win_dev: block offsets, valid and
   // claim words, then the pool)
   unsigned char *win_dev = nullptr;
+  // FP64 unit-phase tables (ph_lo, then ph_hi) of one signal length, kept
+  // for the next calls of that length
+  double2 *ph_cache = nullptr;
+  int64_t ph_cache_n = 0;
   size_t win_bytes = 0;
   double win_delta = 0.0;
   int32_t win_bmin = 0, win_bmax = 0;

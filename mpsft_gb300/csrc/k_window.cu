@@ -88,6 +88,7 @@ __global__ void k_window32(const SigIter *__restrict__ its) {
 // for h <= (n - 1) >> ph_k, from exact integer phases.
 __global__ void k_phase_tables(const SigIter *__restrict__ its) {
   const SigIter &it = its[blockIdx.y];
+  if (!it.ph_build) return;  // (tables shared with another signal, or cached)
   const int64_t n = it.n;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   double s, c;
@@ -255,17 +256,65 @@ __global__ void k_energy_final(const int64_t *__restrict__ ns,
   if (threadIdx.x == 0) e[0] = red[0] / double(run > 0 ? run * kEnergyBlocks : n);
 }
 
+// The estimate alone (per_block > 0): one block per signal, thread t taking
+// sample t of every run, then the block's fixed tree; a signal shorter than
+// kEnergyBlocks runs of per_block samples is summed whole.
+template <typename TX>
+__global__ void __launch_bounds__(256)
+    k_energy_sample(const void *const *__restrict__ xs, const int64_t *__restrict__ ns,
+                    double *__restrict__ energy, int per_block) {
+  __shared__ double red[256];
+  const int sig = blockIdx.x;
+  const TX *x = reinterpret_cast<const TX *>(xs[sig]);
+  const int64_t n = ns[sig];
+  const int64_t run = min(int64_t(per_block), n / kEnergyBlocks);
+  float acc = 0.f;
+  if (run > 0) {
+    for (int r = 0; r < kEnergyBlocks; ++r) {
+      const int64_t start = n * r / kEnergyBlocks;
+      for (int64_t i = threadIdx.x; i < run; i += blockDim.x) {
+        const TX v = x[start + i];
+        const float re = float(v.x), im = float(v.y);
+        acc = fmaf(re, re, fmaf(im, im, acc));
+      }
+    }
+  } else {
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const TX v = x[i];
+      const float re = float(v.x), im = float(v.y);
+      acc = fmaf(re, re, fmaf(im, im, acc));
+    }
+  }
+  red[threadIdx.x] = double(acc);
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    energy[size_t(sig) * kEnergyStride] = red[0] / double(run > 0 ? run * kEnergyBlocks : n);
+  }
+}
+
 }  // namespace
 
 void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
                   double *energy, cudaStream_t s, int per_block) {
+  if (per_block > 0) {
+    if (c128) {
+      k_energy_sample<double2><<<nsig, 256, 0, s>>>(x, n, energy, per_block);
+    } else {
+      k_energy_sample<float2><<<nsig, 256, 0, s>>>(x, n, energy, per_block);
+    }
+    return;
+  }
   dim3 grid(kEnergyBlocks, nsig);
   if (c128) {
-    k_energy_partial<double2><<<grid, 256, 0, s>>>(x, n, energy, per_block);
+    k_energy_partial<double2><<<grid, 256, 0, s>>>(x, n, energy, 0);
   } else {
-    k_energy_partial<float2><<<grid, 256, 0, s>>>(x, n, energy, per_block);
+    k_energy_partial<float2><<<grid, 256, 0, s>>>(x, n, energy, 0);
   }
-  k_energy_final<<<nsig, kEnergyBlocks, 0, s>>>(n, energy, per_block);
+  k_energy_final<<<nsig, kEnergyBlocks, 0, s>>>(n, energy, 0);
 }
 
 bool WindowKernelsLaunchable() {
