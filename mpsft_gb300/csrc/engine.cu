@@ -767,8 +767,8 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
     LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_blue, ctx->side));
   }
-  LaunchModePrep(d_its, nsig, mx.cap, ctx->side);
-  LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side);
+  // mode preparation and bucketing in one kernel
+  LaunchBucket(d_its, nsig, mx.bins, mx.cap, ctx->side, true);
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
   // FP32 path: the FP64 window tables (for the near-tie re-binning and the
   // FP64 kernels) are built on the low-priority stream and joined only
@@ -827,9 +827,9 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   const bool redo = !fp64 && any_forced && mx.m <= kMaxFFT64;
   const bool side_merge = !fp64 && !redo;
   LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s, false, side_merge);
-  // Bluestein setup, mode preparation, bucketing, window(s), fold, FFT, decide
-  // (ahead: the next iteration's plan in addition)
-  if (launched) *launched += (fp64 ? 7 : 8) + (ahead ? 1 : 0);
+  // Bluestein setup, mode preparation with bucketing, window(s), fold, FFT,
+  // decide (ahead: the next iteration's plan in addition)
+  if (launched) *launched += (fp64 ? 6 : 7) + (ahead ? 1 : 0);
   if (!fp64) {
     // side stream: the listed bins' FP64 mode terms (before any merge
     // changes a coefficient), then the merge of the other bins, beside the
@@ -2494,8 +2494,7 @@ int BinInFreqImpl(mpsft_ctx *ctx, int32_t n, int32_t bins, int32_t bits,
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(it.ubuf, sizeof(double2) * it.bins_cap,
                                     inout, row_bytes, row_bytes, it.rows,
                                     cudaMemcpyHostToDevice, st));
-  LaunchModePrep(d_it, 1, s.tab_cap, st);
-  LaunchBucket(d_it, 1, bins, s.tab_cap, st);
+  LaunchBucket(d_it, 1, bins, s.tab_cap, st, true);
   LaunchDecide(d_it, 1, bins, 1, false, true, st);
   MPSFT_CUDA(ctx, cudaGetLastError());
   MPSFT_CUDA(ctx, cudaMemcpy2DAsync(inout, row_bytes, it.ubuf,

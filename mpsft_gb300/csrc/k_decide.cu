@@ -119,13 +119,21 @@ __device__ void BitonicSort(unsigned long long *keys, int m) {
 // error scale eps. Shared memory: the keys (half the table, BucketKeys),
 // then the bins' counts and fill positions.
 __global__ void __launch_bounds__(1024) k_bucket(const SigIter *__restrict__ its,
-                                                 int max_bins) {
+                                                 int max_bins, int prep) {
   PdlEnter(its, kTraceBucket);
   extern __shared__ unsigned long long keys[];
   const SigIter &it = its[blockIdx.x];
   if (!it.active) return;
   const int B = it.bins;
   const int occ = *it.tab_count;
+  if (prep) {
+    // the mode preparation of k_mode_prep for this signal's slots first
+    // (one kernel fewer at the start of an iteration)
+    for (int i = threadIdx.x; i < occ; i += blockDim.x) {
+      ModePrepSlot(it, it.occ_list[i], 0);
+    }
+    __syncthreads();  // their bins are visible to the whole block
+  }
   int *cnt = reinterpret_cast<int *>(keys + BucketKeys(it.tab_cap));
   int *fill = cnt + max_bins;
   // shared keys were sized for half the table (BucketKeys); more occupied
@@ -639,11 +647,11 @@ inline size_t BucketSmem(int max_cap, int max_bins) {
 }
 
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool prep) {
   const size_t sm = BucketSmem(max_cap, max_bins);
   cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        int(sm));
-  Launch(k_bucket, nsig, 1024, sm, s, d_its, max_bins);
+  Launch(k_bucket, nsig, 1024, sm, s, d_its, max_bins, prep ? 1 : 0);
 }
 
 void LaunchDecide(const SigIter *d_its, int nsig, int max_bins, int max_trials,

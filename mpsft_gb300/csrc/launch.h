@@ -114,9 +114,10 @@ constexpr int kEnergyStride = kEnergyBlocks + 1;
 void LaunchEnergy(const void *const *x, const int64_t *n, int nsig, bool c128,
                   double *energy, cudaStream_t s, int per_block = 0);
 
-// Lists of table slots per bin (counting sort by bin).
+// Lists of table slots per bin (counting sort by bin); prep: the mode
+// preparation of LaunchModePrep first, in the same kernel.
 void LaunchBucket(const SigIter *d_its, int nsig, int max_bins, int max_cap,
-                  cudaStream_t s);
+                  cudaStream_t s, bool prep = false);
 
 // Per-bin mode subtraction, energy test, pencil votes and coefficient
 // estimation (the bin loop of Iterate); writes the candidates. With
