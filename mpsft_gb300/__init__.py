@@ -20,6 +20,7 @@ calls raise.
 """
 from __future__ import annotations
 
+import collections.abc
 import ctypes
 import os
 import weakref
@@ -105,6 +106,28 @@ class Stats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchStats(collections.abc.Sequence):
+    """The Stats of a batched solve, one dict per signal, made when read (a
+    caller that drops them, or reads a few, pays no conversion of the rest)."""
+
+    def __init__(self, arr):
+        self._arr = arr
+
+    def __len__(self) -> int:
+        return len(self._arr)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self._arr[j].as_dict() for j in range(*i.indices(len(self._arr)))]
+        return self._arr[i].as_dict()
+
+    def __eq__(self, other) -> bool:
+        return list(self) == list(other)
+
+    def __repr__(self) -> str:
+        return repr(list(self))
 
 
 _lib = None
@@ -613,7 +636,7 @@ class Context:
     def solve_batched(self, sigs: list, rngs: list, opts: list,
                       cap: int | None = None, raise_on_error: bool = True):
         """Many Demo1::Run solves advanced together. Returns
-        (list of (k, coef) arrays, list of Stats dicts)."""
+        (list of (k, coef) arrays, sequence of Stats dicts: BatchStats)."""
         nsig = len(sigs)
         total = sum(cap or (4 * o.k + 4096) for o in opts)
         if self._out_k.size < total:
@@ -635,7 +658,7 @@ class Context:
         ks, cs = self._out_k[:used].copy(), self._out_c[:used].copy()
         bounds = offs.tolist()
         out = [(ks[a:b], cs[a:b]) for a, b in zip(bounds[:-1], bounds[1:])]
-        return out, [stats[i].as_dict() for i in range(nsig)]
+        return out, BatchStats(stats)
 
 
 @dataclass(eq=False)

@@ -23,6 +23,8 @@ constexpr int kMaxBits = 31;       // rows <= 63; a warp lane per bit in decide
 constexpr int kFoldLanes = 8;      // threads sharing one (row pair, bin)
 constexpr int kMaxFoldsPerLane = 10;  // folds f = p / bins <= 80
 constexpr int kMaxFFT = 16384;     // largest Bluestein transform (FP32)
+constexpr int kMaxFFTLog2 = 14;
+static_assert((1 << kMaxFFTLog2) == kMaxFFT, "transform size");
 constexpr int kMaxFFT64 = 8192;    // largest Bluestein transform (FP64)
 constexpr int32_t kEmptyKey = -1;
 constexpr int kRebinChunks = 16;   // re-binning: at most this many chunks of the support
@@ -387,13 +389,21 @@ struct ModN {
 };
 
 
-// FFT twiddle e of the shared table: e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2,
-// in FP64 and rounded to FP32 (every table of the library is filled by this).
-__device__ inline void TwiddleAt(int e, float2 *tw32, double2 *tw64) {
+// The FFT twiddle table, one block per transform size: W_N^e =
+// e^{-2 pi i e / N} (N = 2^L, 1 <= L <= log2 kMaxFFT, e < N / 2) at entry
+// 2^(L-1) - 1 + e, so that the lanes of a warp read consecutive entries.
+constexpr int kTwiddleEntries = kMaxFFT - 1;
+__host__ __device__ constexpr int TwiddleBase(int log2n) { return (1 << (log2n - 1)) - 1; }
+
+// Entry i of the table, in FP64 and rounded to FP32 (every table of the
+// library is filled by this): e^{-2 pi i k / kMaxFFT} with k = e kMaxFFT / N.
+__device__ inline void TwiddleAt(int i, float2 *tw32, double2 *tw64) {
+  const int L = 32 - __clz(i + 1);  // i + 1 in [2^(L-1), 2^L)
+  const int k = (i - TwiddleBase(L)) << (kMaxFFTLog2 - L);
   double s, c;
-  sincospi(-2.0 * double(e) / double(kMaxFFT), &s, &c);
-  tw64[e] = make_double2(c, s);
-  tw32[e] = make_float2(float(c), float(s));
+  sincospi(-2.0 * double(k) / double(kMaxFFT), &s, &c);
+  tw64[i] = make_double2(c, s);
+  tw32[i] = make_float2(float(c), float(s));
 }
 
 __device__ inline float2 cmulf(float2 a, float2 b) {

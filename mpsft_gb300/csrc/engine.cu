@@ -728,8 +728,8 @@ Maxima MaximaOf(const std::vector<SigIter> &h_its) {
 // some signal of an FP32 call takes the FP64 kernels (precision policy).
 // The fixed-bins phase's pipelined body: while this iteration decides, the
 // next one (descriptors its_ahead) is planned and gathered/folded on the
-// prefold stream. Only the row FFT reads the fold buffer, so the next fold
-// starts once this iteration's FFT is done.
+// prefold stream, into the second fold buffer (only this iteration's row FFT
+// reads the first).
 struct Ahead {
   SigIter *its_ahead;
   SolveCtl *ctl;
@@ -743,25 +743,26 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   if (mx.bins == 0) return MPSFT_OK;
   // fork: tables, mode preparation and bucketing on the side stream while
   // the window and the gather/fold run on the main one; the row FFT waits
-  // for the Bluestein tables only, the decisions for the rest (ahead: this
-  // iteration's tables were set up with its fold, in the previous body)
+  // for the Bluestein tables only, the decisions for the rest (ahead: the
+  // tables are the phase prologue's, and this iteration's fold ran in the
+  // previous body)
   MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork, s));
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
   if (ahead) {
-    // the next iteration's plan and window (at fixed bins they read nothing
-    // this iteration writes; the stop rule waits for the plan) from the start
-    // of the body on the prefold stream; its gather/fold and Bluestein
-    // tables follow this iteration's row FFT, below
+    // the next iteration's plan (at fixed bins it reads nothing this
+    // iteration writes; the stop rule waits for it) and its gather/fold, into
+    // the other fold buffer (k_plan swapped them), from the start of the body
+    // on the prefold stream, beside all of this iteration. Its window and
+    // Bluestein tables are those of the phase's prologue: every iteration of
+    // the phase has min_bins bins.
     MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->pre, ctx->ev_fork, 0));
     LaunchPlan(ahead->ctl, ahead->its_ahead, nsig, ahead->plan_max, ctx->pre, true);
     MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_plan_p, ctx->pre));
-    LaunchWindow32(ahead->its_ahead, nsig, mx.p2, ctx->pre);
-    // the next iteration's gather/fold goes into the other fold buffer
-    // (k_plan swapped them), beside all of this iteration
     LaunchBinFold(ahead->its_ahead, nsig, mx.bins, mx.bits, mx.trials, x_c128, false,
                   ctx->pre, false,
                   FoldShapeFor(ctx, mx.tune_bins > 0 ? mx.tune_bins : mx.bins, mx.n,
                                nsig, x_c128));
+    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_p, ctx->pre));
   }
   if (!ahead) {
     LaunchBluesteinSetup(d_its, nsig, mx.m, fp64, ctx->tw32, ctx->tw64, ctx->side);
@@ -808,16 +809,6 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   if (!ahead) MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_blue, 0));
   LaunchRowFFT(d_its, nsig, mx.rows, mx.trials, mx.m, fp64, ctx->tw32, ctx->tw64,
                s);
-  if (ahead) {
-    // the next iteration's Bluestein tables once this iteration's row
-    // transforms have read theirs (its gather/fold, into the other fold
-    // buffer, was queued on the prefold stream at the start of the body)
-    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_fork_p, s));
-    MPSFT_CUDA(ctx, cudaStreamWaitEvent(ctx->pre, ctx->ev_fork_p, 0));
-    LaunchBluesteinSetup(ahead->its_ahead, nsig, mx.m, false, ctx->tw32, ctx->tw64,
-                         ctx->pre);
-    MPSFT_CUDA(ctx, cudaEventRecord(ctx->ev_join_p, ctx->pre));
-  }
   MPSFT_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));  // join
   // near ties of the FP32 pass: listed bins re-binned and re-decided in
   // FP64; signals that the precision policy sends to FP64 (and signals whose
@@ -828,8 +819,9 @@ int LaunchIterationKernels(mpsft_ctx *ctx, const SigIter *d_its, int nsig,
   const bool side_merge = !fp64 && !redo;
   LaunchDecide(d_its, nsig, mx.bins, mx.trials, !fp64, false, s, false, side_merge);
   // Bluestein setup, mode preparation with bucketing, window(s), fold, FFT,
-  // decide (ahead: the next iteration's plan in addition)
-  if (launched) *launched += (fp64 ? 6 : 7) + (ahead ? 1 : 0);
+  // decide (ahead: the next iteration's plan and fold, bucketing, FP64
+  // window, FFT, decide)
+  if (launched) *launched += ahead ? 6 : (fp64 ? 6 : 7);
   if (!fp64) {
     // side stream: the listed bins' FP64 mode terms (before any merge
     // changes a coefficient), then the merge of the other bins, beside the
@@ -1873,11 +1865,10 @@ int mpsft_ctx_create(int device, mpsft_ctx **out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork_l, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_l, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_m, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork_p, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_plan_p, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join_p, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kMaxFFT / 2);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kMaxFFT / 2);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw32, sizeof(float2) * kTwiddleEntries);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw64, sizeof(double2) * kTwiddleEntries);
   if (e != cudaSuccess) {
     cudaGetLastError();
     delete ctx;
@@ -1938,7 +1929,6 @@ int mpsft_ctx_destroy(mpsft_ctx *ctx) {
   if (ctx->ev_fork_l) cudaEventDestroy(ctx->ev_fork_l);
   if (ctx->ev_join_l) cudaEventDestroy(ctx->ev_join_l);
   if (ctx->ev_join_m) cudaEventDestroy(ctx->ev_join_m);
-  if (ctx->ev_fork_p) cudaEventDestroy(ctx->ev_fork_p);
   if (ctx->ev_plan_p) cudaEventDestroy(ctx->ev_plan_p);
   if (ctx->ev_join_p) cudaEventDestroy(ctx->ev_join_p);
   if (ctx->own) cudaStreamDestroy(ctx->own);

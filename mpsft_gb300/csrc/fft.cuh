@@ -34,18 +34,21 @@ __device__ inline double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
 __device__ inline double2 to_d2(double2 a) { return a; }
 
 // Shared-memory layout of the transforms: element i at Pad(i), one empty
-// slot after every 8 elements, so that the threads of the first DIT / last
-// DIF pass (8 consecutive elements each) hit distinct banks. An array of m
+// slot after every 16 elements. Half a warp's 8-byte accesses then fall on
+// 16 distinct bank pairs in every pass (runs of 16 consecutive elements for
+// spans h >= 16; for smaller spans the groups' strided elements shift by one
+// slot per 16), and on 8 distinct pairs with 16-byte elements. An array of m
 // elements occupies PadLen(m) slots.
-__device__ __forceinline__ int Pad(int i) { return i + (i >> 3); }
-__host__ __device__ inline int PadLen(int m) { return m + (m >> 3) + 1; }
+__device__ __forceinline__ int Pad(int i) { return i + (i >> 4); }
+__host__ __device__ inline int PadLen(int m) { return m + (m >> 4) + 1; }
 
-// W_N^e = e^{-2 pi i e / N} (conjugated for the inverse) from the table
-// tw[e'] = e^{-2 pi i e' / kMaxFFT}, e < N / 2.
+// W_N^e = e^{-2 pi i e / N}, N = 2^log2n, e < N / 2 (conjugated for the
+// inverse), from the size-N block of the twiddle table (TwiddleAt): the
+// consecutive e of a warp's lanes read consecutive entries.
 template <typename V>
-__device__ __forceinline__ V Twiddle(const V *__restrict__ tw, int N, int e,
+__device__ __forceinline__ V Twiddle(const V *__restrict__ tw, int log2n, int e,
                                      bool inverse) {
-  V w = __ldg(&tw[e * (kMaxFFT / N)]);
+  V w = __ldg(&tw[TwiddleBase(log2n) + e]);
   if (inverse) w.y = -w.y;
   return w;
 }
@@ -63,14 +66,14 @@ __device__ __forceinline__ V RotMinusI(V w, bool inverse) {
   return r;
 }
 template <typename V>
-__device__ __forceinline__ void PassTwiddles(const V *__restrict__ tw, int h, int k,
+__device__ __forceinline__ void PassTwiddles(const V *__restrict__ tw, int lh, int k,
                                              int R, bool inverse, V *wb) {
   if (R >= 8) {
-    wb[0] = Twiddle(tw, 8 * h, k, inverse);
-    wb[1] = Twiddle(tw, 8 * h, k + h, inverse);
+    wb[0] = Twiddle(tw, lh + 3, k, inverse);
+    wb[1] = Twiddle(tw, lh + 3, k + (1 << lh), inverse);
   }
-  if (R >= 4) wb[2] = Twiddle(tw, 4 * h, k, inverse);
-  wb[3] = Twiddle(tw, 2 * h, k, inverse);
+  if (R >= 4) wb[2] = Twiddle(tw, lh + 2, k, inverse);
+  wb[3] = Twiddle(tw, lh + 1, k, inverse);
 }
 template <typename V>
 __device__ __forceinline__ V TwStage(const V *wb, int S, int m, bool inverse) {
@@ -91,15 +94,16 @@ __device__ __forceinline__ V TwStage(const V *wb, int S, int m, bool inverse) {
 // same size can run side by side in one block); every thread of the block
 // must call them (each pass ends with a block barrier).
 template <typename V, int R>
-__device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
+__device__ __forceinline__ void DifPass(V *a, int m, int lh, const V *tw,
                                         bool inverse, int tid, int nth) {
   const int groups = m / R;
+  const int h = 1 << lh;
   for (int g = tid; g < groups; g += nth) {
     const int k = g & (h - 1);
-    const int base = (g / h) * (R * h) + k;
+    const int base = ((g >> lh) << lh) * R + k;
     V x[R];
     V wb[4];  // the pass's table twiddles (loads issued with the data)
-    PassTwiddles(tw, h, k, R, inverse, wb);
+    PassTwiddles(tw, lh, k, R, inverse, wb);
 #pragma unroll
     for (int j = 0; j < R; ++j) x[j] = a[Pad(base + j * h)];
     // stages of span S h, S = R/2 .. 1: pairs (j, j + S), twiddle
@@ -122,15 +126,16 @@ __device__ __forceinline__ void DifPass(V *a, int m, int h, const V *tw,
 }
 
 template <typename V, int R>
-__device__ __forceinline__ void DitPass(V *a, int m, int h, const V *tw,
+__device__ __forceinline__ void DitPass(V *a, int m, int lh, const V *tw,
                                         bool inverse, int tid, int nth) {
   const int groups = m / R;
+  const int h = 1 << lh;
   for (int g = tid; g < groups; g += nth) {
     const int k = g & (h - 1);
-    const int base = (g / h) * (R * h) + k;
+    const int base = ((g >> lh) << lh) * R + k;
     V x[R];
     V wb[4];
-    PassTwiddles(tw, h, k, R, inverse, wb);
+    PassTwiddles(tw, lh, k, R, inverse, wb);
 #pragma unroll
     for (int j = 0; j < R; ++j) x[j] = a[Pad(base + j * h)];
     // stages of span S h, S = 1 .. R/2: twiddle W_{2Sh}^{k + (j mod S) h}
@@ -160,13 +165,13 @@ __device__ void BlockFFTDif(V *a, int m, int log2m, const V *__restrict__ tw,
   int left = log2m;
   while (left > 0) {
     const int r = left >= 3 ? 3 : left;
-    const int h = 1 << (left - r);  // smallest span of this pass
+    const int lh = left - r;  // log2 of the smallest span of this pass
     if (r == 3) {
-      DifPass<V, 8>(a, m, h, tw, inverse, tid, nth);
+      DifPass<V, 8>(a, m, lh, tw, inverse, tid, nth);
     } else if (r == 2) {
-      DifPass<V, 4>(a, m, h, tw, inverse, tid, nth);
+      DifPass<V, 4>(a, m, lh, tw, inverse, tid, nth);
     } else {
-      DifPass<V, 2>(a, m, h, tw, inverse, tid, nth);
+      DifPass<V, 2>(a, m, lh, tw, inverse, tid, nth);
     }
     left -= r;
   }
@@ -179,13 +184,13 @@ __device__ void BlockFFTDit(V *a, int m, int log2m, const V *__restrict__ tw,
   int done = 0;
   while (done < log2m) {
     const int r = log2m - done >= 3 ? 3 : log2m - done;
-    const int h = 1 << done;  // smallest span of this pass
+    // (done: log2 of the smallest span of this pass)
     if (r == 3) {
-      DitPass<V, 8>(a, m, h, tw, inverse, tid, nth);
+      DitPass<V, 8>(a, m, done, tw, inverse, tid, nth);
     } else if (r == 2) {
-      DitPass<V, 4>(a, m, h, tw, inverse, tid, nth);
+      DitPass<V, 4>(a, m, done, tw, inverse, tid, nth);
     } else {
-      DitPass<V, 2>(a, m, h, tw, inverse, tid, nth);
+      DitPass<V, 2>(a, m, done, tw, inverse, tid, nth);
     }
     done += r;
   }

@@ -110,7 +110,7 @@ struct mpsft_ctx {
   // fourth stream, at the lowest priority: in the fixed-bins phase, the plan
   // and gather/fold of the next iteration while the current one decides
   cudaStream_t pre = nullptr;
-  cudaEvent_t ev_fork_p = nullptr, ev_plan_p = nullptr, ev_join_p = nullptr;
+  cudaEvent_t ev_plan_p = nullptr, ev_join_p = nullptr;
   cudaEvent_t ev_loop0 = nullptr, ev_loop1 = nullptr;  // timing of the loop
   // stream the solve graph is captured on, and the last instantiated graph
   cudaStream_t cap = nullptr;

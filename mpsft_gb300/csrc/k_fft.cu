@@ -136,12 +136,12 @@ __global__ void __launch_bounds__(kRowFftThreads)
   __syncthreads();
   BlockFFTDit(a, live ? M : 0, it.fft_log2m, tw, true, tid, nth);
   float ss = 0.f;  // this thread's share of the row's sum of |U|^2
+  float mx = 0.f;  // and of its largest |U|
   if (live && out32) {
     // FP32 bins: exact power-of-two scale, float-float row factor
     const float inv_mf = 1.0f / float(M);
     const float2 bh = bq_ff[0], bl = bq_ff[1];
     float2 *dst = it.ubuf32 + (size_t(tr) * it.rows + row) * it.bins_cap;
-    float mx = 0.f;
     for (int k0 = tid; k0 < B; k0 += 8 * nth) {
       V w[8];
 #pragma unroll
@@ -162,12 +162,10 @@ __global__ void __launch_bounds__(kRowFftThreads)
         }
       }
     }
-    atomicMax(&row_max_bits[lr], __float_as_uint(mx));
   } else if (live) {
     const double inv_m = 1.0 / double(M);
     const double2 bq = make_double2(it.bq_re[tr], it.bq_im[tr]);
     double2 *dst = it.ubuf + (size_t(tr) * it.rows + row) * it.bins_cap;
-    float mx = 0.f;
     for (int k0 = tid; k0 < B; k0 += 8 * nth) {
       V w[8];
 #pragma unroll
@@ -187,16 +185,21 @@ __global__ void __launch_bounds__(kRowFftThreads)
         }
       }
     }
-    // non-negative floats order like their bit patterns
-    atomicMax(&row_max_bits[lr], __float_as_uint(mx));
   }
   // the row's sum of |U|^2 in a fixed order: a shuffle tree over segments of
   // min(nth, 32) threads (a row's threads are consecutive, nth a power of
   // two), then the row's segments in order
   __shared__ float seg_ss[kRowFftThreads / 8];
   const int seg = nth < 32 ? nth : 32;
-  for (int o = seg >> 1; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-  if ((threadIdx.x & (seg - 1)) == 0) seg_ss[threadIdx.x / seg] = ss;
+  for (int o = seg >> 1; o > 0; o >>= 1) {
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & (seg - 1)) == 0) {
+    seg_ss[threadIdx.x / seg] = ss;
+    // non-negative floats order like their bit patterns
+    if (live) atomicMax(&row_max_bits[lr], __float_as_uint(mx));
+  }
   __syncthreads();  // (rows past the last only reach the barriers)
   if (live && tid == 0 && it.row_max != nullptr) {
     it.row_max[tr * it.rows + row] = __uint_as_float(row_max_bits[lr]);
@@ -318,10 +321,10 @@ __global__ void __launch_bounds__(64 * kDirectRowsPerBlock)
 }  // namespace
 
 // Shared memory of a block: one padded row of the largest transform, or the
-// rows of smaller ones side by side (at most 4096 + 512 + 64 slots).
+// rows of smaller ones side by side (at most 4096 + 256 + 64 slots).
 inline size_t RowFftSlots(int max_m) {
   const size_t one = size_t(PadLen(max_m));
-  const size_t packed = size_t(kRowFftThreads) * 8 + kRowFftThreads + kRowsMax;
+  const size_t packed = size_t(kRowFftThreads) * 8 + kRowFftThreads / 2 + kRowsMax;
   return one > packed ? one : packed;
 }
 

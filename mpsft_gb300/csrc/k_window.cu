@@ -19,7 +19,7 @@ namespace {
 
 __global__ void k_twiddles(float2 *tw32, double2 *tw64) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= kMaxFFT / 2) return;
+  if (e >= kTwiddleEntries) return;
   TwiddleAt(e, tw32, tw64);
 }
 
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(512)
 }  // namespace
 
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s) {
-  const int n = kMaxFFT / 2;
+  const int n = kTwiddleEntries;
   k_twiddles<<<(n + 255) / 256, 256, 0, s>>>(tw32, tw64);
 }
 

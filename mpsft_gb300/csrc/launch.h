@@ -33,7 +33,7 @@ inline void Launch(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
   cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
 }
 
-// e^{-2 pi i e / kMaxFFT}, e < kMaxFFT/2, for the FFT twiddles.
+// The FFT twiddle table (kTwiddleEntries entries, TwiddleAt).
 void LaunchTwiddles(float2 *tw32, double2 *tw64, cudaStream_t s);
 // dst (device) = src_dev (device address of pinned, mapped host memory), any
 // alignment and size.

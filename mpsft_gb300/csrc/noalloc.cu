@@ -40,8 +40,8 @@ constexpr size_t Align256(size_t v) { return (v + 255) & ~size_t(255); }
 constexpr size_t kOffReady = 0;
 constexpr size_t kOffIter = kOffReady + 256;
 constexpr size_t kOffTw32 = kOffIter + Align256(sizeof(SigIter));
-constexpr size_t kOffTw64 = kOffTw32 + Align256(sizeof(float2) * kMaxFFT / 2);
-constexpr size_t kOffWt32 = kOffTw64 + Align256(sizeof(double2) * kMaxFFT / 2);
+constexpr size_t kOffTw64 = kOffTw32 + Align256(sizeof(float2) * kTwiddleEntries);
+constexpr size_t kOffWt32 = kOffTw64 + Align256(sizeof(double2) * kTwiddleEntries);
 constexpr size_t kOffWt64 = kOffWt32 + Align256(sizeof(float) * (kNaMaxP2 + 1));
 constexpr size_t kOffFold = kOffWt64 + Align256(sizeof(double) * (kNaMaxP2 + 1));
 constexpr size_t kOffChirp =
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(1024)
                     uint32_t *ready) {
   if (threadIdx.x == 0) *dst = it;
   if (*(volatile uint32_t *)ready == kTwiddlesReady) return;
-  for (int e = threadIdx.x; e < kMaxFFT / 2; e += blockDim.x) {
+  for (int e = threadIdx.x; e < kTwiddleEntries; e += blockDim.x) {
     TwiddleAt(e, tw32, tw64);
   }
   __threadfence();
