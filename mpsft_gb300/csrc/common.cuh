@@ -31,6 +31,9 @@ constexpr int kRebinChunks = 16;   // re-binning: at most this many chunks of th
 // chunks of a window support of p samples: runs of at least 16 samples per
 // lane (32 lanes per chunk; a short support spreads over several warps, so
 // that each lane waits for few rounds of gathers), at most kRebinChunks
+constexpr int kStashHeader = 256;   // bytes before a stash buffer's samples
+// samples of a stash buffer at most (per trial: max(p, this))
+constexpr int64_t kStashMaxSamples = int64_t(1) << 20;
 __host__ __device__ inline int RebinChunks(int p) {
   const int c = (p + 511) / 512;
   return c < 1 ? 1 : (c > kRebinChunks ? kRebinChunks : c);
@@ -111,6 +114,15 @@ struct SigIter {
   // iteration (planned ahead) folds into it while this iteration's row
   // transforms read fold (k_plan swaps the two)
   void *fold_alt;
+  // the samples the FP32 fold gathered, for the near-tie re-binning (which
+  // then reads them in order instead of gathering them again from x):
+  // a header word (1: this iteration's fold wrote them, StashRows rows;
+  // 0: it did not) then, for trial tr, stashed row r and -p2 <= t <= p2,
+  // sample (tr StashRows + r) p + t + p2, of the input's type. null when
+  // unused. stash_alt: the second buffer, for the iteration planned ahead
+  // (k_plan swaps the two with fold / fold_alt)
+  unsigned char *stash, *stash_alt;
+  int64_t stash_cap;  // samples per buffer
   double2 *ubuf;
   // solves and iterations on the FP32 path: the FP32 pass's bins (the row
   // FFT writes here instead of ubuf, which then holds only FP64 bins)
@@ -205,6 +217,20 @@ struct SigIter {
   uint32_t *trace_count;
   uint32_t trace_cap;
 };
+
+// The rows whose gathered samples the FP32 fold stashes this iteration (the
+// fold and the re-binning evaluate it alike): every row while the fold
+// gathers from at most an eighth of the signal's samples (the gathers then
+// hit distinct sectors at the random-gather rate, and the sequential writes
+// of the stash take little of the bandwidth), else row 0 alone (read again
+// by every listed bin); 0 without a stash.
+__host__ __device__ inline int StashRows(const SigIter &it) {
+  if (it.stash == nullptr) return 0;
+  const int64_t row = int64_t(it.p) * it.trials;
+  const int64_t all = row * it.rows;
+  if (all <= it.stash_cap && all <= int64_t(it.n) / 8) return it.rows;
+  return row <= it.stash_cap ? 1 : 0;
+}
 
 // Per-signal state of a solve run on the device (k_plan / k_finish). The
 // host fills the configuration and the draw table; the device owns the rest.

@@ -147,12 +147,25 @@ enum DecideMode { kDecide = 0, kSubtractOnly = 1, kDecideExact = 2 };
 // FP64 (relative error below 2^-52, so at most 2^-21 absolute); when the
 // exact value lies within 2^-18 of a half-integer, that FP64 evaluation is
 // used instead so that the rounding is the reference's.
-__device__ inline int64_t RoundK1(int64_t n, int beta, uint32_t xs, int L, int B) {
+// No 64-bit division: with Q = floor(num / 2^{L+1}) (< n B < 2^62),
+// floor(num / den) = floor(Q / B), estimated from psi = round(2^64 / (2B))
+// to within one and corrected exactly.
+__host__ __device__ inline int64_t RoundK1(int64_t n, int beta, uint32_t xs, int L,
+                                           int B, uint64_t psi) {
   const uint64_t den = uint64_t(B) << (L + 1);
   const uint64_t num =
       uint64_t(n) * ((uint64_t(beta) << (L + 1)) + 2 * uint64_t(xs) + 1);
-  const uint64_t q = num / den;
-  const uint64_t r = num - q * den;
+  const uint64_t Q = num >> (L + 1);
+  uint64_t q = MulHi64(2 * Q, psi);  // |2 Q psi / 2^64 - Q / B| < 1/4
+  int64_t rq = int64_t(Q) - int64_t(q * uint64_t(B));
+  if (rq < 0) {
+    --q;
+    rq += B;
+  } else if (rq >= B) {
+    ++q;
+    rq -= B;
+  }
+  const uint64_t r = (uint64_t(rq) << (L + 1)) + (num & ((uint64_t(1) << (L + 1)) - 1));
   const uint64_t d = 2 * r > den ? 2 * r - den : den - 2 * r;  // 2 den |frac - 1/2|
   if (d <= (den >> 17)) {
     const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
@@ -256,7 +269,7 @@ __device__ __forceinline__ int DecideTail(const SigIter &it, int beta, int mode,
   int64_t k1;
   double wf = 0.0;
   if (pending) {
-    k1 = RoundK1(n, beta, xs, L, B);
+    k1 = RoundK1(n, beta, xs, L, B, it.psi);
   } else {
     const double xi1 = ldexp(2.0 * double(xs) + 1.0, -(L + 1));
     k1 = int64_t(round(double(n) * (double(beta) + xi1) / double(B)));

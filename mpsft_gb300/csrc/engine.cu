@@ -251,6 +251,7 @@ struct Shape {
   int32_t m_cap = 0, tab_cap = 0;
   bool fp64 = false;
   bool fp32_bins = false;  // FP32 pass bins in ubuf32 (solves, iterations)
+  int64_t stash_cap = 0;   // complex64 samples per stash buffer (0: none)
 };
 
 void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
@@ -261,6 +262,14 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   // 16-byte cells: the FP32 path may redo an iteration in FP64
   it->fold = cv.take<double2>(cells);
   it->fold_alt = s.fp32_bins ? cv.take<double2>(cells) : nullptr;
+  it->stash = it->stash_alt = nullptr;
+  it->stash_cap = 0;
+  if (s.stash_cap > 0) {
+    const size_t sb = kStashHeader + sizeof(float2) * size_t(s.stash_cap);
+    it->stash = cv.take<unsigned char>(sb);
+    it->stash_alt = cv.take<unsigned char>(sb);
+    it->stash_cap = s.stash_cap;
+  }
   it->ubuf = cv.take<double2>(cells);
   it->ubuf32 = s.fp32_bins ? cv.take<float2>(cells) : nullptr;
   it->row_max = cv.take<float>(size_t(s.trials) * s.rows_cap);
@@ -1394,6 +1403,12 @@ int SolveMany(mpsft_ctx *ctx, const mpsft_signal *const *sigs,
     }
     s.fp64 = fp64;
     s.fp32_bins = !fp64;
+    // complex64 FP32 solves stash the fold's gathered samples (StashRows)
+    if (!fp64 && !x_c128) {
+      s.stash_cap = int64_t(s.trials) *
+                    std::max<int64_t>(2 * int64_t(s.p2_cap) + 1,
+                                      std::min<int64_t>(n / 8, kStashMaxSamples));
+    }
     Carve probe{nullptr};
     SigIter dummy{};
     int32_t *ctl = nullptr;

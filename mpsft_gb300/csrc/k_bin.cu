@@ -235,6 +235,12 @@ __global__ void __launch_bounds__(256, 4)
   const int g = blockIdx.y % gmax;
   const int tr = blockIdx.y / gmax;
   if (tr >= it.trials || g > it.bits) return;
+  // the stash's header: whether this fold stashes its gathered samples (the
+  // pairwise shapes on complex64 input do; the row cluster does not)
+  constexpr bool kStash = !CLUSTER && sizeof(TX) == sizeof(float2);
+  if (it.stash != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    *reinterpret_cast<int32_t *>(it.stash) = kStash ? 1 : 0;
+  }
   const int sc = CLUSTER ? ClusterGroups(it.folds, it.bits) : -1;
   if (g <= sc) {
     // the row cluster on the CTAs of groups 0..sc: a warp per base bin
@@ -276,11 +282,25 @@ __global__ void __launch_bounds__(256, 4)
 
   const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
   const float *__restrict__ wt = it.wt32;
+  // stashed rows of this group (the + row, the - row) and their samples
+  // at t = 0
+  const int srows = kStash ? StashRows(it) : 0;
+  const int rp = g == 0 ? 0 : 2 * g - 1, rm = 2 * g;
+  TX *sp = nullptr, *sm = nullptr;
+  if (rp < srows) {
+    sp = reinterpret_cast<TX *>(it.stash + kStashHeader) +
+         (size_t(tr) * srows + rp) * it.p + it.p2;
+  }
+  if (pair && rm < srows) {
+    sm = reinterpret_cast<TX *>(it.stash + kStashHeader) +
+         (size_t(tr) * srows + rm) * it.p + it.p2;
+  }
   CompF r1, i1, r2, i2;
   for (int k0 = 0; k0 < cnt; k0 += kFoldBatch) {
     TX x1[kFoldBatch], x2[kFoldBatch];
     float w[kFoldBatch];
     uint32_t p32[kFoldBatch];
+    const int64_t tb = t;  // t of the batch's first fold
 #pragma unroll
     for (int u = 0; u < kFoldBatch; ++u) {
       if (k0 + u < cnt) {
@@ -309,6 +329,10 @@ __global__ void __launch_bounds__(256, 4)
           r2.add(v2.x * wr + v2.y * wi);
           i2.add(v2.y * wr - v2.x * wi);
         }
+        // the + row's sample at t, the - row's at -t
+        const int64_t tu = tb + int64_t(u) * D;
+        if (sp != nullptr) sp[tu] = x1[u];
+        if (sm != nullptr) sm[-tu] = x2[u];
       }
     }
   }

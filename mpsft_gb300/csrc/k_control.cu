@@ -71,11 +71,14 @@ __global__ void k_plan(SolveCtl *__restrict__ ctl, SigIter *__restrict__ its,
     return;
   }
   if (ahead && it.fold_alt != nullptr) {
-    // the planned iteration folds into the buffer this one's row transforms
-    // do not read
+    // the planned iteration folds (and stashes its samples) into the
+    // buffers this one's row transforms and re-binning do not read
     void *f = it.fold;
     it.fold = it.fold_alt;
     it.fold_alt = f;
+    unsigned char *st = it.stash;
+    it.stash = it.stash_alt;
+    it.stash_alt = st;
   }
   // Everything that depends on the bins only (and on the signal's constants)
   // stays from the previous iteration when the bins repeat (most late

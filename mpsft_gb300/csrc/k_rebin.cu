@@ -17,6 +17,11 @@
 // from exact integer phases; each block sum then enters an FP64 total through
 // A_blk. The window comes from a float-float table of the FP64 window.
 //
+// The samples x[(a (tau_r + t) + c) mod n] come from the stash the FP32 fold
+// wrote when it stashed the row (StashRows: every row when the fold gathers
+// from few sectors, else row 0), read in order, and are gathered from x
+// again otherwise (random accesses, at the random-gather rate).
+//
 // Work item = (signal, listed bin, trial, listed row, chunk of the support;
 // RebinChunks(p) chunks),
 // one warp each; the 32 lanes split the chunk into consecutive runs; lane sums
@@ -133,15 +138,17 @@ __global__ void __launch_bounds__(256, 2)
        w += int64_t(gridDim.x) * 8) {
     int sig = 0;
     while (w >= items_end[sig]) ++sig;
-    int64_t local = w - (sig > 0 ? items_end[sig - 1] : 0);
+    // (a signal's items: at most kMaxListed * kMaxTrials * rows * chunks,
+    // far below 2^32, so the decode divides in 32 bits)
+    uint32_t local = uint32_t(w - (sig > 0 ? items_end[sig - 1] : 0));
     const SigIter &it = its[sig];
     const int nch = RebinChunks(it.p);
-    const int c = int(local % nch);
-    local /= nch;
-    const int r = int(local % it.rows);
-    local /= it.rows;
-    const int t = int(local % it.trials);
-    const int e = int(local / it.trials);
+    const int c = int(local % uint32_t(nch));
+    local /= uint32_t(nch);
+    const int r = int(local % uint32_t(it.rows));
+    local /= uint32_t(it.rows);
+    const int t = int(local % uint32_t(it.trials));
+    const int e = int(local / uint32_t(it.trials));
     // row not listed (a null mask lists every row)
     if (r > 0 && it.esc_mask != nullptr &&
         !((it.esc_mask[e] >> ((r - 1) >> 1)) & 1u)) {
@@ -182,6 +189,16 @@ __global__ void __launch_bounds__(256, 2)
     pw[lane + 32] = p1;
     __syncwarp();
     double tr = 0.0, ti = 0.0;
+    // the row's samples from the fold's stash when it wrote them (read in
+    // order), else gathered from x
+    const TX *__restrict__ sx = nullptr;
+    if (it.stash != nullptr && __ldcg(reinterpret_cast<const int32_t *>(it.stash)) == 1) {
+      const int srows = StashRows(it);
+      if (r < srows) {
+        sx = reinterpret_cast<const TX *>(it.stash + kStashHeader) +
+             (size_t(t) * srows + r) * it.p + it.p2;
+      }
+    }
     if (t0 < t1) {
       const int64_t twoB = 2 * B;
       const int64_t u0 = mod(tau + t0);
@@ -204,7 +221,7 @@ __global__ void __launch_bounds__(256, 2)
           for (int u = 0; u < 8; ++u) {
             if (kb + u < len) {
               const int64_t tt = tb + kb + u;
-              v[u] = __ldg(&x[j]);
+              v[u] = sx != nullptr ? sx[tt] : __ldg(&x[j]);
               wv[u] = __ldg(&wff[tt < 0 ? -tt : tt]);
               j += astep;
               if (j >= nn) j -= nn;

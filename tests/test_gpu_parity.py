@@ -189,6 +189,50 @@ def test_config2_full_size_matches_oracle(ctx, port, prec):
     assert alg < 1e-2
 
 
+@pytest.mark.parametrize("shape", [6, 8])
+def test_stashed_rebinning_matches_oracle(ctx, port, shape):
+    """The pairwise fold shapes (6: split 4, 8: split 8) stash the samples
+    they gather (row 0 while the fold reads much of the signal, every row
+    once it gathers from few sectors) and the near-tie re-binning reads them
+    instead of gathering them again: the oracle's frequency sets (same
+    draws), coefficients within the FP32 tolerance, and the host-driven loop
+    with the same frequency sets and coefficients within that tolerance."""
+    from mpsft_gb300.signals import make_signal
+
+    sigs, opts, wants, seeds = [], [], [], []
+    for i, (n, s) in enumerate([(1 << 20, 300), (1 << 20, 150)]):
+        sg = make_signal(n, s, 4100 + i, magnitude="loguniform", snr_db=60.0)
+        seeds.append(910 + i)
+        want, _ = port.demo1_run(sg.x.astype(np.complex128), s, sg.sigma, seeds[-1],
+                                 min_bins=51, window_delta=1e-5, max_stale_iter=5)
+        wants.append(want)
+        sigs.append(ctx.upload(sg.x))
+        opts.append(ctx.solve_options(s, sg.sigma, min_bins=51, window_delta=1e-5,
+                                      window_threshold=0.1, max_stale_iter=5,
+                                      precision=m.FP32))
+    try:
+        ctx.set_fold_shape(shape)
+        out, stats = ctx.solve_batched(sigs, [m.Rng(sd) for sd in seeds], opts)
+        assert sum(st["escalated"] for st in stats) > 0  # bins were re-binned
+        for (k, c), want, st in zip(out, wants, stats):
+            assert st["status"] == 0
+            wk = np.array(sorted(want))
+            assert k.tolist() == wk.tolist()
+            got = {int(a): b for a, b in zip(k, c)}
+            assert coef_err(got, wk, [want[kk] for kk in wk]) < TOL_COEF[m.FP32]
+        ctx.set_profiling(True)
+        out2, _ = ctx.solve_batched(sigs, [m.Rng(sd) for sd in seeds], opts)
+        ctx.set_profiling(False)
+        for (k, c), (k2, c2) in zip(out, out2):
+            assert np.array_equal(k, k2)
+            assert np.linalg.norm(c - c2) / np.linalg.norm(c) < TOL_COEF[m.FP32]
+    finally:
+        ctx.set_fold_shape(-1)
+        ctx.set_profiling(False)
+        for sg in sigs:
+            sg.free()
+
+
 def test_batched_equals_single(ctx):
     from mpsft_gb300.signals import make_signal
 
