@@ -308,9 +308,10 @@ void CarveSignal(Carve &cv, const Shape &s, SigIter *it, int32_t **ctl) {
   it->cand_k0 = cv.take<int32_t>(s.bins_cap);
   it->cand_coef = cv.take<double2>(s.bins_cap);
   it->cand_err = cv.take<double>(s.bins_cap);
-  // (the re-binning evaluates the listed bins' step powers itself)
-  it->esc_pow = nullptr;
-  it->esc_step = nullptr;
+  // the listed bins' phase-step powers (s^k, k < 64, and s^64), evaluated
+  // once per bin by the FP32 decide that lists it
+  it->esc_pow = s.fp32_bins ? cv.take<float4>(size_t(kMaxListed) * 64) : nullptr;
+  it->esc_step = s.fp32_bins ? cv.take<double2>(kMaxListed) : nullptr;
   it->esc_list = cv.take<int32_t>(kMaxListed);
   it->esc_mask = cv.take<uint32_t>(kMaxListed);
   it->esc_cap = kMaxListed;

@@ -219,12 +219,17 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && TMAX == 1) ? 6 : 1)
   } else {
     e = DecideBin<T, TMAX>(it, beta, FromBins{it, beta}, mode);
   }
-  // a listed near tie: its re-binning's arrival counters cleared; with mark,
-  // the bin's candidate is held back from the merge (cand_valid +
-  // kCandListed) until its FP64 decision
+  // a listed near tie: with mark, the bin's candidate is held back from the
+  // merge (cand_valid + kCandListed) until its FP64 decision; its
+  // re-binning's arrival counters cleared and (solves and iterations) its
+  // phase-step powers evaluated, once for all the re-binning's work items
   if (e >= 0) {
     if (mark && (threadIdx.x & 31) == 0) it.cand_valid[beta] += kCandListed;
-    ClearListedBin(it, e, threadIdx.x & 31);
+    if (it.esc_pow != nullptr) {
+      PrepListedBin(it, e, beta, threadIdx.x & 31);
+    } else {
+      ClearListedBin(it, e, threadIdx.x & 31);
+    }
   }
 }
 

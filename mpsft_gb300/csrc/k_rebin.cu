@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(256, 2)
     const int64_t t0 = c0 + lane * per;
     const int64_t t1 = min(t0 + per, c1);
     // the bin's phase-step powers s^k (k < 64) into shared memory and s^64
-    // (StepPowers): evaluated here in a solve, from the per-bin tables in the
-    // direct evaluation of every bin
+    // (StepPowers): from the per-bin tables its preparation filled, else
+    // evaluated here
     const int64_t g = 2 * int64_t(beta) + 1;
     const uint32_t bm = mod(it.b);
     float4 p0, p1;

@@ -43,8 +43,7 @@ __device__ inline double2 PowerOfStep(const SigIter &it, int64_t k, uint32_t b,
 }
 
 // Listed bin e: its (trial, row) arrival counters cleared, by the lanes of
-// one warp. In a solve the re-binning evaluates the bin's phase-step powers
-// itself, beside each work item's own start phase.
+// one warp.
 __device__ inline void ClearListedBin(const SigIter &it, int e, int lane) {
   for (int i = lane; i < it.trials * it.rows; i += 32) {
     it.esc_cnt[size_t(e) * it.trials * it.rows + i] = 0;
@@ -69,8 +68,10 @@ __device__ inline void StepPowers(const SigIter &it, int beta, int lane, float4 
   *p1 = make_float4(zr.hi, zi.hi, zr.lo, zi.lo);
 }
 
-// The direct evaluation of every bin (no solve tables, FP64 sincospi per
-// power): the powers once per bin into esc_pow / esc_step, and the counters.
+// A listed bin's preparation: its counters, and its phase-step powers once
+// into esc_pow / esc_step (by the FP32 decide that lists it; for the direct
+// evaluation of every bin, without solve tables, by k_rebin_prep with an
+// FP64 sincospi per power).
 __device__ __noinline__ void PrepListedBin(const SigIter &it, int e, int beta,
                                            int lane) {
   ClearListedBin(it, e, lane);
