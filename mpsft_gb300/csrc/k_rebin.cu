@@ -87,6 +87,61 @@ __device__ __forceinline__ void SampleTimesWindow(double2 v, float2 w, FF *re,
   *im = FFOf(v.y * wd);
 }
 
+// The samples t0 <= t < t1 of a work item summed against the bin's phase
+// steps (s^k in pw, s^64 in S, e^{2 pi i phi(t0)} = (ar, ai)) into (tr, ti).
+// FROM_STASH: the samples read in order from the fold's stash (src[t]);
+// else gathered, x[j] with j stepping by a mod n. The two are separate loops,
+// so that each keeps its eight loads in flight together.
+template <typename TX, bool FROM_STASH>
+__device__ __forceinline__ void SumRun(const TX *__restrict__ src, uint32_t j,
+                                       uint32_t astep, uint32_t nn,
+                                       const float2 *__restrict__ wff,
+                                       const float4 *pw, int64_t t0, int64_t t1,
+                                       double2 S, double ar, double ai, double *tr,
+                                       double *ti) {
+  for (int64_t tb = t0; tb < t1; tb += kPowLen) {
+    const int len = int(min(int64_t(kPowLen), t1 - tb));
+    FF sr{0.f, 0.f}, si{0.f, 0.f};
+    for (int kb = 0; kb < len; kb += 8) {
+      TX v[8];
+      float2 wv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (kb + u < len) {
+          const int64_t tt = tb + kb + u;
+          if (FROM_STASH) {
+            v[u] = __ldg(&src[tt]);
+          } else {
+            v[u] = __ldg(&src[j]);
+            j += astep;
+            if (j >= nn) j -= nn;
+          }
+          wv[u] = __ldg(&wff[tt < 0 ? -tt : tt]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (kb + u < len) {
+          FF xr, xi;
+          SampleTimesWindow(v[u], wv[u], &xr, &xi);
+          const float4 p = pw[kb + u];
+          const FF pr{p.x, p.z}, pi{p.y, p.w};
+          // (xr + i xi)(pr + i pi)
+          AccFF(sr, DotFF(xr, pr, Neg(xi), pi));
+          AccFF(si, DotFF(xr, pi, xi, pr));
+        }
+      }
+    }
+    const double br = double(sr.hi) + double(sr.lo);
+    const double bi = double(si.hi) + double(si.lo);
+    *tr += ar * br - ai * bi;
+    *ti += ar * bi + ai * br;
+    const double nar = ar * S.x - ai * S.y;
+    ai = ar * S.y + ai * S.x;
+    ar = nar;
+  }
+}
+
 // The preparation of the direct evaluation of every bin (mpsft_bin_in_time,
 // FP64_DIRECT): one warp per listed bin. A solve's FP32 decide kernel
 // prepares its listed bins itself when it lists them.
@@ -208,45 +263,12 @@ __global__ void __launch_bounds__(256, 2)
       const int64_t m0 = mod(int64_t(bm) * u0);
       const int64_t r0 = PosMod(g * t0, twoB);
       const double2 a0 = StepPhase(it, m0, r0);
-      double ar = a0.x, ai = a0.y;
-      const TX *__restrict__ x = reinterpret_cast<const TX *>(it.x);
-      const float2 *__restrict__ wff = it.wtff;
-      for (int64_t tb = t0; tb < t1; tb += kPowLen) {
-        const int len = int(min(int64_t(kPowLen), t1 - tb));
-        FF sr{0.f, 0.f}, si{0.f, 0.f};
-        for (int kb = 0; kb < len; kb += 8) {
-          TX v[8];
-          float2 wv[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            if (kb + u < len) {
-              const int64_t tt = tb + kb + u;
-              v[u] = sx != nullptr ? sx[tt] : __ldg(&x[j]);
-              wv[u] = __ldg(&wff[tt < 0 ? -tt : tt]);
-              j += astep;
-              if (j >= nn) j -= nn;
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            if (kb + u < len) {
-              FF xr, xi;
-              SampleTimesWindow(v[u], wv[u], &xr, &xi);
-              const float4 p = pw[kb + u];
-              const FF pr{p.x, p.z}, pi{p.y, p.w};
-              // (xr + i xi)(pr + i pi)
-              AccFF(sr, DotFF(xr, pr, Neg(xi), pi));
-              AccFF(si, DotFF(xr, pi, xi, pr));
-            }
-          }
-        }
-        const double br = double(sr.hi) + double(sr.lo);
-        const double bi = double(si.hi) + double(si.lo);
-        tr += ar * br - ai * bi;
-        ti += ar * bi + ai * br;
-        const double nar = ar * S.x - ai * S.y;
-        ai = ar * S.y + ai * S.x;
-        ar = nar;
+      // (only complex64 input has a stash)
+      if (sizeof(TX) == sizeof(float2) && sx != nullptr) {
+        SumRun<TX, true>(sx, 0u, 0u, 0u, it.wtff, pw, t0, t1, S, a0.x, a0.y, &tr, &ti);
+      } else {
+        SumRun<TX, false>(reinterpret_cast<const TX *>(it.x), j, astep, nn, it.wtff, pw,
+                          t0, t1, S, a0.x, a0.y, &tr, &ti);
       }
     }
 #pragma unroll
