@@ -193,7 +193,16 @@ struct mpsft_rng {
   // and that it has not taken itself yet: taken before its next draw (a
   // reseed drops them)
   int64_t pending = 0;
+  // a reseed is applied to the engine at its next use (seeding fills the
+  // engine's whole state): a batched solve's working copies then seed
+  // themselves on the host threads that fill the draw tables, side by side
+  bool seed_pending = false;
+  int32_t seed_value = 0;
   void CatchUp() {
+    if (seed_pending) {
+      eng.seed(seed_value);
+      seed_pending = false;
+    }
     for (; pending > 0; --pending) uid(eng);
   }
   int32_t Draw() {
@@ -205,7 +214,8 @@ struct mpsft_rng {
     return nd(eng);
   }
   void Seed(int32_t seed) {
-    eng.seed(seed);
+    seed_pending = true;
+    seed_value = seed;
     pending = 0;
   }
 };
