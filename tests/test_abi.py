@@ -120,3 +120,21 @@ def test_mode_map_rejects_bad_arguments(lib):
     r = m.Rng(1)
     assert lib.mpsft_generate_mode_map(r._h, 10, 11, None, None) == m.ERR_INVALID
     assert lib.mpsft_generate_mode_map(None, 10, 1, None, None) == m.ERR_INVALID
+
+
+def test_batch_stats_sequence():
+    """solve_batched's per-signal stats: a read-only sequence of dicts, made
+    when read."""
+    import json
+
+    arr = (m.Stats * 3)()
+    arr[0].iterations, arr[2].iterations, arr[2].found = 4, 7, 5
+    st = m.BatchStats(arr)
+    assert len(st) == 3
+    assert st[2]["iterations"] == 7 and st[-1]["found"] == 5
+    assert [s["iterations"] for s in st] == [4, 0, 7]
+    assert [s["iterations"] for s in st[1:]] == [0, 7]
+    assert st == [a.as_dict() for a in arr]
+    assert json.loads(json.dumps(list(st)))[0]["iterations"] == 4
+    with pytest.raises(IndexError):
+        st[3]
